@@ -1,0 +1,161 @@
+/* psoci_gpu.h — C ABI of the GB300 Hamiltonian-build / Davidson-sigma library
+ * (libpsoci_gpu.so, built from psoci_gb300/csrc for sm_103a).
+ *
+ * The library replaces, on one GPU, the data-parallel path of PSOCI that runs from the
+ * determinant layer through the Davidson subspace step.  Each entry point names the
+ * reference interface it stands in for (paths inside psociRestart-Cori/).  Global Arrays /
+ * DRA storage becomes device arrays owned by the context; there are no MPI ranks.
+ *
+ * Conventions
+ *   - every function returns a psoci_status; none aborts the process;
+ *   - orbital, configuration and SEF indices are 0-based;
+ *   - one context = one device + one CUDA stream; calls on one context are not thread-safe;
+ *   - "host" pointers are ordinary host memory; the *_device variants take device pointers
+ *     valid on the context's device and run on the context's stream.
+ */
+#ifndef PSOCI_GPU_H
+#define PSOCI_GPU_H
+#include <stdint.h>
+#include <stddef.h>
+
+#if defined(__GNUC__)
+#define PSOCI_API __attribute__((visibility("default")))
+#else
+#define PSOCI_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  PSOCI_OK = 0,
+  PSOCI_ERR_INVALID_ARG = 1,  /* bad sizes, null pointers, out-of-range labels          */
+  PSOCI_ERR_UNSUPPORTED = 2,  /* > 11 open shells, nbf > 128, ... (reference limits)     */
+  PSOCI_ERR_STATE = 3,        /* call order violated (e.g. sigma before build)           */
+  PSOCI_ERR_CUDA = 4,         /* CUDA runtime error; psoci_last_error() has the text      */
+  PSOCI_ERR_NOMEM = 5,        /* device allocation failed                                 */
+  PSOCI_ERR_TIMEOUT = 6,      /* a bounded device-side wait ran out                       */
+  PSOCI_ERR_NOT_CONVERGED = 7,/* Davidson hit its iteration limit                         */
+  PSOCI_ERR_NUMERIC = 8,      /* NaN/Inf met in a residual or subspace matrix             */
+  PSOCI_ERR_IO = 9            /* file missing, truncated or of the wrong format           */
+} psoci_status;
+
+typedef struct psoci_ctx psoci_ctx;
+
+typedef struct {
+  int device;        /* CUDA device ordinal                                       */
+  int verbose;       /* 0 silent, 1 phase timings on stderr                        */
+} psoci_opts;
+
+/* Precision of the stored Hamiltonian used by sigma. */
+typedef enum {
+  PSOCI_PREC_FP64 = 0,   /* FP64 elements, FP64 products and sums                        */
+  PSOCI_PREC_MIXED = 1   /* FP32 elements and FP32 products, FP64 accumulation            */
+} psoci_prec;
+
+typedef enum {
+  PSOCI_HMODE_CSR_FP64 = 0,   /* stored FP64 CSR only                                   */
+  PSOCI_HMODE_CSR_BOTH = 1    /* stored FP64 CSR plus an FP32 copy of the elements      */
+} psoci_hmode;
+
+/* Replaces GA::Initialize + the PsociGAhamiltonian constructor
+ * (driver.PSOCI.splittest.C:296, PsociGAhamiltonian.C:269). */
+PSOCI_API psoci_status psoci_create(psoci_ctx **ctx, const psoci_opts *opts);
+/* Replaces PsociGAhamiltonian::destroyGAspace and friends. */
+PSOCI_API void psoci_destroy(psoci_ctx *ctx);
+PSOCI_API const char *psoci_status_str(psoci_status s);
+/* Text of the last error on this context (CUDA message, bad argument, ...). */
+PSOCI_API const char *psoci_last_error(const psoci_ctx *ctx);
+
+/* Replaces PsociIntegrals::fetchAndProcessIntegrals (PsociIntegrals.C:914-961) and the
+ * broadcast of the packed tables (:559, :780).
+ *   one_packed: nbf(nbf+1)/2 doubles, entry (i>=j) at i(i+1)/2+j, holding h_ij for equal
+ *               irreps and the spin-orbit value SO_ij (i>j) otherwise — the table layout
+ *               of PsociIntegrals.C:505-535;
+ *   eri_packed: canonical 8-fold table, NNDAF(NNDAF(nbf)) doubles (PsociIntegrals.C:889). */
+PSOCI_API psoci_status psoci_set_integrals(psoci_ctx *ctx, int nbf, const double *one_packed,
+                                 const double *eri_packed, double ecore);
+
+/* Replaces PsociConfigs::readConfigsToGA (PsociConfigs.C:336-496) once the file is parsed:
+ * nconf configurations in file order (SEF index = running sum of nsef in this order),
+ * occ = nconf*nbf bytes of 0/1/2, jsym = 1-based spatial symmetry per configuration.
+ * Unlike the reference (PsociConfigs.C:247), all-open-shell configurations are accepted. */
+PSOCI_API psoci_status psoci_set_configs(psoci_ctx *ctx, int nbf, int nelec, int ksym, int mx_open,
+                               int nconf, const int32_t *jsym, const uint8_t *occ);
+
+/* Replaces PsociGADeterminants::generateDistributedDeterminantsSmallMemoryGA
+ * (PsociGADeterminants.C:1608-1731) / PsociDeterminants::computeConfigs
+ * (PsociDeterminants.C:856-975) and computeNsefEntryPoints (PsociGAhamiltonian.C:4022).
+ * Builds determinant bit-strings, phases and spin projections on the device. */
+PSOCI_API psoci_status psoci_build_determinants(psoci_ctx *ctx);
+/* Counts after psoci_build_determinants. */
+PSOCI_API psoci_status psoci_get_counts(const psoci_ctx *ctx, int64_t *nsef_total, int64_t *ndet_total,
+                              int *max_nsef, int *max_ndet);
+/* Host copy of the determinant table, for parity checks.  Per determinant d:
+ * alpha[d*words+w], beta[d*words+w] (bit p = orbital p), phase[d] (0/1), ms[d]
+ * (the reference's spin_projection); detoff/sefoff: nconf+1 prefix sums.  words = ceil(nbf/64).
+ * Any output pointer may be NULL. */
+PSOCI_API psoci_status psoci_get_determinants(const psoci_ctx *ctx, uint64_t *alpha, uint64_t *beta,
+                                    uint8_t *phase, int32_t *ms, int64_t *detoff, int64_t *sefoff);
+
+/* Replaces PsociGAhamiltonian::constructGlobalHamiltonianAltOrbMapDirectChunkJmap
+ * (PsociGAhamiltonian.C:2530-2857) with packSefsef (:4077-4136): the full symmetric H in CSR
+ * (both triangles; each off-diagonal element is the reference's lower-triangle value), elements
+ * with |x| >= 1e-8 or on the diagonal.  *nnz receives the stored count. */
+PSOCI_API psoci_status psoci_build_hamiltonian(psoci_ctx *ctx, psoci_hmode mode, int64_t *nnz);
+/* Host copy of the CSR (rowptr[N+1], cols[nnz], vals[nnz]); NULLs allowed. */
+PSOCI_API psoci_status psoci_get_hamiltonian(const psoci_ctx *ctx, int64_t *rowptr, int32_t *cols, double *vals);
+/* Replaces PsociGAhamiltonian::fetchDIAG_SEF / fetchDiags (PsociGAhamiltonian.C:9014). */
+PSOCI_API psoci_status psoci_get_diag(const psoci_ctx *ctx, double *diag);
+
+/* Replaces PsociGAhamiltonian::matrixVectorProductsSplitChunkMultipleJchunks
+ * (PsociGAhamiltonian.C:6921-7270), k vectors at once.  X, Y: N x k, row-major (element
+ * (r, v) at r*k+v), host memory. */
+PSOCI_API psoci_status psoci_sigma(psoci_ctx *ctx, int k, const double *X, double *Y, psoci_prec prec);
+/* Same on device memory, rows of leading dimension ld (>= k), on the context stream. */
+PSOCI_API psoci_status psoci_sigma_device(psoci_ctx *ctx, int k, const double *dX, int ldx, double *dY,
+                                int ldy, psoci_prec prec);
+
+typedef struct {
+  int nroots;          /* roots wanted                                                  */
+  int max_subspace;    /* basis size that triggers a collapse (reference: 4*nroots)      */
+  int max_iter;        /* iteration limit (reference: 1000 per tolerance)                */
+  double rtol;         /* residual-norm tolerance for convergence                        */
+  psoci_prec prec;     /* sigma precision during the iterations                          */
+  int refine;          /* 1: FP64 sigma refinement pass after a MIXED run                */
+  int block;           /* 1: block Davidson (all unconverged roots per iteration);
+                          0: one new vector per iteration, as the reference does          */
+  double precond_min;  /* |D_i - lambda| guard of the preconditioner (reference 1e-3)     */
+} psoci_dav_opts;
+
+typedef struct {
+  int iterations;      /* Davidson iterations                                            */
+  int sigma_calls;     /* H*v products (counted per vector)                              */
+  int collapses;       /* subspace contractions                                          */
+  int refine_iters;    /* FP64 iterations after the mixed phase                          */
+  double seconds;      /* wall time of psoci_davidson                                    */
+  double sigma_seconds;/* device time inside sigma kernels                               */
+} psoci_dav_stats;
+
+/* Replaces the Davidson loop of driver.PSOCI.splittest.C:1186-1311 with
+ * PsociGAsubspace::generateIncrementalSubspace / diagSubspaceGOP / computeRnormSingle
+ * (PsociGAsubspace.C:273-366, :1088-1171, :874-1000) and PsociGAbasis precondition /
+ * orthonormalize / expandAndReplaceVectorsNew (PsociGAbasis.C:1860-1919, :1371-1474,
+ * :483-583).  Initial guess: unit vectors on the nroots lowest diagonal elements.
+ * evals[nroots] are electronic energies (add ecore for totals); evecs (N x nroots,
+ * column-major: root r at r*N) and rnorms[nroots] may be NULL. */
+PSOCI_API psoci_status psoci_davidson(psoci_ctx *ctx, const psoci_dav_opts *opts, double *evals,
+                            double *evecs, double *rnorms, psoci_dav_stats *stats);
+
+/* The cudaStream_t (as void*) that every kernel of this context is launched on, for callers
+ * that time or order work around the library's calls.  No reference counterpart. */
+PSOCI_API void *psoci_stream(const psoci_ctx *ctx);
+
+/* Core energy passed to psoci_set_integrals (PsociIntegrals::fetchCoreEnergy). */
+PSOCI_API double psoci_core_energy(const psoci_ctx *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PSOCI_GPU_H */

@@ -1,0 +1,259 @@
+"""Python host side over the C ABI of libpsoci_gpu.so (include/psoci_gpu.h).
+
+``Context`` owns one ``psoci_ctx`` (one GPU, one stream) and exposes the entry points with
+numpy arguments.  There is no CPU fallback: if the native library is missing, or no CUDA
+device is present, construction raises ``PsociError``.
+"""
+from __future__ import annotations
+
+import ctypes
+import dataclasses
+import os
+from typing import Optional
+
+import numpy as np
+
+from . import build as _build
+
+PSOCI_OK = 0
+STATUS = {
+    0: "ok", 1: "invalid argument", 2: "unsupported", 3: "call order", 4: "cuda error", 5: "out of device memory",
+    6: "device wait timed out", 7: "not converged", 8: "non-finite value", 9: "i/o error",
+}
+PREC_FP64, PREC_MIXED = 0, 1
+HMODE_CSR_FP64, HMODE_CSR_BOTH = 0, 1
+
+
+class PsociError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"{STATUS.get(status, status)}: {msg}")
+        self.status = status
+
+
+class _Opts(ctypes.Structure):
+    _fields_ = [("device", ctypes.c_int), ("verbose", ctypes.c_int)]
+
+
+class DavOpts(ctypes.Structure):
+    _fields_ = [("nroots", ctypes.c_int), ("max_subspace", ctypes.c_int), ("max_iter", ctypes.c_int),
+                ("rtol", ctypes.c_double), ("prec", ctypes.c_int), ("refine", ctypes.c_int), ("block", ctypes.c_int),
+                ("precond_min", ctypes.c_double)]
+
+
+class DavStats(ctypes.Structure):
+    _fields_ = [("iterations", ctypes.c_int), ("sigma_calls", ctypes.c_int), ("collapses", ctypes.c_int),
+                ("refine_iters", ctypes.c_int), ("seconds", ctypes.c_double), ("sigma_seconds", ctypes.c_double)]
+
+
+# every entry point of include/psoci_gpu.h: name -> (restype, argtypes)
+_P = ctypes.c_void_p
+_I64P = ctypes.POINTER(ctypes.c_int64)
+_I32P = ctypes.POINTER(ctypes.c_int32)
+_U64P = ctypes.POINTER(ctypes.c_uint64)
+_U8P = ctypes.POINTER(ctypes.c_uint8)
+_DP = ctypes.POINTER(ctypes.c_double)
+_IP = ctypes.POINTER(ctypes.c_int)
+SIGNATURES = {
+    "psoci_create": (ctypes.c_int, [ctypes.POINTER(_P), ctypes.POINTER(_Opts)]),
+    "psoci_destroy": (None, [_P]),
+    "psoci_status_str": (ctypes.c_char_p, [ctypes.c_int]),
+    "psoci_last_error": (ctypes.c_char_p, [_P]),
+    "psoci_set_integrals": (ctypes.c_int, [_P, ctypes.c_int, _DP, _DP, ctypes.c_double]),
+    "psoci_set_configs": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                         _I32P, _U8P]),
+    "psoci_build_determinants": (ctypes.c_int, [_P]),
+    "psoci_get_counts": (ctypes.c_int, [_P, _I64P, _I64P, _IP, _IP]),
+    "psoci_get_determinants": (ctypes.c_int, [_P, _U64P, _U64P, _U8P, _I32P, _I64P, _I64P]),
+    "psoci_build_hamiltonian": (ctypes.c_int, [_P, ctypes.c_int, _I64P]),
+    "psoci_get_hamiltonian": (ctypes.c_int, [_P, _I64P, _I32P, _DP]),
+    "psoci_get_diag": (ctypes.c_int, [_P, _DP]),
+    "psoci_sigma": (ctypes.c_int, [_P, ctypes.c_int, _DP, _DP, ctypes.c_int]),
+    "psoci_sigma_device": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
+                                          ctypes.c_int, ctypes.c_int]),
+    "psoci_davidson": (ctypes.c_int, [_P, ctypes.POINTER(DavOpts), _DP, _DP, _DP, ctypes.POINTER(DavStats)]),
+    "psoci_core_energy": (ctypes.c_double, [_P]),
+    "psoci_stream": (ctypes.c_void_p, [_P]),
+}
+
+_lib = None
+
+
+def load_library(build_if_missing: bool = True) -> ctypes.CDLL:
+    """Load libpsoci_gpu.so (building it in-tree when absent or stale)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = _build.LIB
+    if build_if_missing:
+        path = _build.build()
+    if not os.path.exists(path):
+        raise PsociError(4, f"native library {path} is missing; run psoci_gb300.build.build()")
+    lib = ctypes.CDLL(path)
+    for name, (res, args) in SIGNATURES.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = lib
+    return lib
+
+
+def _ptr(a: np.ndarray, t):
+    return a.ctypes.data_as(t)
+
+
+@dataclasses.dataclass
+class DavidsonResult:
+    evals: np.ndarray
+    evecs: Optional[np.ndarray]
+    rnorms: np.ndarray
+    iterations: int
+    sigma_calls: int
+    collapses: int
+    refine_iters: int
+    seconds: float
+    sigma_seconds: float
+
+
+class Context:
+    """One GPU context: integrals, configurations, determinants, H, Davidson."""
+
+    def __init__(self, device: int = 0, verbose: int = 0):
+        self.lib = load_library()
+        self.ctx = _P()
+        opts = _Opts(device, verbose)
+        st = self.lib.psoci_create(ctypes.byref(self.ctx), ctypes.byref(opts))
+        if st != PSOCI_OK:
+            raise PsociError(st, "psoci_create failed (no CUDA device?)")
+        self.nsef = 0
+        self.nnz = 0
+
+    def close(self):
+        if getattr(self, "ctx", None):
+            self.lib.psoci_destroy(self.ctx)
+            self.ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _check(self, st: int, what: str):
+        if st != PSOCI_OK:
+            msg = self.lib.psoci_last_error(self.ctx)
+            raise PsociError(st, f"{what}: {msg.decode() if msg else ''}")
+
+    # -- inputs ------------------------------------------------------------------------
+    def set_integrals(self, nbf: int, one_packed: np.ndarray, eri_packed: np.ndarray, ecore: float = 0.0):
+        one = np.ascontiguousarray(one_packed, np.float64)
+        eri = np.ascontiguousarray(eri_packed, np.float64)
+        self._check(self.lib.psoci_set_integrals(self.ctx, nbf, _ptr(one, _DP), _ptr(eri, _DP), float(ecore)),
+                    "set_integrals")
+
+    def set_configs(self, nbf, nelec, ksym, mx_open, jsym, occ):
+        js = np.ascontiguousarray(jsym, np.int32)
+        oc = np.ascontiguousarray(occ, np.uint8)
+        self._check(self.lib.psoci_set_configs(self.ctx, nbf, nelec, ksym, mx_open, len(js), _ptr(js, _I32P),
+                                               _ptr(oc, _U8P)), "set_configs")
+
+    def load_problem(self, p):
+        """Integrals and configurations of an inputs.Problem."""
+        self.set_integrals(p.nbf, p.one_packed(), p.eri, p.ecore)
+        self.set_configs(p.nbf, p.nelec, p.ksym, p.mx_open, p.jsym, p.occ)
+
+    # -- determinants --------------------------------------------------------------------
+    def build_determinants(self):
+        self._check(self.lib.psoci_build_determinants(self.ctx), "build_determinants")
+        nsef, ndet = ctypes.c_int64(), ctypes.c_int64()
+        ms, md = ctypes.c_int(), ctypes.c_int()
+        self._check(self.lib.psoci_get_counts(self.ctx, ctypes.byref(nsef), ctypes.byref(ndet), ctypes.byref(ms),
+                                              ctypes.byref(md)), "get_counts")
+        self.nsef, self.ndet = nsef.value, ndet.value
+        return self.nsef, self.ndet
+
+    def get_determinants(self, nconf: int, nbf: int):
+        words = (nbf + 63) // 64
+        a = np.zeros(self.ndet * words, np.uint64)
+        b = np.zeros(self.ndet * words, np.uint64)
+        ph = np.zeros(self.ndet, np.uint8)
+        ms = np.zeros(self.ndet, np.int32)
+        do = np.zeros(nconf + 1, np.int64)
+        so = np.zeros(nconf + 1, np.int64)
+        self._check(self.lib.psoci_get_determinants(self.ctx, _ptr(a, _U64P), _ptr(b, _U64P), _ptr(ph, _U8P),
+                                                    _ptr(ms, _I32P), _ptr(do, _I64P), _ptr(so, _I64P)),
+                    "get_determinants")
+        return dict(alpha=a.reshape(-1, words), beta=b.reshape(-1, words), phase=ph, ms=ms, detoff=do, sefoff=so)
+
+    # -- Hamiltonian ---------------------------------------------------------------------
+    def build_hamiltonian(self, mixed: bool = True) -> int:
+        nnz = ctypes.c_int64()
+        self._check(self.lib.psoci_build_hamiltonian(self.ctx, HMODE_CSR_BOTH if mixed else HMODE_CSR_FP64,
+                                                     ctypes.byref(nnz)), "build_hamiltonian")
+        self.nnz = nnz.value
+        return self.nnz
+
+    def get_hamiltonian(self):
+        rp = np.zeros(self.nsef + 1, np.int64)
+        ci = np.zeros(max(self.nnz, 1), np.int32)
+        va = np.zeros(max(self.nnz, 1), np.float64)
+        self._check(self.lib.psoci_get_hamiltonian(self.ctx, _ptr(rp, _I64P), _ptr(ci, _I32P), _ptr(va, _DP)),
+                    "get_hamiltonian")
+        return rp, ci[:self.nnz], va[:self.nnz]
+
+    def get_diag(self):
+        d = np.zeros(self.nsef)
+        self._check(self.lib.psoci_get_diag(self.ctx, _ptr(d, _DP)), "get_diag")
+        return d
+
+    # -- sigma ---------------------------------------------------------------------------
+    def sigma(self, X: np.ndarray, prec: int = PREC_FP64) -> np.ndarray:
+        """Y = H X for X of shape [N, k] (row-major), host memory."""
+        X = np.ascontiguousarray(X, np.float64)
+        if X.ndim == 1:
+            X = X[:, None]
+        Y = np.zeros_like(X)
+        self._check(self.lib.psoci_sigma(self.ctx, X.shape[1], _ptr(X, _DP), _ptr(Y, _DP), prec), "sigma")
+        return Y
+
+    def sigma_device(self, dX_ptr: int, ldx: int, dY_ptr: int, ldy: int, k: int, prec: int = PREC_FP64):
+        self._check(self.lib.psoci_sigma_device(self.ctx, k, ctypes.c_void_p(dX_ptr), ldx, ctypes.c_void_p(dY_ptr), ldy,
+                                                prec), "sigma_device")
+
+    # -- Davidson ------------------------------------------------------------------------
+    def davidson(self, nroots: int, rtol: float = 1e-6, mixed: bool = False, refine: bool = True,
+                 block: bool = True, max_subspace: int = 0, max_iter: int = 1000, want_vectors: bool = False,
+                 precond_min: float = 1e-3) -> DavidsonResult:
+        o = DavOpts(nroots, max_subspace, max_iter, rtol, PREC_MIXED if mixed else PREC_FP64, int(refine), int(block),
+                    precond_min)
+        ev = np.zeros(nroots)
+        rn = np.zeros(nroots)
+        vec = np.zeros((nroots, self.nsef)) if want_vectors else None
+        stats = DavStats()
+        st = self.lib.psoci_davidson(self.ctx, ctypes.byref(o), _ptr(ev, _DP),
+                                     _ptr(vec, _DP) if vec is not None else None, _ptr(rn, _DP), ctypes.byref(stats))
+        self._check(st, "davidson")
+        return DavidsonResult(ev, vec, rn, stats.iterations, stats.sigma_calls, stats.collapses, stats.refine_iters,
+                              stats.seconds, stats.sigma_seconds)
+
+    def core_energy(self) -> float:
+        return self.lib.psoci_core_energy(self.ctx)
+
+    def stream_handle(self) -> int:
+        """cudaStream_t of this context (for CUDA events on the launching stream)."""
+        return int(self.lib.psoci_stream(self.ctx) or 0)
+
+
+def solve(problem, nroots: int = 8, mixed: bool = True, rtol: float = 1e-6, device: int = 0, verbose: int = 0,
+          **kw) -> DavidsonResult:
+    """End to end: host inputs -> determinants -> H -> Davidson -> eigenvalues on the host."""
+    with Context(device, verbose) as c:
+        c.load_problem(problem)
+        c.build_determinants()
+        c.build_hamiltonian(mixed=mixed)
+        return c.davidson(nroots, rtol=rtol, mixed=mixed, **kw)

@@ -1,0 +1,276 @@
+// C ABI of libpsoci_gpu.so (declared in include/psoci_gpu.h).
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "psoci_internal.cuh"
+
+psoci_status psoci_davidson_impl(psoci_ctx *c, const psoci_dav_opts *o, double *evals, double *evecs, double *rnorms,
+                                 psoci_dav_stats *stats);
+
+namespace {
+psoci_status set_device(psoci_ctx *c) {
+  PSOCI_CUDA(c, cudaSetDevice(c->device));
+  return PSOCI_OK;
+}
+void release_all(psoci_ctx *c) {
+  psoci_h_release(c);
+  psoci_dets_release(c);
+  psoci_free(c->d_one);
+  psoci_free(c->d_eri);
+  psoci_free(c->d_e1);
+  psoci_free(c->d_e2);
+  psoci_free(c->d_jsym);
+  psoci_free(c->d_nopen);
+  psoci_free(c->d_x);
+  psoci_free(c->d_y);
+  psoci_free(c->d_x32);
+}
+}  // namespace
+
+extern "C" {
+
+const char *psoci_status_str(psoci_status s) {
+  switch (s) {
+    case PSOCI_OK: return "ok";
+    case PSOCI_ERR_INVALID_ARG: return "invalid argument";
+    case PSOCI_ERR_UNSUPPORTED: return "unsupported";
+    case PSOCI_ERR_STATE: return "call order";
+    case PSOCI_ERR_CUDA: return "cuda error";
+    case PSOCI_ERR_NOMEM: return "out of device memory";
+    case PSOCI_ERR_TIMEOUT: return "device wait timed out";
+    case PSOCI_ERR_NOT_CONVERGED: return "not converged";
+    case PSOCI_ERR_NUMERIC: return "non-finite value";
+    case PSOCI_ERR_IO: return "i/o error";
+  }
+  return "unknown status";
+}
+
+const char *psoci_last_error(const psoci_ctx *c) { return c ? c->err.c_str() : "null context"; }
+
+psoci_status psoci_create(psoci_ctx **out, const psoci_opts *opts) {
+  if (!out) return PSOCI_ERR_INVALID_ARG;
+  *out = nullptr;
+  psoci_ctx *c = new psoci_ctx();
+  c->device = opts ? opts->device : 0;
+  c->verbose = opts ? opts->verbose : 0;
+  int ndev = 0;
+  cudaError_t e = cudaGetDeviceCount(&ndev);
+  if (e != cudaSuccess || ndev == 0) {
+    cudaGetLastError();
+    delete c;
+    return PSOCI_ERR_CUDA;
+  }
+  if (c->device < 0 || c->device >= ndev) {
+    delete c;
+    return PSOCI_ERR_INVALID_ARG;
+  }
+  if (cudaSetDevice(c->device) != cudaSuccess || cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    cudaGetLastError();
+    delete c;
+    return PSOCI_ERR_CUDA;
+  }
+  *out = c;
+  return PSOCI_OK;
+}
+
+void psoci_destroy(psoci_ctx *c) {
+  if (!c) return;
+  cudaSetDevice(c->device);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  release_all(c);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+}
+
+double psoci_core_energy(const psoci_ctx *c) { return c ? c->ecore : 0.0; }
+
+void *psoci_stream(const psoci_ctx *c) { return c ? (void *)c->stream : nullptr; }
+
+psoci_status psoci_set_integrals(psoci_ctx *c, int nbf, const double *one, const double *eri, double ecore) {
+  if (!c) return PSOCI_ERR_INVALID_ARG;
+  if (nbf < 1 || !one || !eri) return psoci_fail(c, PSOCI_ERR_INVALID_ARG, "set_integrals: bad arguments");
+  if (nbf > 64 * PSOCI_MAX_WORDS) return psoci_fail(c, PSOCI_ERR_UNSUPPORTED, "set_integrals: nbf > 128");
+  if (c->have_cfgs && c->nbf != nbf) return psoci_fail(c, PSOCI_ERR_INVALID_ARG, "set_integrals: nbf differs from configurations");
+  psoci_status s;
+  if ((s = set_device(c))) return s;
+  psoci_h_release(c);
+  int64_t n1 = (int64_t)nbf * (nbf + 1) / 2, n2 = n1 * (n1 + 1) / 2;
+  if ((s = psoci_alloc(c, &c->d_one, n1)) || (s = psoci_alloc(c, &c->d_eri, n2))) return s;
+  PSOCI_CUDA(c, cudaMemcpyAsync(c->d_one, one, sizeof(double) * n1, cudaMemcpyHostToDevice, c->stream));
+  PSOCI_CUDA(c, cudaMemcpyAsync(c->d_eri, eri, sizeof(double) * n2, cudaMemcpyHostToDevice, c->stream));
+  PSOCI_CUDA(c, cudaStreamSynchronize(c->stream));
+  c->nbf = nbf;
+  c->n1 = n1;
+  c->n2 = n2;
+  c->ecore = ecore;
+  c->have_ints = true;
+  return PSOCI_OK;
+}
+
+psoci_status psoci_set_configs(psoci_ctx *c, int nbf, int nelec, int ksym, int mx_open, int nconf, const int32_t *jsym,
+                               const uint8_t *occ) {
+  if (!c) return PSOCI_ERR_INVALID_ARG;
+  if (nbf < 1 || nelec < 1 || nconf < 1 || !jsym || !occ || ksym < 1 || mx_open < 0)
+    return psoci_fail(c, PSOCI_ERR_INVALID_ARG, "set_configs: bad arguments");
+  if (nbf > 64 * PSOCI_MAX_WORDS) return psoci_fail(c, PSOCI_ERR_UNSUPPORTED, "set_configs: nbf > 128");
+  if (c->have_ints && c->nbf != nbf) return psoci_fail(c, PSOCI_ERR_INVALID_ARG, "set_configs: nbf differs from integrals");
+  const int W = (nbf + 63) / 64;
+  std::vector<uint64_t> e1((size_t)nconf * W, 0), e2((size_t)nconf * W, 0);
+  std::vector<int32_t> nopen(nconf);
+  for (int i = 0; i < nconf; ++i) {
+    const uint8_t *o = occ + (size_t)i * nbf;
+    int ne = 0, no = 0;
+    for (int p = 0; p < nbf; ++p) {
+      if (o[p] > 2) {
+        char b[128];
+        snprintf(b, sizeof(b), "set_configs: configuration %d orbital %d occupation %d", i, p, (int)o[p]);
+        return psoci_fail(c, PSOCI_ERR_INVALID_ARG, b);
+      }
+      ne += o[p];
+      no += (o[p] == 1);
+      if (o[p] >= 1) e1[(size_t)i * W + p / 64] |= 1ull << (p % 64);
+      if (o[p] == 2) e2[(size_t)i * W + p / 64] |= 1ull << (p % 64);
+    }
+    if (ne != nelec) {
+      char b[128];
+      snprintf(b, sizeof(b), "set_configs: configuration %d holds %d electrons, expected %d", i, ne, nelec);
+      return psoci_fail(c, PSOCI_ERR_INVALID_ARG, b);
+    }
+    if (no > PSOCI_MAX_OPEN) return psoci_fail(c, PSOCI_ERR_UNSUPPORTED, "set_configs: more than 11 open shells");
+    if (jsym[i] < 1) return psoci_fail(c, PSOCI_ERR_INVALID_ARG, "set_configs: jsym labels are 1-based");
+    nopen[i] = no;
+  }
+  psoci_status s;
+  if ((s = set_device(c))) return s;
+  psoci_h_release(c);
+  psoci_dets_release(c);
+  if ((s = psoci_alloc(c, &c->d_e1, e1.size())) || (s = psoci_alloc(c, &c->d_e2, e2.size())) ||
+      (s = psoci_alloc(c, &c->d_jsym, nconf)) || (s = psoci_alloc(c, &c->d_nopen, nconf)))
+    return s;
+  PSOCI_CUDA(c, cudaMemcpyAsync(c->d_e1, e1.data(), sizeof(uint64_t) * e1.size(), cudaMemcpyHostToDevice, c->stream));
+  PSOCI_CUDA(c, cudaMemcpyAsync(c->d_e2, e2.data(), sizeof(uint64_t) * e2.size(), cudaMemcpyHostToDevice, c->stream));
+  PSOCI_CUDA(c, cudaMemcpyAsync(c->d_jsym, jsym, sizeof(int32_t) * nconf, cudaMemcpyHostToDevice, c->stream));
+  PSOCI_CUDA(c, cudaMemcpyAsync(c->d_nopen, nopen.data(), sizeof(int32_t) * nconf, cudaMemcpyHostToDevice, c->stream));
+  PSOCI_CUDA(c, cudaStreamSynchronize(c->stream));
+  c->nbf = nbf;
+  c->nelec = nelec;
+  c->ksym = ksym;
+  c->mx_open = mx_open;
+  c->nconf = nconf;
+  c->words = W;
+  c->h_jsym.assign(jsym, jsym + nconf);
+  c->h_occ.assign(occ, occ + (size_t)nconf * nbf);
+  c->have_cfgs = true;
+  return PSOCI_OK;
+}
+
+psoci_status psoci_build_determinants(psoci_ctx *c) {
+  if (!c) return PSOCI_ERR_INVALID_ARG;
+  psoci_status s;
+  if ((s = set_device(c))) return s;
+  return psoci_dets_build(c);
+}
+
+psoci_status psoci_get_counts(const psoci_ctx *c, int64_t *nsef, int64_t *ndet, int *max_nsef, int *max_ndet) {
+  if (!c) return PSOCI_ERR_INVALID_ARG;
+  if (!c->have_dets) return PSOCI_ERR_STATE;
+  if (nsef) *nsef = c->nsef_total;
+  if (ndet) *ndet = c->ndet_total;
+  if (max_nsef) *max_nsef = c->max_nsef;
+  if (max_ndet) *max_ndet = c->max_ndet;
+  return PSOCI_OK;
+}
+
+psoci_status psoci_get_determinants(const psoci_ctx *cc, uint64_t *alpha, uint64_t *beta, uint8_t *phase, int32_t *ms,
+                                    int64_t *detoff, int64_t *sefoff) {
+  psoci_ctx *c = const_cast<psoci_ctx *>(cc);
+  if (!c) return PSOCI_ERR_INVALID_ARG;
+  if (!c->have_dets) return psoci_fail(c, PSOCI_ERR_STATE, "get_determinants: not built");
+  psoci_status s;
+  if ((s = set_device(c))) return s;
+  size_t nd = (size_t)c->ndet_total;
+  if (alpha) PSOCI_CUDA(c, cudaMemcpy(alpha, c->d_alpha, sizeof(uint64_t) * nd * c->words, cudaMemcpyDeviceToHost));
+  if (beta) PSOCI_CUDA(c, cudaMemcpy(beta, c->d_beta, sizeof(uint64_t) * nd * c->words, cudaMemcpyDeviceToHost));
+  if (phase) PSOCI_CUDA(c, cudaMemcpy(phase, c->d_phase, nd, cudaMemcpyDeviceToHost));
+  if (ms) PSOCI_CUDA(c, cudaMemcpy(ms, c->d_ms, sizeof(int32_t) * nd, cudaMemcpyDeviceToHost));
+  if (detoff) memcpy(detoff, c->h_detoff.data(), sizeof(int64_t) * (c->nconf + 1));
+  if (sefoff) memcpy(sefoff, c->h_sefoff.data(), sizeof(int64_t) * (c->nconf + 1));
+  return PSOCI_OK;
+}
+
+psoci_status psoci_build_hamiltonian(psoci_ctx *c, psoci_hmode mode, int64_t *nnz) {
+  if (!c) return PSOCI_ERR_INVALID_ARG;
+  if (mode != PSOCI_HMODE_CSR_FP64 && mode != PSOCI_HMODE_CSR_BOTH)
+    return psoci_fail(c, PSOCI_ERR_INVALID_ARG, "build_hamiltonian: unknown mode");
+  psoci_status s;
+  if ((s = set_device(c))) return s;
+  int64_t n = 0;
+  s = psoci_h_build(c, mode, &n);
+  if (nnz) *nnz = (s == PSOCI_OK) ? n : 0;
+  return s;
+}
+
+psoci_status psoci_get_hamiltonian(const psoci_ctx *cc, int64_t *rowptr, int32_t *cols, double *vals) {
+  psoci_ctx *c = const_cast<psoci_ctx *>(cc);
+  if (!c) return PSOCI_ERR_INVALID_ARG;
+  if (!c->have_h) return psoci_fail(c, PSOCI_ERR_STATE, "get_hamiltonian: not built");
+  psoci_status s;
+  if ((s = set_device(c))) return s;
+  if (rowptr)
+    PSOCI_CUDA(c, cudaMemcpy(rowptr, c->d_rowptr, sizeof(int64_t) * (c->nsef_total + 1), cudaMemcpyDeviceToHost));
+  if (cols) PSOCI_CUDA(c, cudaMemcpy(cols, c->d_col, sizeof(int32_t) * c->nnz, cudaMemcpyDeviceToHost));
+  if (vals) PSOCI_CUDA(c, cudaMemcpy(vals, c->d_val, sizeof(double) * c->nnz, cudaMemcpyDeviceToHost));
+  return PSOCI_OK;
+}
+
+psoci_status psoci_get_diag(const psoci_ctx *cc, double *diag) {
+  psoci_ctx *c = const_cast<psoci_ctx *>(cc);
+  if (!c || !diag) return PSOCI_ERR_INVALID_ARG;
+  if (!c->have_h) return psoci_fail(c, PSOCI_ERR_STATE, "get_diag: not built");
+  psoci_status s;
+  if ((s = set_device(c))) return s;
+  PSOCI_CUDA(c, cudaMemcpy(diag, c->d_diag, sizeof(double) * c->nsef_total, cudaMemcpyDeviceToHost));
+  return PSOCI_OK;
+}
+
+psoci_status psoci_sigma_device(psoci_ctx *c, int k, const double *dX, int ldx, double *dY, int ldy, psoci_prec prec) {
+  if (!c || !dX || !dY) return PSOCI_ERR_INVALID_ARG;
+  psoci_status s;
+  if ((s = set_device(c))) return s;
+  if (prec == PSOCI_PREC_MIXED) {
+    size_t need = (size_t)c->nsef_total * 8;
+    if (c->x32_cap < need) {
+      if ((s = psoci_alloc(c, &c->d_x32, need))) return s;
+      c->x32_cap = need;
+    }
+  }
+  return psoci_sigma_launch(c, k, dX, ldx, dY, ldy, prec, c->d_x32);
+}
+
+psoci_status psoci_sigma(psoci_ctx *c, int k, const double *X, double *Y, psoci_prec prec) {
+  if (!c || !X || !Y || k < 1) return PSOCI_ERR_INVALID_ARG;
+  if (!c->have_h) return psoci_fail(c, PSOCI_ERR_STATE, "sigma: Hamiltonian not built");
+  psoci_status s;
+  if ((s = set_device(c))) return s;
+  size_t need = (size_t)c->nsef_total * k;
+  if (c->xy_cap < need) {
+    if ((s = psoci_alloc(c, &c->d_x, need)) || (s = psoci_alloc(c, &c->d_y, need))) return s;
+    c->xy_cap = need;
+  }
+  PSOCI_CUDA(c, cudaMemcpyAsync(c->d_x, X, sizeof(double) * need, cudaMemcpyHostToDevice, c->stream));
+  if ((s = psoci_sigma_device(c, k, c->d_x, k, c->d_y, k, prec))) return s;
+  PSOCI_CUDA(c, cudaMemcpyAsync(Y, c->d_y, sizeof(double) * need, cudaMemcpyDeviceToHost, c->stream));
+  PSOCI_CUDA(c, cudaStreamSynchronize(c->stream));
+  return PSOCI_OK;
+}
+
+psoci_status psoci_davidson(psoci_ctx *c, const psoci_dav_opts *opts, double *evals, double *evecs, double *rnorms,
+                            psoci_dav_stats *stats) {
+  if (!c) return PSOCI_ERR_INVALID_ARG;
+  psoci_status s;
+  if ((s = set_device(c))) return s;
+  return psoci_davidson_impl(c, opts, evals, evecs, rnorms, stats);
+}
+
+}  // extern "C"

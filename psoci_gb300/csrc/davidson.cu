@@ -1,0 +1,639 @@
+// Davidson eigensolver on the device.
+//
+// Reference flow (psociRestart-Cori/): driver.PSOCI.splittest.C:1186-1311 with
+//   PsociGAsubspace::generateIncrementalSubspace (PsociGAsubspace.C:273-366)  S, G columns
+//   PsociGAsubspace::diagSubspaceGOP (:1088-1171) -> dsygv                     Rayleigh-Ritz
+//   PsociGAsubspace::computeRnormSingle (:874-1000)                            residual
+//   PsociGAbasis::precondition (PsociGAbasis.C:1860-1919)   t_i = r_i/(D_i-l) if |D_i-l| > 1e-3
+//   PsociGAbasis::orthonormalizeAppendedVectors (:1371-1474)                   Gram-Schmidt
+//   PsociGAbasis::expandAndReplaceVectorsNew (:483-583)   collapse V and HV, no recompute
+//
+// The reference adds one vector per iteration, for the first unconverged root.  Here the
+// default is block Davidson: every unconverged root contributes a preconditioned residual
+// each iteration, so one pass over H serves the whole block (block = 0 keeps the
+// reference's one-vector step).  The basis is kept orthonormal (CGS2 against V, then
+// Cholesky-QR twice inside the new block), so S = I and the generalised problem of the
+// reference reduces to a symmetric one, solved by a one-CTA cyclic Jacobi in FP64.
+//
+// Vectors are N x ld row-major: the k entries of one SEF row are contiguous, which is
+// what the sigma kernel gathers.  All subspace arithmetic is FP64.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <numeric>
+#include <vector>
+
+#include "psoci_internal.cuh"
+
+namespace {
+
+constexpr int TN_THREADS = 256;
+constexpr int TN_ROWS = 32;       // rows staged per tile
+constexpr int TN_MAXOUT = 8;      // outputs per thread => m*k <= 2048
+constexpr int NN_THREADS = 256;
+constexpr int MAX_SUB = 96;       // Jacobi keeps two m x m FP64 matrices in shared memory
+
+// C_partial[blk][i*k + j] = sum over the block's rows of A[r, a0+i] * B[r, b0+j]
+__global__ void __launch_bounds__(TN_THREADS) k_tn(int64_t n, const double *__restrict__ A, int lda, int a0, int m,
+                                                   const double *__restrict__ B, int ldb, int b0, int k,
+                                                   double *__restrict__ partial, int64_t rows_per_blk) {
+  extern __shared__ double sm[];
+  double *As = sm;                 // [TN_ROWS][m]
+  double *Bs = sm + TN_ROWS * m;   // [TN_ROWS][k]
+  const int nout = m * k;
+  double acc[TN_MAXOUT];
+#pragma unroll
+  for (int o = 0; o < TN_MAXOUT; ++o) acc[o] = 0.0;
+  int64_t r0 = (int64_t)blockIdx.x * rows_per_blk;
+  int64_t r1 = min(n, r0 + rows_per_blk);
+  for (int64_t rt = r0; rt < r1; rt += TN_ROWS) {
+    int rows = (int)min((int64_t)TN_ROWS, r1 - rt);
+    for (int e = threadIdx.x; e < TN_ROWS * m; e += blockDim.x) {
+      int rr = e / m, i = e - rr * m;
+      As[e] = (rr < rows) ? A[(rt + rr) * lda + a0 + i] : 0.0;
+    }
+    for (int e = threadIdx.x; e < TN_ROWS * k; e += blockDim.x) {
+      int rr = e / k, j = e - rr * k;
+      Bs[e] = (rr < rows) ? B[(rt + rr) * ldb + b0 + j] : 0.0;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int o = 0; o < TN_MAXOUT; ++o) {
+      int idx = threadIdx.x + o * TN_THREADS;
+      if (idx < nout) {
+        int i = idx / k, j = idx - i * k;
+        double s = acc[o];
+        for (int rr = 0; rr < rows; ++rr) s = fma(As[rr * m + i], Bs[rr * k + j], s);
+        acc[o] = s;
+      }
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int o = 0; o < TN_MAXOUT; ++o) {
+    int idx = threadIdx.x + o * TN_THREADS;
+    if (idx < nout) partial[(int64_t)blockIdx.x * nout + idx] = acc[o];
+  }
+}
+
+// C[i*ldc + c0 + j] = sum_b partial[b][i*k + j]   (fixed order: deterministic)
+__global__ void k_reduce_partials(const double *__restrict__ partial, int nblk, int m, int k, double *C, int ldc,
+                                  int c0) {
+  int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= m * k) return;
+  double s = 0.0;
+  for (int b = 0; b < nblk; ++b) s += partial[(int64_t)b * m * k + idx];
+  int i = idx / k, j = idx - i * k;
+  C[i * ldc + c0 + j] = s;
+}
+
+// Out[r, o0+j] = beta*Out[r, o0+j] + alpha * sum_i A[r, a0+i] * Y[i*ldy + y0 + j]
+__global__ void __launch_bounds__(NN_THREADS) k_nn(int64_t n, const double *__restrict__ A, int lda, int a0, int m,
+                                                   const double *__restrict__ Y, int ldy, int y0, int k, double alpha,
+                                                   double beta, double *Out, int ldo, int o0) {
+  extern __shared__ double sm[];
+  double *Ys = sm;              // [m][k]
+  double *As = sm + m * k;      // [32][m]
+  for (int e = threadIdx.x; e < m * k; e += blockDim.x) {
+    int i = e / k, j = e - i * k;
+    Ys[e] = Y[i * ldy + y0 + j];
+  }
+  __syncthreads();
+  for (int64_t rt = (int64_t)blockIdx.x * 32; rt < n; rt += (int64_t)gridDim.x * 32) {
+    int rows = (int)min((int64_t)32, n - rt);
+    for (int e = threadIdx.x; e < 32 * m; e += blockDim.x) {
+      int rr = e / m, i = e - rr * m;
+      As[e] = (rr < rows) ? A[(rt + rr) * lda + a0 + i] : 0.0;
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < 32 * k; e += blockDim.x) {
+      int rr = e / k, j = e - rr * k;
+      if (rr < rows) {
+        double s = 0.0;
+        for (int i = 0; i < m; ++i) s = fma(As[rr * m + i], Ys[i * k + j], s);
+        double *o = Out + (rt + rr) * ldo + o0 + j;
+        *o = (beta == 0.0) ? alpha * s : fma(beta, *o, alpha * s);
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// R[r, j] = HX[r, j] - theta[j] * X[r, j]; partial squared norms per block
+__global__ void k_residual(int64_t n, int nr, const double *__restrict__ X, const double *__restrict__ HX,
+                           const double *__restrict__ theta, double *__restrict__ R, double *__restrict__ partial) {
+  __shared__ double red[256];
+  for (int j = 0; j < nr; ++j) {
+    double th = theta[j];
+    double s = 0.0;
+    for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+      double v = HX[r * nr + j] - th * X[r * nr + j];
+      R[r * nr + j] = v;
+      s = fma(v, v, s);
+    }
+    red[threadIdx.x] = s;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+      if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) partial[(int64_t)blockIdx.x * nr + j] = red[0];
+    __syncthreads();
+  }
+}
+
+__global__ void k_sum_cols(const double *partial, int nblk, int nr, double *out) {
+  int j = threadIdx.x;
+  if (j >= nr) return;
+  double s = 0.0;
+  for (int b = 0; b < nblk; ++b) s += partial[(int64_t)b * nr + j];
+  out[j] = s;
+}
+
+// T[r, c] = R[r, sel[c]] / (D[r] - theta[sel[c]]) where |D - theta| > dmin, else R
+__global__ void k_precond(int64_t n, int nr, const double *__restrict__ R, const double *__restrict__ D,
+                          const double *__restrict__ theta, const int *__restrict__ sel, int nsel, double dmin,
+                          double *__restrict__ T, int ldt) {
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n * nsel; e += (int64_t)gridDim.x * blockDim.x) {
+    int64_t r = e / nsel;
+    int c = (int)(e - r * nsel);
+    int j = sel[c];
+    double v = R[r * nr + j];
+    double d = D[r] - theta[j];
+    if (fabs(d) > dmin) v = v / d;
+    T[r * ldt + c] = v;
+  }
+}
+
+// Gram matrix S (b x b) -> upper-triangular inverse factor F (b x b'), columns of kept
+// vectors compacted, so that T * F has orthonormal columns.  Drops a column whose
+// Cholesky pivot falls below drop_tol^2 of its original norm (linear dependence).
+__global__ void k_cholqr_factor(const double *S, int b, const double *ref, int ldref, double drop_tol, double *F,
+                                int *nkept) {
+  __shared__ double Finv[16 * 16];
+  __shared__ int keep[16];
+  if (threadIdx.x != 0) return;
+  // Cholesky S = R^T R with R upper; dropped columns get zero rows
+  double Rm[16][16];
+  for (int i = 0; i < b; ++i)
+    for (int j = 0; j < b; ++j) Rm[i][j] = 0.0;
+  int nk = 0;
+  for (int j = 0; j < b; ++j) {
+    double s = S[j * b + j];
+    double orig = ref ? ref[j * ldref + j] : s;
+    for (int i = 0; i < j; ++i) s -= Rm[i][j] * Rm[i][j];
+    if (!(orig > 0.0) || s <= drop_tol * drop_tol * orig || !(s > 0.0)) {
+      keep[j] = 0;
+      continue;
+    }
+    keep[j] = 1;
+    ++nk;
+    double rjj = sqrt(s);
+    Rm[j][j] = rjj;
+    for (int c = j + 1; c < b; ++c) {
+      double t = S[j * b + c];
+      for (int i = 0; i < j; ++i) t -= Rm[i][j] * Rm[i][c];
+      Rm[j][c] = t / rjj;
+    }
+  }
+  // invert the kept upper-triangular part: F = R^{-1} restricted to kept rows/cols
+  for (int i = 0; i < b * b; ++i) Finv[i] = 0.0;
+  for (int j = 0; j < b; ++j) {
+    if (!keep[j]) continue;
+    Finv[j * b + j] = 1.0 / Rm[j][j];
+    for (int i = j - 1; i >= 0; --i) {
+      if (!keep[i]) continue;
+      double t = 0.0;
+      for (int q = i + 1; q <= j; ++q)
+        if (keep[q]) t += Rm[i][q] * Finv[q * b + j];
+      Finv[i * b + j] = -t / Rm[i][i];
+    }
+  }
+  // compact kept columns
+  int c = 0;
+  for (int j = 0; j < b; ++j) {
+    if (!keep[j]) continue;
+    for (int i = 0; i < b; ++i) F[i * b + c] = Finv[i * b + j];
+    ++c;
+  }
+  for (; c < b; ++c)
+    for (int i = 0; i < b; ++i) F[i * b + c] = 0.0;
+  *nkept = nk;
+}
+
+// G (ld x ld): mirror new columns [m0, m1) into rows and symmetrise the new diagonal block
+__global__ void k_symmetrize(double *G, int ld, int m0, int m1) {
+  for (int e = threadIdx.x; e < m1 * (m1 - m0); e += blockDim.x) {
+    int i = e / (m1 - m0), j = m0 + e % (m1 - m0);
+    if (i < m0) G[j * ld + i] = G[i * ld + j];
+    else if (i < j) {
+      double a = 0.5 * (G[i * ld + j] + G[j * ld + i]);
+      G[i * ld + j] = a;
+      G[j * ld + i] = a;
+    }
+  }
+}
+
+// G = diag(theta[0:m]) after a collapse
+__global__ void k_diag_g(double *G, int ld, int m, const double *theta) {
+  for (int e = threadIdx.x; e < m * m; e += blockDim.x) {
+    int i = e / m, j = e % m;
+    G[i * ld + j] = (i == j) ? theta[i] : 0.0;
+  }
+}
+
+// One-CTA cyclic Jacobi (round-robin parallel ordering) for a symmetric m x m matrix.
+// Out: theta ascending, Y (ld x ld, column c = eigenvector c).  status: sweeps used, or
+// -1 if the off-diagonal norm did not fall below tolerance in max_sweeps.
+__global__ void k_jacobi(const double *G, int ld, int m, double *theta, double *Y, int max_sweeps, int *status) {
+  extern __shared__ double sm[];
+  double *A = sm;                 // m x m
+  double *V = sm + m * m;         // m x m
+  __shared__ double cs[MAX_SUB / 2 + 1][2];
+  __shared__ int pq[MAX_SUB / 2 + 1][2];
+  __shared__ double red[512];
+  __shared__ int order[MAX_SUB];
+  const int tid = threadIdx.x, nt = blockDim.x;
+  for (int e = tid; e < m * m; e += nt) {
+    int i = e / m, j = e % m;
+    A[e] = G[i * ld + j];
+    V[e] = (i == j) ? 1.0 : 0.0;
+  }
+  __syncthreads();
+  const int np = (m + 1) & ~1;  // even player count (a dummy when m is odd)
+  int sweeps = 0;
+  bool converged = (m <= 1);
+  for (int sw = 0; sw < max_sweeps && !converged; ++sw) {
+    // off-diagonal and total Frobenius norms
+    double off = 0.0, tot = 0.0;
+    for (int e = tid; e < m * m; e += nt) {
+      double a = A[e];
+      tot += a * a;
+      if (e / m != e % m) off += a * a;
+    }
+    red[tid] = off;
+    __syncthreads();
+    for (int o = nt / 2; o > 0; o >>= 1) { if (tid < o) red[tid] += red[tid + o]; __syncthreads(); }
+    off = red[0];
+    __syncthreads();
+    red[tid] = tot;
+    __syncthreads();
+    for (int o = nt / 2; o > 0; o >>= 1) { if (tid < o) red[tid] += red[tid + o]; __syncthreads(); }
+    tot = red[0];
+    __syncthreads();
+    if (off <= 1e-26 * tot || off == 0.0) { converged = true; break; }
+    ++sweeps;
+    for (int rnd = 0; rnd < np - 1; ++rnd) {
+      // pairs of this round
+      for (int kq = tid; kq < np / 2; kq += nt) {
+        int a = (kq == 0) ? 0 : 1 + ((kq - 1 + rnd) % (np - 1));
+        int bidx = np - 1 - kq;
+        int b = 1 + ((bidx - 1 + rnd) % (np - 1));
+        int p = min(a, b), q = max(a, b);
+        double c = 1.0, s = 0.0;
+        if (q < m) {
+          double apq = A[p * m + q];
+          if (apq != 0.0) {
+            double tau = (A[q * m + q] - A[p * m + p]) / (2.0 * apq);
+            double t = (tau >= 0.0 ? 1.0 : -1.0) / (fabs(tau) + sqrt(1.0 + tau * tau));
+            c = 1.0 / sqrt(1.0 + t * t);
+            s = t * c;
+          }
+        }
+        cs[kq][0] = c; cs[kq][1] = s;
+        pq[kq][0] = p; pq[kq][1] = q;
+      }
+      __syncthreads();
+      // A <- A J (columns), V <- V J
+      for (int e = tid; e < (np / 2) * m; e += nt) {
+        int kq = e / m, i = e % m;
+        int p = pq[kq][0], q = pq[kq][1];
+        if (q >= m) continue;
+        double c = cs[kq][0], s = cs[kq][1];
+        double aip = A[i * m + p], aiq = A[i * m + q];
+        A[i * m + p] = c * aip - s * aiq;
+        A[i * m + q] = s * aip + c * aiq;
+        double vip = V[i * m + p], viq = V[i * m + q];
+        V[i * m + p] = c * vip - s * viq;
+        V[i * m + q] = s * vip + c * viq;
+      }
+      __syncthreads();
+      // A <- J^T A (rows)
+      for (int e = tid; e < (np / 2) * m; e += nt) {
+        int kq = e / m, j = e % m;
+        int p = pq[kq][0], q = pq[kq][1];
+        if (q >= m) continue;
+        double c = cs[kq][0], s = cs[kq][1];
+        double apj = A[p * m + j], aqj = A[q * m + j];
+        A[p * m + j] = c * apj - s * aqj;
+        A[q * m + j] = s * apj + c * aqj;
+      }
+      __syncthreads();
+    }
+  }
+  // sort eigenvalues ascending (rank sort; ties broken by index)
+  for (int i = tid; i < m; i += nt) {
+    double di = A[i * m + i];
+    int rank = 0;
+    for (int j = 0; j < m; ++j) {
+      double dj = A[j * m + j];
+      if (dj < di || (dj == di && j < i)) ++rank;
+    }
+    order[rank] = i;
+  }
+  __syncthreads();
+  for (int e = tid; e < m * m; e += nt) {
+    int i = e / m, c = e % m;
+    Y[i * ld + c] = V[i * m + order[c]];
+  }
+  for (int c = tid; c < m; c += nt) theta[c] = A[order[c] * m + order[c]];
+  if (tid == 0) *status = converged ? sweeps : -1;
+}
+
+__global__ void k_set_unit(double *V, int ld, int c0, const int64_t *idx, int nr) {
+  int j = threadIdx.x;
+  if (j < nr) V[idx[j] * ld + c0 + j] = 1.0;
+}
+
+__global__ void k_copy_cols(int64_t n, const double *src, int lds, int s0, double *dst, int ldd, int d0, int k) {
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n * k; e += (int64_t)gridDim.x * blockDim.x) {
+    int64_t r = e / k;
+    int j = (int)(e - r * k);
+    dst[r * ldd + d0 + j] = src[r * lds + s0 + j];
+  }
+}
+
+struct Work {
+  psoci_ctx *c = nullptr;
+  int64_t N = 0;
+  int ld = 0, nr = 0;
+  double *V = nullptr, *HV = nullptr, *G = nullptr, *Y = nullptr, *theta = nullptr;
+  double *X = nullptr, *HX = nullptr, *R = nullptr, *T = nullptr, *tmp = nullptr;
+  double *partial = nullptr, *small = nullptr, *F = nullptr, *norms = nullptr;
+  float *x32 = nullptr;
+  int *sel = nullptr, *ibuf = nullptr;
+  int64_t *idx = nullptr;
+  int nblk = 0;
+  int64_t rows_per_blk = 0;
+  std::vector<cudaEvent_t> ev;
+  ~Work() {
+    psoci_free(V); psoci_free(HV); psoci_free(G); psoci_free(Y); psoci_free(theta); psoci_free(X); psoci_free(HX);
+    psoci_free(R); psoci_free(T); psoci_free(tmp); psoci_free(partial); psoci_free(small); psoci_free(F);
+    psoci_free(norms); psoci_free(x32); psoci_free(sel); psoci_free(ibuf); psoci_free(idx);
+    for (auto e : ev) cudaEventDestroy(e);
+  }
+};
+
+// C (ldc, column offset c0) = A[:, a0:a0+m]^T B[:, b0:b0+k]
+psoci_status tn(Work &w, const double *A, int lda, int a0, int m, const double *B, int ldb, int b0, int k, double *C,
+                int ldc, int c0) {
+  psoci_ctx *c = w.c;
+  if (m * k > TN_THREADS * TN_MAXOUT) return psoci_fail(c, PSOCI_ERR_INVALID_ARG, "tn: block too large");
+  size_t smem = sizeof(double) * TN_ROWS * (m + k);
+  k_tn<<<w.nblk, TN_THREADS, smem, c->stream>>>(w.N, A, lda, a0, m, B, ldb, b0, k, w.partial, w.rows_per_blk);
+  k_reduce_partials<<<(m * k + 127) / 128, 128, 0, c->stream>>>(w.partial, w.nblk, m, k, C, ldc, c0);
+  PSOCI_CUDA(c, cudaGetLastError());
+  return PSOCI_OK;
+}
+
+psoci_status nn(Work &w, const double *A, int lda, int a0, int m, const double *Y, int ldy, int y0, int k, double alpha,
+                double beta, double *Out, int ldo, int o0) {
+  psoci_ctx *c = w.c;
+  size_t smem = sizeof(double) * (m * k + 32 * m);
+  int blocks = (int)std::min<int64_t>((w.N + 31) / 32, 152 * 8);
+  k_nn<<<std::max(blocks, 1), NN_THREADS, smem, c->stream>>>(w.N, A, lda, a0, m, Y, ldy, y0, k, alpha, beta, Out, ldo,
+                                                             o0);
+  PSOCI_CUDA(c, cudaGetLastError());
+  return PSOCI_OK;
+}
+
+psoci_status sigma_block(Work &w, const double *X, int ldx, double *Y, int ldy, int k, psoci_prec prec) {
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  w.ev.push_back(e0);
+  w.ev.push_back(e1);
+  cudaEventRecord(e0, w.c->stream);
+  psoci_status s = psoci_sigma_launch(w.c, k, X, ldx, Y, ldy, prec, w.x32);
+  cudaEventRecord(e1, w.c->stream);
+  return s;
+}
+
+// orthonormalise T[:, 0:b] against V[:, 0:m] and within itself; kept columns land in
+// V[:, m:m+b'].  Returns b' through *bk.
+psoci_status orthonormalize(Work &w, int m, int b, int *bk) {
+  psoci_ctx *c = w.c;
+  psoci_status s;
+  const int ld = w.ld, tld = w.nr;
+  // squared norms before the projection: a column that loses all but 1e-10 of its norm
+  // against V (or the block's earlier columns) carries no new direction and is dropped
+  double *ref = w.small + (size_t)ld * ld / 2;
+  if ((s = tn(w, w.T, tld, 0, b, w.T, tld, 0, b, ref, b, 0))) return s;
+  for (int pass = 0; pass < 2 && m > 0; ++pass) {
+    // C = V^T T (m x b) into w.small (ld = b), T -= V C
+    if ((s = tn(w, w.V, ld, 0, m, w.T, tld, 0, b, w.small, b, 0))) return s;
+    if ((s = nn(w, w.V, ld, 0, m, w.small, b, 0, b, -1.0, 1.0, w.T, tld, 0))) return s;
+  }
+  // Cholesky-QR twice: first into tmp, then into V[:, m:]
+  int nk = b;
+  for (int pass = 0; pass < 2; ++pass) {
+    const double *src = (pass == 0) ? w.T : w.tmp;
+    int srcld = (pass == 0) ? tld : w.nr;
+    if ((s = tn(w, src, srcld, 0, nk, src, srcld, 0, nk, w.small, nk, 0))) return s;
+    k_cholqr_factor<<<1, 32, 0, c->stream>>>(w.small, nk, pass == 0 ? ref : nullptr, b, 1e-10, w.F, w.ibuf);
+    PSOCI_CUDA(c, cudaGetLastError());
+    int nk2 = 0;
+    PSOCI_CUDA(c, cudaMemcpyAsync(&nk2, w.ibuf, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    PSOCI_CUDA(c, cudaStreamSynchronize(c->stream));
+    if (nk2 == 0) { *bk = 0; return PSOCI_OK; }
+    if (pass == 0) {
+      if ((s = nn(w, w.T, tld, 0, nk, w.F, nk, 0, nk2, 1.0, 0.0, w.tmp, w.nr, 0))) return s;
+    } else {
+      if ((s = nn(w, w.tmp, w.nr, 0, nk, w.F, nk, 0, nk2, 1.0, 0.0, w.V, ld, m))) return s;
+    }
+    nk = nk2;
+  }
+  *bk = nk;
+  return PSOCI_OK;
+}
+
+}  // namespace
+
+psoci_status psoci_davidson_impl(psoci_ctx *c, const psoci_dav_opts *o, double *evals, double *evecs, double *rnorms,
+                                 psoci_dav_stats *stats) {
+  if (!c->have_h) return psoci_fail(c, PSOCI_ERR_STATE, "davidson: Hamiltonian not built");
+  if (!o) return psoci_fail(c, PSOCI_ERR_INVALID_ARG, "davidson: null options");
+  const int64_t N = c->nsef_total;
+  const int nr = o->nroots;
+  if (nr < 1 || nr > 16 || nr > N) return psoci_fail(c, PSOCI_ERR_INVALID_ARG, "davidson: nroots must be 1..16 and <= N");
+  int maxsub = o->max_subspace > 0 ? o->max_subspace : 4 * nr;
+  maxsub = std::max(maxsub, 3 * nr);
+  maxsub = std::min<int64_t>(maxsub, std::min<int64_t>(MAX_SUB, N));
+  if (maxsub < 2 * nr && N >= 2 * nr) return psoci_fail(c, PSOCI_ERR_INVALID_ARG, "davidson: subspace too small");
+  if (o->prec == PSOCI_PREC_MIXED && !c->d_val32)
+    return psoci_fail(c, PSOCI_ERR_STATE, "davidson: MIXED needs PSOCI_HMODE_CSR_BOTH");
+  const double rtol = o->rtol > 0 ? o->rtol : 1e-6;
+  const double dmin = o->precond_min > 0 ? o->precond_min : 1e-3;
+  const int max_iter = o->max_iter > 0 ? o->max_iter : 1000;
+  auto t_start = std::chrono::steady_clock::now();
+
+  Work w;
+  w.c = c;
+  w.N = N;
+  w.nr = nr;
+  w.ld = (maxsub + 1) & ~1;
+  const int ld = w.ld;
+  w.nblk = (int)std::min<int64_t>(std::max<int64_t>(1, (N + 255) / 256), 152 * 4);
+  w.rows_per_blk = (N + w.nblk - 1) / w.nblk;
+  psoci_status s;
+  if ((s = psoci_alloc(c, &w.V, (size_t)N * ld)) || (s = psoci_alloc(c, &w.HV, (size_t)N * ld)) ||
+      (s = psoci_alloc(c, &w.G, (size_t)ld * ld)) || (s = psoci_alloc(c, &w.Y, (size_t)ld * ld)) ||
+      (s = psoci_alloc(c, &w.theta, ld)) || (s = psoci_alloc(c, &w.X, (size_t)N * nr)) ||
+      (s = psoci_alloc(c, &w.HX, (size_t)N * nr)) || (s = psoci_alloc(c, &w.R, (size_t)N * nr)) ||
+      (s = psoci_alloc(c, &w.T, (size_t)N * nr)) || (s = psoci_alloc(c, &w.tmp, (size_t)N * std::max(nr, 2 * nr))) ||
+      (s = psoci_alloc(c, &w.partial, (size_t)w.nblk * TN_THREADS * TN_MAXOUT)) ||
+      (s = psoci_alloc(c, &w.small, (size_t)ld * ld)) || (s = psoci_alloc(c, &w.F, 16 * 16)) ||
+      (s = psoci_alloc(c, &w.norms, 16)) || (s = psoci_alloc(c, &w.sel, 16)) || (s = psoci_alloc(c, &w.ibuf, 4)) ||
+      (s = psoci_alloc(c, &w.idx, 16)))
+    return s;
+  if (o->prec == PSOCI_PREC_MIXED || o->refine)
+    if ((s = psoci_alloc(c, &w.x32, (size_t)N * 8))) return s;
+  cudaStream_t st = c->stream;
+  const size_t jac_smem = sizeof(double) * 2 * MAX_SUB * MAX_SUB;
+  PSOCI_CUDA(c, cudaFuncSetAttribute(k_jacobi, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)jac_smem));
+  PSOCI_CUDA(c, cudaFuncSetAttribute(k_nn, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024));
+  PSOCI_CUDA(c, cudaFuncSetAttribute(k_tn, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024));
+  PSOCI_CUDA(c, cudaMemsetAsync(w.V, 0, sizeof(double) * N * ld, st));
+  PSOCI_CUDA(c, cudaMemsetAsync(w.G, 0, sizeof(double) * ld * ld, st));
+
+  // guess: unit vectors on the nr lowest diagonal elements
+  std::vector<double> hdiag(N);
+  PSOCI_CUDA(c, cudaMemcpyAsync(hdiag.data(), c->d_diag, sizeof(double) * N, cudaMemcpyDeviceToHost, st));
+  PSOCI_CUDA(c, cudaStreamSynchronize(st));
+  std::vector<int64_t> order(N);
+  std::iota(order.begin(), order.end(), 0);
+  std::partial_sort(order.begin(), order.begin() + nr, order.end(),
+                    [&](int64_t a, int64_t b) { return hdiag[a] < hdiag[b] || (hdiag[a] == hdiag[b] && a < b); });
+  PSOCI_CUDA(c, cudaMemcpyAsync(w.idx, order.data(), sizeof(int64_t) * nr, cudaMemcpyHostToDevice, st));
+  k_set_unit<<<1, 32, 0, st>>>(w.V, ld, 0, w.idx, nr);
+
+  psoci_prec prec = o->prec;
+  bool refine_phase = (prec == PSOCI_PREC_FP64);
+  const double tol_mixed = std::max(rtol, 1e-5);
+  int m = nr;
+  int iters = 0, sigma_calls = 0, collapses = 0, refine_iters = 0;
+  if ((s = sigma_block(w, w.V, ld, w.HV, ld, nr, prec))) return s;
+  sigma_calls += nr;
+  if ((s = tn(w, w.V, ld, 0, m, w.HV, ld, 0, m, w.G, ld, 0))) return s;
+  k_symmetrize<<<1, 256, 0, st>>>(w.G, ld, 0, m);
+
+  std::vector<double> h_norm(nr), h_theta(ld);
+  std::vector<int> sel;
+  bool done = false;
+  psoci_status result = PSOCI_OK;
+  int jstat = 0;
+  while (!done) {
+    if (iters >= max_iter) { result = PSOCI_ERR_NOT_CONVERGED; break; }
+    ++iters;
+    if (refine_phase && prec != o->prec) ++refine_iters;
+    k_jacobi<<<1, 256, jac_smem, st>>>(w.G, ld, m, w.theta, w.Y, 60, w.ibuf);
+    PSOCI_CUDA(c, cudaGetLastError());
+    // Ritz vectors, their images and residuals
+    if ((s = nn(w, w.V, ld, 0, m, w.Y, ld, 0, nr, 1.0, 0.0, w.X, nr, 0))) return s;
+    if ((s = nn(w, w.HV, ld, 0, m, w.Y, ld, 0, nr, 1.0, 0.0, w.HX, nr, 0))) return s;
+    int rb = (int)std::min<int64_t>((N + 255) / 256, 152 * 4);
+    k_residual<<<rb, 256, 0, st>>>(N, nr, w.X, w.HX, w.theta, w.R, w.partial);
+    k_sum_cols<<<1, 32, 0, st>>>(w.partial, rb, nr, w.norms);
+    PSOCI_CUDA(c, cudaGetLastError());
+    PSOCI_CUDA(c, cudaMemcpyAsync(h_norm.data(), w.norms, sizeof(double) * nr, cudaMemcpyDeviceToHost, st));
+    PSOCI_CUDA(c, cudaMemcpyAsync(h_theta.data(), w.theta, sizeof(double) * m, cudaMemcpyDeviceToHost, st));
+    PSOCI_CUDA(c, cudaMemcpyAsync(&jstat, w.ibuf, sizeof(int), cudaMemcpyDeviceToHost, st));
+    PSOCI_CUDA(c, cudaStreamSynchronize(st));
+    for (int j = 0; j < nr; ++j) {
+      if (!std::isfinite(h_norm[j]) || !std::isfinite(h_theta[j]))
+        return psoci_fail(c, PSOCI_ERR_NUMERIC, "davidson: non-finite residual or Ritz value");
+      h_norm[j] = std::sqrt(h_norm[j]);
+    }
+    const double tol = refine_phase ? rtol : tol_mixed;
+    sel.clear();
+    for (int j = 0; j < nr; ++j)
+      if (h_norm[j] > tol) {
+        sel.push_back(j);
+        if (!o->block) break;
+      }
+    if (c->verbose)
+      fprintf(stderr, "psoci davidson it=%d m=%d %s max|r|=%.3e e0=%.12f jacobi=%d\n", iters, m,
+              refine_phase ? "fp64" : "mixed", *std::max_element(h_norm.begin(), h_norm.end()), h_theta[0], jstat);
+    if (sel.empty()) {
+      if (!refine_phase && o->refine) {
+        // FP64 refinement: restart from the Ritz vectors with exact (FP64) H products
+        refine_phase = true;
+        prec = PSOCI_PREC_FP64;
+        if ((s = nn(w, w.V, ld, 0, m, w.Y, ld, 0, nr, 1.0, 0.0, w.T, nr, 0))) return s;
+        int bk = 0;
+        if ((s = orthonormalize(w, 0, nr, &bk))) return s;
+        m = bk;
+        if (m == 0) return psoci_fail(c, PSOCI_ERR_NUMERIC, "davidson: refinement basis collapsed");
+        if ((s = sigma_block(w, w.V, ld, w.HV, ld, m, prec))) return s;
+        sigma_calls += m;
+        if ((s = tn(w, w.V, ld, 0, m, w.HV, ld, 0, m, w.G, ld, 0))) return s;
+        k_symmetrize<<<1, 256, 0, st>>>(w.G, ld, 0, m);
+        continue;
+      }
+      done = true;
+      break;
+    }
+    int nsel = (int)sel.size();
+    PSOCI_CUDA(c, cudaMemcpyAsync(w.sel, sel.data(), sizeof(int) * nsel, cudaMemcpyHostToDevice, st));
+    k_precond<<<(int)std::min<int64_t>((N * nsel + 255) / 256, 152 * 16), 256, 0, st>>>(N, nr, w.R, c->d_diag, w.theta,
+                                                                                         w.sel, nsel, dmin, w.T, nr);
+    PSOCI_CUDA(c, cudaGetLastError());
+    if (m + nsel > maxsub) {
+      // collapse onto the lowest keep Ritz vectors (reference: 2*nroots), V and HV alike
+      int keep = std::min(m, std::max(nr, std::min(2 * nr, maxsub - nsel)));
+      if ((s = nn(w, w.V, ld, 0, m, w.Y, ld, 0, keep, 1.0, 0.0, w.tmp, 2 * nr, 0))) return s;
+      k_copy_cols<<<152 * 8, 256, 0, st>>>(N, w.tmp, 2 * nr, 0, w.V, ld, 0, keep);
+      if ((s = nn(w, w.HV, ld, 0, m, w.Y, ld, 0, keep, 1.0, 0.0, w.tmp, 2 * nr, 0))) return s;
+      k_copy_cols<<<152 * 8, 256, 0, st>>>(N, w.tmp, 2 * nr, 0, w.HV, ld, 0, keep);
+      k_diag_g<<<1, 256, 0, st>>>(w.G, ld, keep, w.theta);
+      PSOCI_CUDA(c, cudaGetLastError());
+      m = keep;
+      ++collapses;
+    }
+    int bk = 0;
+    if ((s = orthonormalize(w, m, nsel, &bk))) return s;
+    if (bk == 0) { result = PSOCI_ERR_NOT_CONVERGED; break; }
+    if ((s = sigma_block(w, w.V + m, ld, w.HV + m, ld, bk, prec))) return s;
+    sigma_calls += bk;
+    if ((s = tn(w, w.V, ld, 0, m + bk, w.HV, ld, m, bk, w.G, ld, m))) return s;
+    k_symmetrize<<<1, 256, 0, st>>>(w.G, ld, m, m + bk);
+    PSOCI_CUDA(c, cudaGetLastError());
+    m += bk;
+  }
+  PSOCI_CUDA(c, cudaStreamSynchronize(st));
+  // outputs
+  if (evals) for (int j = 0; j < nr; ++j) evals[j] = h_theta[j];
+  if (rnorms) for (int j = 0; j < nr; ++j) rnorms[j] = h_norm[j];
+  if (evecs) {
+    std::vector<double> hx((size_t)N * nr);
+    PSOCI_CUDA(c, cudaMemcpy(hx.data(), w.X, sizeof(double) * N * nr, cudaMemcpyDeviceToHost));
+    for (int64_t r = 0; r < N; ++r)
+      for (int j = 0; j < nr; ++j) evecs[(size_t)j * N + r] = hx[(size_t)r * nr + j];
+  }
+  if (stats) {
+    stats->iterations = iters;
+    stats->sigma_calls = sigma_calls;
+    stats->collapses = collapses;
+    stats->refine_iters = refine_iters;
+    stats->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
+    double sig = 0.0;
+    for (size_t e = 0; e + 1 < w.ev.size(); e += 2) {
+      float ms = 0.f;
+      if (cudaEventElapsedTime(&ms, w.ev[e], w.ev[e + 1]) == cudaSuccess) sig += ms * 1e-3;
+    }
+    stats->sigma_seconds = sig;
+  }
+  if (result != PSOCI_OK) return psoci_fail(c, result, "davidson: did not converge within the iteration limit");
+  return PSOCI_OK;
+}

@@ -1,0 +1,132 @@
+// Internal declarations shared by the translation units of libpsoci_gpu.so.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/psoci_gpu.h"
+
+#define PSOCI_MAX_OPEN 11     // reference limit (PsociDeterminants.hpp:95-101)
+#define PSOCI_MAX_WORDS 2     // nbf <= 128
+#define PSOCI_SEG 32          // neighbours per warp segment in the H build
+#define PSOCI_MIN_VALUE 1.0e-8  // packSefsef threshold (PsociHamiltonian.hpp:37)
+
+// ------------------------------------------------------------------------------------
+// host-side context
+// ------------------------------------------------------------------------------------
+struct DevBuf {
+  void *p = nullptr;
+  size_t bytes = 0;
+};
+
+struct psoci_ctx {
+  int device = 0;
+  int verbose = 0;
+  cudaStream_t stream = nullptr;
+  std::string err;
+
+  // integrals
+  int nbf = 0;
+  double ecore = 0.0;
+  double *d_one = nullptr;  // packed 1-e (SO folded), nbf(nbf+1)/2
+  double *d_eri = nullptr;  // canonical packed 2-e
+  int64_t n1 = 0, n2 = 0;
+  bool have_ints = false;
+
+  // configurations
+  int nelec = 0, ksym = 0, mx_open = 0, nconf = 0, words = 1;
+  bool have_cfgs = false;
+  std::vector<int32_t> h_jsym;
+  std::vector<uint8_t> h_occ;
+  uint64_t *d_e1 = nullptr;   // [nconf*words] bit p: occ_p >= 1
+  uint64_t *d_e2 = nullptr;   // [nconf*words] bit p: occ_p == 2
+  int32_t *d_jsym = nullptr;  // [nconf]
+  int32_t *d_nopen = nullptr; // [nconf]
+
+  // determinants
+  bool have_dets = false;
+  std::vector<int64_t> h_sefoff, h_detoff;  // nconf+1
+  int64_t nsef_total = 0, ndet_total = 0;
+  int max_nsef = 0, max_ndet = 0;
+  int64_t *d_sefoff = nullptr, *d_detoff = nullptr;
+  uint64_t *d_alpha = nullptr, *d_beta = nullptr;  // [ndet*words]
+  uint8_t *d_phase = nullptr;                      // [ndet]
+  uint8_t *d_nalpha = nullptr;                     // [ndet]
+  int32_t *d_ms = nullptr;                         // [ndet]
+  // template table: per (class, nopen) a run of (amask, bmask, msoff)
+  uint32_t *d_tmpl = nullptr;   // packed: amask | bmask<<12 ; ms offset stored separately
+  int32_t *d_tmpl_ms = nullptr;
+  int32_t *d_tmpl_off = nullptr;  // [4*12+1] start of each (class, nopen) run
+
+  // Hamiltonian
+  bool have_h = false;
+  int64_t nnz = 0;
+  int64_t npairs = 0, nseg = 0;
+  int64_t *d_rowptr = nullptr;
+  int32_t *d_col = nullptr;
+  double *d_val = nullptr;
+  float *d_val32 = nullptr;
+  double *d_diag = nullptr;
+  double build_seconds = 0.0;
+
+  // scratch for host-pointer sigma
+  double *d_x = nullptr, *d_y = nullptr;
+  size_t xy_cap = 0;
+  float *d_x32 = nullptr;
+  size_t x32_cap = 0;
+};
+
+// error helpers -----------------------------------------------------------------------
+psoci_status psoci_fail(psoci_ctx *c, psoci_status s, const std::string &msg);
+psoci_status psoci_cuda_fail(psoci_ctx *c, cudaError_t e, const char *where);
+#define PSOCI_CUDA(c, call)                                            \
+  do {                                                                 \
+    cudaError_t _e = (call);                                           \
+    if (_e != cudaSuccess) return psoci_cuda_fail((c), _e, #call);     \
+  } while (0)
+
+template <typename T>
+psoci_status psoci_alloc(psoci_ctx *c, T **p, size_t count) {
+  if (*p) { cudaFree(*p); *p = nullptr; }
+  if (count == 0) count = 1;
+  cudaError_t e = cudaMalloc((void **)p, count * sizeof(T));
+  if (e != cudaSuccess) {
+    *p = nullptr;
+    cudaGetLastError();
+    return psoci_fail(c, e == cudaErrorMemoryAllocation ? PSOCI_ERR_NOMEM : PSOCI_ERR_CUDA,
+                      std::string("cudaMalloc: ") + cudaGetErrorString(e));
+  }
+  return PSOCI_OK;
+}
+template <typename T>
+void psoci_free(T *&p) {
+  if (p) cudaFree(p);
+  p = nullptr;
+}
+
+// device-wide exclusive scan of int64 counts (in place allowed); returns total on host
+psoci_status psoci_scan_i64(psoci_ctx *c, const int64_t *d_in, int64_t *d_out, int64_t n, int64_t *total);
+
+// sigma (sigma.cu) — device pointers, row-major N x k with leading dims
+psoci_status psoci_sigma_launch(psoci_ctx *c, int k, const double *dX, int ldx, double *dY, int ldy,
+                                psoci_prec prec, float *dX32);
+
+// determinant templates (dets.cu)
+psoci_status psoci_dets_build(psoci_ctx *c);
+psoci_status psoci_h_build(psoci_ctx *c, psoci_hmode mode, int64_t *nnz);
+void psoci_h_release(psoci_ctx *c);
+void psoci_dets_release(psoci_ctx *c);
+
+// ------------------------------------------------------------------------------------
+// device helpers
+// ------------------------------------------------------------------------------------
+__device__ __forceinline__ int64_t tri64(int64_t i, int64_t j) {
+  int64_t a = i > j ? i : j, b = i > j ? j : i;
+  return a * (a + 1) / 2 + b;
+}
+// canonical 8-fold index (PsociIntegrals.C:889-898), 0-based
+__device__ __forceinline__ int64_t canon4(int i, int j, int k, int l) {
+  return tri64(tri64(i, j), tri64(k, l));
+}

@@ -1,0 +1,120 @@
+// Error helpers and the device-wide exclusive scan used by the builders.
+#include <cstdio>
+
+#include "psoci_internal.cuh"
+
+psoci_status psoci_fail(psoci_ctx *c, psoci_status s, const std::string &msg) {
+  if (c) c->err = msg;
+  return s;
+}
+
+psoci_status psoci_cuda_fail(psoci_ctx *c, cudaError_t e, const char *where) {
+  char buf[512];
+  snprintf(buf, sizeof(buf), "%s: %s", where, cudaGetErrorString(e));
+  if (c) c->err = buf;
+  return (e == cudaErrorMemoryAllocation) ? PSOCI_ERR_NOMEM : PSOCI_ERR_CUDA;
+}
+
+namespace {
+constexpr int SCAN_T = 512;
+constexpr int SCAN_PER = 8;
+constexpr int SCAN_CHUNK = SCAN_T * SCAN_PER;
+
+// block-wide exclusive scan of one chunk; writes per-block total
+__global__ void k_scan_chunk(const int64_t *in, int64_t *out, int64_t n, int64_t *blocksum, const int64_t *blockoff) {
+  __shared__ int64_t warp_tot[SCAN_T / 32];
+  int64_t base = (int64_t)blockIdx.x * SCAN_CHUNK + (int64_t)threadIdx.x * SCAN_PER;
+  int64_t v[SCAN_PER];
+  int64_t sum = 0;
+#pragma unroll
+  for (int q = 0; q < SCAN_PER; ++q) {
+    int64_t idx = base + q;
+    v[q] = (idx < n) ? in[idx] : 0;
+    sum += v[q];
+  }
+  // warp inclusive scan of per-thread sums
+  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  int64_t incl = sum;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    int64_t t = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += t;
+  }
+  if (lane == 31) warp_tot[wid] = incl;
+  __syncthreads();
+  if (wid == 0) {
+    int64_t w = (lane < SCAN_T / 32) ? warp_tot[lane] : 0;
+    int64_t wi = w;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      int64_t t = __shfl_up_sync(0xffffffffu, wi, o);
+      if (lane >= o) wi += t;
+    }
+    if (lane < SCAN_T / 32) warp_tot[lane] = wi - w;  // exclusive warp offsets
+    if (lane == SCAN_T / 32 - 1 && blocksum) blocksum[blockIdx.x] = wi;
+  }
+  __syncthreads();
+  if (out) {
+    int64_t run = warp_tot[wid] + (incl - sum) + (blockoff ? blockoff[blockIdx.x] : 0);
+#pragma unroll
+    for (int q = 0; q < SCAN_PER; ++q) {
+      int64_t idx = base + q;
+      if (idx < n) out[idx] = run;
+      run += v[q];
+    }
+  }
+}
+
+__global__ void k_write_total(const int64_t *in, const int64_t *out, int64_t n, int64_t *total_slot) {
+  // out[n] = out[n-1] + in[n-1]
+  if (n == 0) *total_slot = 0;
+  else *total_slot = out[n - 1] + in[n - 1];
+}
+}  // namespace
+
+// exclusive scan of n counts into out[0..n]; out[n] = total; total also returned on host.
+// in and out must not alias.
+psoci_status psoci_scan_i64(psoci_ctx *c, const int64_t *d_in, int64_t *d_out, int64_t n, int64_t *total) {
+  cudaStream_t s = c->stream;
+  if (n <= 0) {
+    int64_t z = 0;
+    PSOCI_CUDA(c, cudaMemcpyAsync(d_out, &z, sizeof(int64_t), cudaMemcpyHostToDevice, s));
+    PSOCI_CUDA(c, cudaStreamSynchronize(s));
+    if (total) *total = 0;
+    return PSOCI_OK;
+  }
+  int64_t nb = (n + SCAN_CHUNK - 1) / SCAN_CHUNK;
+  int64_t *d_bs = nullptr, *d_bo = nullptr;
+  psoci_status st = psoci_alloc(c, &d_bs, nb + 1);
+  if (st) return st;
+  st = psoci_alloc(c, &d_bo, nb + 1);
+  if (st) { psoci_free(d_bs); return st; }
+  k_scan_chunk<<<(unsigned)nb, SCAN_T, 0, s>>>(d_in, nullptr, n, d_bs, nullptr);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) {
+    if (nb > 1) {
+      int64_t tb = 0;
+      st = psoci_scan_i64(c, d_bs, d_bo, nb, &tb);
+    } else {
+      int64_t z = 0;
+      e = cudaMemcpyAsync(d_bo, &z, sizeof(int64_t), cudaMemcpyHostToDevice, s);
+    }
+  }
+  if (e == cudaSuccess && st == PSOCI_OK) {
+    k_scan_chunk<<<(unsigned)nb, SCAN_T, 0, s>>>(d_in, d_out, n, nullptr, d_bo);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess && st == PSOCI_OK) {
+    k_write_total<<<1, 1, 0, s>>>(d_in, d_out, n, d_out + n);
+    e = cudaGetLastError();
+  }
+  int64_t tot = 0;
+  if (e == cudaSuccess && st == PSOCI_OK) e = cudaMemcpyAsync(&tot, d_out + n, sizeof(int64_t), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess && st == PSOCI_OK) e = cudaStreamSynchronize(s);
+  psoci_free(d_bs);
+  psoci_free(d_bo);
+  if (st != PSOCI_OK) return st;
+  if (e != cudaSuccess) return psoci_cuda_fail(c, e, "psoci_scan_i64");
+  if (total) *total = tot;
+  return PSOCI_OK;
+}

@@ -1,0 +1,137 @@
+"""GPU path vs the oracle (C restatement of the reference), through the C ABI.
+
+Bars: determinant bit-strings, phases and spin projections bit-exact; CSR structure
+identical to the reference's lower triangle mirrored; element values within 1e-12 Eh
+(the element kernel follows the reference's operation order, so they are usually
+identical); FP64 sigma within 1e-12 relative; FP64 Davidson eigenvalues within 1e-10 Eh
+of a dense/ARPACK solve of the oracle matrix; mixed-precision eigenvalues within 1e-7 Eh.
+"""
+import numpy as np
+import pytest
+import scipy.linalg as sla
+
+from helpers import SMALL_CASES, det_lists_to_bits, gpu_bits, high_open_problem, lower_to_full, small_problem
+
+pytestmark = pytest.mark.gpu
+
+H_TOL = 1e-12
+SIGMA_RTOL = 1e-12
+EIG_TOL_FP64 = 1e-10
+EIG_TOL_MIXED = 1e-7
+
+
+def _ctx(p):
+    from psoci_gb300 import api
+
+    c = api.Context(0)
+    c.load_problem(p)
+    c.build_determinants()
+    return c
+
+
+def _check_dets(c, O, p):
+    g = c.get_determinants(p.nconf, p.nbf)
+    cc = O.config_counts()
+    assert (np.diff(g["detoff"]) == cc[:, 0]).all()
+    assert (np.diff(g["sefoff"]) == cc[:, 1]).all()
+    for i in range(p.nconf):
+        ref = det_lists_to_bits(O.config_dets(i), p.nbf)
+        d0 = g["detoff"][i]
+        for d, (a, b, ms, ph) in enumerate(ref):
+            assert gpu_bits(g["alpha"][d0 + d]) == a, (i, d)
+            assert gpu_bits(g["beta"][d0 + d]) == b, (i, d)
+            assert int(g["ms"][d0 + d]) == ms, (i, d)
+            assert int(g["phase"][d0 + d]) == ph, (i, d)
+
+
+def _check_h(c, O, p):
+    rp, ci, va = O.build_lower(4)
+    n = O.num_sefs()
+    F = lower_to_full(rp, ci, va, n)
+    c.build_hamiltonian(mixed=True)
+    grp, gci, gva = c.get_hamiltonian()
+    assert c.nnz == F.nnz
+    assert (grp == F.indptr).all()
+    assert (gci == F.indices).all()
+    diff = np.abs(gva - F.data).max() if F.nnz else 0.0
+    assert diff <= H_TOL, diff
+    d = c.get_diag()
+    assert np.abs(d - O.diag()).max() <= H_TOL
+    return F
+
+
+@pytest.mark.parametrize("name,ksym", SMALL_CASES)
+def test_dets_and_h_small(oracle_mod, name, ksym):
+    p = small_problem(name, ksym)
+    O = oracle_mod.Oracle(p)
+    c = _ctx(p)
+    _check_dets(c, O, p)
+    _check_h(c, O, p)
+
+
+@pytest.mark.parametrize("nelec,ksym", [(10, 1), (10, 2), (9, 1), (11, 4)])
+def test_high_open_shells(oracle_mod, nelec, ksym):
+    """8-11 open shells: the largest templates and the multi-word paths of the kernels."""
+    p = high_open_problem(nbf=14, nelec=nelec, ksym=ksym, per=2)
+    O = oracle_mod.Oracle(p)
+    c = _ctx(p)
+    _check_dets(c, O, p)
+    _check_h(c, O, p)
+
+
+def test_two_word_orbitals(oracle_mod):
+    """nbf > 64: bit-strings span two 64-bit words."""
+    from psoci_gb300.inputs import make_problem
+
+    p = make_problem("mrcis", seed=7, ksym=2, nact=4, nelec=4, nvirt=68)
+    assert p.nbf > 64
+    O = oracle_mod.Oracle(p)
+    c = _ctx(p)
+    _check_dets(c, O, p)
+    _check_h(c, O, p)
+
+
+def test_sigma_fp64_and_mixed(oracle_mod):
+    p = small_problem("fci_6e8o", 1)
+    O = oracle_mod.Oracle(p)
+    c = _ctx(p)
+    rp, ci, va = O.build_lower(4)
+    c.build_hamiltonian(mixed=True)
+    rng = np.random.default_rng(0)
+    for k in (1, 3, 8, 11):
+        X = rng.standard_normal((c.nsef, k))
+        Yref = O.sigma_lower(rp, ci, va, X.T.copy()).T
+        Y = c.sigma(X)
+        scale = np.abs(Yref).max()
+        assert np.abs(Y - Yref).max() <= SIGMA_RTOL * scale * 10
+        Ym = c.sigma(X, prec=1)
+        assert np.abs(Ym - Yref).max() <= 1e-5 * scale
+
+
+@pytest.mark.parametrize("name,ksym", [("fci_6e8o", 1), ("fci_5e6o", 2)])
+def test_davidson_fp64_and_mixed(oracle_mod, name, ksym):
+    p = small_problem(name, ksym)
+    O = oracle_mod.Oracle(p)
+    rp, ci, va = O.build_lower(4)
+    F = lower_to_full(rp, ci, va, O.num_sefs())
+    ref = sla.eigvalsh(F.toarray())
+    nroots = 4
+    c = _ctx(p)
+    c.build_hamiltonian(mixed=True)
+    r64 = c.davidson(nroots, rtol=1e-8, mixed=False)
+    assert np.abs(r64.evals - ref[:nroots]).max() <= EIG_TOL_FP64, (r64.evals, ref[:nroots])
+    rmx = c.davidson(nroots, rtol=1e-8, mixed=True, refine=True)
+    assert np.abs(rmx.evals - ref[:nroots]).max() <= EIG_TOL_MIXED
+    r1 = c.davidson(nroots, rtol=1e-8, mixed=False, block=False)
+    assert np.abs(r1.evals - ref[:nroots]).max() <= EIG_TOL_FP64
+
+
+def test_end_to_end_solve(oracle_mod):
+    from psoci_gb300 import api
+
+    p = small_problem("fci_6e8o", 4)
+    O = oracle_mod.Oracle(p)
+    rp, ci, va = O.build_lower(4)
+    ref = sla.eigvalsh(lower_to_full(rp, ci, va, O.num_sefs()).toarray())
+    res = api.solve(p, nroots=6, mixed=True, rtol=1e-7)
+    assert np.abs(res.evals - ref[:6]).max() <= EIG_TOL_MIXED
