@@ -104,6 +104,11 @@ PSOCI_API psoci_status psoci_get_determinants(const psoci_ctx *ctx, uint64_t *al
  * (both triangles; each off-diagonal element is the reference's lower-triangle value), elements
  * with |x| >= 1e-8 or on the diagonal.  *nnz receives the stored count. */
 PSOCI_API psoci_status psoci_build_hamiltonian(psoci_ctx *ctx, psoci_hmode mode, int64_t *nnz);
+/* Replaces PsociHamiltonian::generateSOCIblocks (PsociHamiltonian.C:401-558) for a batch of
+ * configuration pairs: block q is the reference's nsef_A x nsef_B sefsef matrix for
+ * (A[q], B[q]) in the reference's roles, row-major, stored consecutively in out (host) in
+ * pair order; pairs beyond a double excitation give zero blocks.  Needs the determinants. */
+PSOCI_API psoci_status psoci_blocks(psoci_ctx *ctx, int npairs, const int32_t *A, const int32_t *B, double *out);
 /* Host copy of the CSR (rowptr[N+1], cols[nnz], vals[nnz]); NULLs allowed. */
 PSOCI_API psoci_status psoci_get_hamiltonian(const psoci_ctx *ctx, int64_t *rowptr, int32_t *cols, double *vals);
 /* Replaces PsociGAhamiltonian::fetchDIAG_SEF / fetchDiags (PsociGAhamiltonian.C:9014). */
@@ -147,6 +152,32 @@ typedef struct {
  * column-major: root r at r*N) and rnorms[nroots] may be NULL. */
 PSOCI_API psoci_status psoci_davidson(psoci_ctx *ctx, const psoci_dav_opts *opts, double *evals,
                             double *evecs, double *rnorms, psoci_dav_stats *stats);
+
+/* Initial guess for the next psoci_davidson (the reference's -r vector restart,
+ * driver.PSOCI.splittest.C:962-972): k vectors of length N, root-major (vector r at r*N).
+ * Missing roots are completed with unit vectors on the lowest diagonal elements.
+ * k = 0 clears the guess. */
+PSOCI_API psoci_status psoci_set_guess(psoci_ctx *ctx, int k, const double *vecs);
+
+/* CI vector files in the reference's PsociVector "scalable" layout (PsociVector.C:530-706,
+ * written by PsociGAvectors::dumpVectorScalable, PsociGAvectors.C:207-326).  binary = 0:
+ * ASCII (header "nbasis nroots" / "width prec", per root its 1-based number then nbasis
+ * values fixed with 14 decimals in 18 columns, title trailer); binary = 1: int64 header,
+ * per root an int64 tag and nbasis doubles, title bytes.  vecs is root-major. */
+PSOCI_API psoci_status psoci_write_vectors(const char *path, int binary, int64_t nbasis, int nroots,
+                                           const double *vecs, const char *title);
+/* Reads up to max_roots vectors of length nbasis (readVectorScalable, PsociGAvectors.C:539-658);
+ * PSOCI_ERR_IO on a missing, truncated or mismatched file. */
+PSOCI_API psoci_status psoci_read_vectors(const char *path, int binary, int64_t nbasis, int max_roots,
+                                          double *vecs, int *nroots_read);
+
+/* Hamiltonian checkpoint, replacing SendHamiltonianToDRA / FetchHamiltonianFromDRA
+ * (PsociConstructHamiltonian.C:461-696) with one file in this library's own format (CSR,
+ * diagonal, optional FP32 copy, a hash of the configuration space and a payload checksum).
+ * Loading needs psoci_build_determinants on the same configurations; a file from other
+ * configurations, a truncated file or a checksum mismatch gives PSOCI_ERR_IO. */
+PSOCI_API psoci_status psoci_save_hamiltonian(const psoci_ctx *ctx, const char *path);
+PSOCI_API psoci_status psoci_load_hamiltonian(psoci_ctx *ctx, const char *path);
 
 /* The cudaStream_t (as void*) that every kernel of this context is launched on, for callers
  * that time or order work around the library's calls.  No reference counterpart. */

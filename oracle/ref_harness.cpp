@@ -30,6 +30,7 @@
 #include "PsociDeterminants.hpp"
 #include "PsociHamiltonian.hpp"
 #include "PsociIntegrals.hpp"
+#include "PsociVector.hpp"
 
 using namespace std;
 
@@ -281,6 +282,51 @@ long ref_build_lower(const unsigned char *occ, int nthreads, long *rowptr, int *
     }
   (void)N;
   return nnz;
+}
+
+/* CI vector files through the reference's PsociVector, in the call sequence of
+ * PsociGAvectors::dumpVectorScalable / readVectorScalable (PsociGAvectors.C:207-326,
+ * :539-658), one burst per root.  The exact file name is used (PsociVector(filename)). */
+int ref_vec_write(const char *path, int binary, long nbasis, int nroots, const double *vecs, const char *title) {
+  PsociVector pv{string(path)};
+  pv.setMode(VECTOR_WRITE);
+  pv.OpenFile();
+  pair<int64_t, int64_t> info(nbasis, nroots);
+  if (binary) pv.scalable_WriteHeaderBurstBinary(info);
+  else pv.scalable_WriteHeaderBurst(info);
+  for (int j = 0; j < nroots; ++j) {
+    vector<double> v(vecs + (size_t)j * nbasis, vecs + (size_t)(j + 1) * nbasis);
+    if (binary) pv.WriteBurstBinaryScalable(true, j + 1, v, info);
+    else {
+      pv.WriteBurstScalable(true, j + 1, v, info);
+      pv.WriteBurstScalableEOL();
+    }
+  }
+  (void)title;
+  if (binary) pv.WriteBurstScalableBinaryTrailer();
+  else pv.WriteBurstScalableTrailer();
+  pv.CloseFile();
+  return 0;
+}
+
+int ref_vec_read(const char *path, int binary, long nbasis, int maxroots, double *out) {
+  PsociVector pv{string(path)};
+  pv.setMode(VECTOR_READ);
+  pv.OpenFile();
+  pair<int64_t, int64_t> info;
+  if (binary) pv.scalable_ReadHeaderBurstBinary(info);
+  else pv.scalable_ReadHeaderBurst(info);
+  if (info.first != nbasis) return -1;
+  int n = (int)min<int64_t>(info.second, maxroots);
+  for (int j = 0; j < n; ++j) {
+    vector<double> v(nbasis);
+    if (binary) pv.ReadBurstScalableBinary(true, (int)nbasis, v, info);
+    else pv.ReadBurstScalable(true, (int)nbasis, v, info);
+    /* the binary reader clears the vector and reads into its storage (PsociVector.C:461-480) */
+    memcpy(out + (size_t)j * nbasis, v.data(), sizeof(double) * nbasis);
+  }
+  pv.CloseFile();
+  return n;
 }
 
 }  /* extern "C" */

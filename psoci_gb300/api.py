@@ -65,6 +65,7 @@ SIGNATURES = {
     "psoci_get_counts": (ctypes.c_int, [_P, _I64P, _I64P, _IP, _IP]),
     "psoci_get_determinants": (ctypes.c_int, [_P, _U64P, _U64P, _U8P, _I32P, _I64P, _I64P]),
     "psoci_build_hamiltonian": (ctypes.c_int, [_P, ctypes.c_int, _I64P]),
+    "psoci_blocks": (ctypes.c_int, [_P, ctypes.c_int, _I32P, _I32P, _DP]),
     "psoci_get_hamiltonian": (ctypes.c_int, [_P, _I64P, _I32P, _DP]),
     "psoci_get_diag": (ctypes.c_int, [_P, _DP]),
     "psoci_sigma": (ctypes.c_int, [_P, ctypes.c_int, _DP, _DP, ctypes.c_int]),
@@ -73,6 +74,12 @@ SIGNATURES = {
     "psoci_davidson": (ctypes.c_int, [_P, ctypes.POINTER(DavOpts), _DP, _DP, _DP, ctypes.POINTER(DavStats)]),
     "psoci_core_energy": (ctypes.c_double, [_P]),
     "psoci_stream": (ctypes.c_void_p, [_P]),
+    "psoci_set_guess": (ctypes.c_int, [_P, ctypes.c_int, _DP]),
+    "psoci_write_vectors": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int, ctypes.c_int64, ctypes.c_int, _DP,
+                                           ctypes.c_char_p]),
+    "psoci_read_vectors": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int, ctypes.c_int64, ctypes.c_int, _DP, _IP]),
+    "psoci_save_hamiltonian": (ctypes.c_int, [_P, ctypes.c_char_p]),
+    "psoci_load_hamiltonian": (ctypes.c_int, [_P, ctypes.c_char_p]),
 }
 
 _lib = None
@@ -198,6 +205,21 @@ class Context:
         self.nnz = nnz.value
         return self.nnz
 
+    def blocks(self, A, B, nsef_per_config):
+        """Reference sefsef blocks for pairs (A[q], B[q]); returns a list of 2-D arrays."""
+        A = np.ascontiguousarray(A, np.int32)
+        B = np.ascontiguousarray(B, np.int32)
+        ns = np.asarray(nsef_per_config)
+        sizes = ns[A] * ns[B]
+        out = np.zeros(max(int(sizes.sum()), 1))
+        self._check(self.lib.psoci_blocks(self.ctx, len(A), _ptr(A, _I32P), _ptr(B, _I32P), _ptr(out, _DP)), "blocks")
+        res, o = [], 0
+        for a, b in zip(A, B):
+            n = int(ns[a] * ns[b])
+            res.append(out[o:o + n].reshape(int(ns[a]), int(ns[b])))
+            o += n
+        return res
+
     def get_hamiltonian(self):
         rp = np.zeros(self.nsef + 1, np.int64)
         ci = np.zeros(max(self.nnz, 1), np.int32)
@@ -244,9 +266,48 @@ class Context:
     def core_energy(self) -> float:
         return self.lib.psoci_core_energy(self.ctx)
 
+    def set_guess(self, vecs):
+        """Restart vectors for the next davidson(): array [k, N] (or None to clear)."""
+        if vecs is None:
+            self._check(self.lib.psoci_set_guess(self.ctx, 0, None), "set_guess")
+            return
+        v = np.ascontiguousarray(np.atleast_2d(vecs), np.float64)
+        self._check(self.lib.psoci_set_guess(self.ctx, v.shape[0], _ptr(v, _DP)), "set_guess")
+
+    def save_hamiltonian(self, path: str):
+        self._check(self.lib.psoci_save_hamiltonian(self.ctx, path.encode()), "save_hamiltonian")
+
+    def load_hamiltonian(self, path: str):
+        self._check(self.lib.psoci_load_hamiltonian(self.ctx, path.encode()), "load_hamiltonian")
+        nnz = ctypes.c_int64()
+        # the stored count is not exposed separately: read it back from the CSR row pointers
+        rp = np.zeros(self.nsef + 1, np.int64)
+        self._check(self.lib.psoci_get_hamiltonian(self.ctx, _ptr(rp, _I64P), None, None), "get_hamiltonian")
+        self.nnz = int(rp[-1])
+        del nnz
+
     def stream_handle(self) -> int:
         """cudaStream_t of this context (for CUDA events on the launching stream)."""
         return int(self.lib.psoci_stream(self.ctx) or 0)
+
+
+def write_vectors(path: str, vecs: np.ndarray, binary: bool = False, title: str = ""):
+    """CI vectors [nroots, nbasis] to a file in the reference's PsociVector layout."""
+    lib = load_library()
+    v = np.ascontiguousarray(np.atleast_2d(vecs), np.float64)
+    st = lib.psoci_write_vectors(path.encode(), int(binary), v.shape[1], v.shape[0], _ptr(v, _DP), title.encode())
+    if st != PSOCI_OK:
+        raise PsociError(st, f"write_vectors {path}")
+
+
+def read_vectors(path: str, nbasis: int, max_roots: int, binary: bool = False) -> np.ndarray:
+    lib = load_library()
+    out = np.zeros((max_roots, nbasis))
+    n = ctypes.c_int()
+    st = lib.psoci_read_vectors(path.encode(), int(binary), nbasis, max_roots, _ptr(out, _DP), ctypes.byref(n))
+    if st != PSOCI_OK:
+        raise PsociError(st, f"read_vectors {path}")
+    return out[:n.value]
 
 
 def solve(problem, nroots: int = 8, mixed: bool = True, rtol: float = 1e-6, device: int = 0, verbose: int = 0,

@@ -17,7 +17,7 @@ CSRC = os.path.join(HERE, "csrc")
 LIBDIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(LIBDIR, "libpsoci_gpu.so")
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
-SOURCES = ["util.cu", "dets.cu", "hbuild.cu", "sigma.cu", "davidson.cu", "capi.cu"]
+SOURCES = ["util.cu", "dets.cu", "hbuild.cu", "sigma.cu", "davidson.cu", "capi.cu", "io.cu"]
 PER_FILE = {"hbuild.cu": ["--fmad=false"]}
 
 
@@ -42,7 +42,11 @@ def _stale() -> bool:
     if not os.path.exists(LIB):
         return True
     t = os.path.getmtime(LIB)
-    deps = [os.path.join(CSRC, f) for f in os.listdir(CSRC)] + [os.path.join(HERE, "..", "include", "psoci_gpu.h"), __file__]
+    deps = [os.path.join(CSRC, f) for f in os.listdir(CSRC)] + [os.path.join(HERE, "..", "include", "psoci_gpu.h"), __file__,
+                                                               os.path.join(HERE, "host", "driver_splittest.cpp"),
+                                                               os.path.join(HERE, "..", "include", "psoci", "PsociGpu.hpp")]
+    if not os.path.exists(DRIVER):
+        return True
     return any(os.path.getmtime(d) > t for d in deps if os.path.exists(d))
 
 
@@ -60,9 +64,25 @@ def build(force: bool = False, extra: list[str] | None = None, verbose: bool = F
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
     os.replace(tmp, LIB)
+    build_driver()
     if verbose:
         print("built", LIB, file=sys.stderr)
     return LIB
+
+
+DRIVER = os.path.join(LIBDIR, "psoci_driver")
+
+
+def build_driver() -> str:
+    """The C++ host driver (psoci_gb300/host/driver_splittest.cpp) linked against the library."""
+    src = os.path.join(HERE, "host", "driver_splittest.cpp")
+    inc = os.path.join(HERE, "..", "include")
+    cmd = ["g++", "-std=c++17", "-O2", "-I" + inc, src, "-o", DRIVER, "-L" + LIBDIR, "-lpsoci_gpu",
+           "-Wl,-rpath,$ORIGIN"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"driver build failed:\n{r.stdout}\n{r.stderr}")
+    return DRIVER
 
 
 if __name__ == "__main__":

@@ -211,6 +211,13 @@ psoci_status psoci_build_hamiltonian(psoci_ctx *c, psoci_hmode mode, int64_t *nn
   return s;
 }
 
+psoci_status psoci_blocks(psoci_ctx *c, int npairs, const int32_t *A, const int32_t *B, double *out) {
+  if (!c) return PSOCI_ERR_INVALID_ARG;
+  psoci_status s;
+  if ((s = set_device(c))) return s;
+  return psoci_h_blocks(c, npairs, A, B, out);
+}
+
 psoci_status psoci_get_hamiltonian(const psoci_ctx *cc, int64_t *rowptr, int32_t *cols, double *vals) {
   psoci_ctx *c = const_cast<psoci_ctx *>(cc);
   if (!c) return PSOCI_ERR_INVALID_ARG;
@@ -262,6 +269,19 @@ psoci_status psoci_sigma(psoci_ctx *c, int k, const double *X, double *Y, psoci_
   if ((s = psoci_sigma_device(c, k, c->d_x, k, c->d_y, k, prec))) return s;
   PSOCI_CUDA(c, cudaMemcpyAsync(Y, c->d_y, sizeof(double) * need, cudaMemcpyDeviceToHost, c->stream));
   PSOCI_CUDA(c, cudaStreamSynchronize(c->stream));
+  return PSOCI_OK;
+}
+
+psoci_status psoci_set_guess(psoci_ctx *c, int k, const double *vecs) {
+  if (!c || k < 0 || (k > 0 && !vecs)) return PSOCI_ERR_INVALID_ARG;
+  if (k == 0) {
+    c->guess.clear();
+    c->guess_k = 0;
+    return PSOCI_OK;
+  }
+  if (!c->have_dets) return psoci_fail(c, PSOCI_ERR_STATE, "set_guess: build the determinants first");
+  c->guess.assign(vecs, vecs + (size_t)k * c->nsef_total);
+  c->guess_k = k;
   return PSOCI_OK;
 }
 

@@ -515,16 +515,31 @@ psoci_status psoci_davidson_impl(psoci_ctx *c, const psoci_dav_opts *o, double *
   std::iota(order.begin(), order.end(), 0);
   std::partial_sort(order.begin(), order.begin() + nr, order.end(),
                     [&](int64_t a, int64_t b) { return hdiag[a] < hdiag[b] || (hdiag[a] == hdiag[b] && a < b); });
-  PSOCI_CUDA(c, cudaMemcpyAsync(w.idx, order.data(), sizeof(int64_t) * nr, cudaMemcpyHostToDevice, st));
-  k_set_unit<<<1, 32, 0, st>>>(w.V, ld, 0, w.idx, nr);
-
   psoci_prec prec = o->prec;
   bool refine_phase = (prec == PSOCI_PREC_FP64);
   const double tol_mixed = std::max(rtol, 1e-5);
   int m = nr;
+  if (c->guess_k > 0 && (int64_t)c->guess.size() == (int64_t)c->guess_k * N) {
+    // restart vectors first, unit vectors on the lowest diagonal elements for the rest;
+    // orthonormalised like any new block
+    std::vector<double> t0((size_t)N * nr, 0.0);
+    const int kg = std::min(nr, c->guess_k);
+    for (int j = 0; j < kg; ++j)
+      for (int64_t r = 0; r < N; ++r) t0[(size_t)r * nr + j] = c->guess[(size_t)j * N + r];
+    for (int j = kg; j < nr; ++j) t0[(size_t)order[j - kg] * nr + j] = 1.0;
+    PSOCI_CUDA(c, cudaMemcpyAsync(w.T, t0.data(), sizeof(double) * N * nr, cudaMemcpyHostToDevice, st));
+    int bk = 0;
+    if ((s = orthonormalize(w, 0, nr, &bk))) return s;
+    if (bk < 1) return psoci_fail(c, PSOCI_ERR_NUMERIC, "davidson: restart vectors are linearly dependent");
+    m = bk;
+    PSOCI_CUDA(c, cudaStreamSynchronize(st));
+  } else {
+    PSOCI_CUDA(c, cudaMemcpyAsync(w.idx, order.data(), sizeof(int64_t) * nr, cudaMemcpyHostToDevice, st));
+    k_set_unit<<<1, 32, 0, st>>>(w.V, ld, 0, w.idx, nr);
+  }
   int iters = 0, sigma_calls = 0, collapses = 0, refine_iters = 0;
-  if ((s = sigma_block(w, w.V, ld, w.HV, ld, nr, prec))) return s;
-  sigma_calls += nr;
+  if ((s = sigma_block(w, w.V, ld, w.HV, ld, m, prec))) return s;
+  sigma_calls += m;
   if ((s = tn(w, w.V, ld, 0, m, w.HV, ld, 0, m, w.G, ld, 0))) return s;
   k_symmetrize<<<1, 256, 0, st>>>(w.G, ld, 0, m);
 

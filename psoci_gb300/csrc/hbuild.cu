@@ -75,6 +75,12 @@ struct Params {
   const int32_t *seg_n;
   const int64_t *seg_rowoff;
   int64_t *seg_cnt;        // count pass output / fill pass row offsets (local)
+  // single-pass fast build: kept entries are appended to slab slots, then copied in order
+  int64_t *seg_slot;       // slab position of each (segment, row)
+  unsigned long long *slab_counter;
+  int64_t slab_cap;
+  int32_t *slab_col;
+  double *slab_val;
   const int64_t *rowptr;
   int32_t *col;
   double *val;
@@ -133,36 +139,139 @@ __device__ __forceinline__ double g1(const Params &P, int i, int j) { return __l
 // ------------------------------------------------------------------------------------
 // excitation screen
 // ------------------------------------------------------------------------------------
+// Excitation orbitals between occupations A and B, ascending with multiplicity:
+// A has more electrons than B in iex, fewer in jex (generateSOCIblocks, PsociHamiltonian.C:496-512).
 template <int W>
-__device__ __forceinline__ bool within_two(const Params &P, const uint64_t *a1, const uint64_t *a2, int64_t j) {
-  int d = 0;
+__device__ __forceinline__ int excitation(const uint64_t *e1A, const uint64_t *e2A, const uint64_t *e1B,
+                                          const uint64_t *e2B, int *ex, int *jy) {
+  int ni = 0, nj = 0;
 #pragma unroll
-  for (int w = 0; w < W; ++w)
-    d += __popcll(a1[w] ^ __ldg(P.e1 + j * W + w)) + __popcll(a2[w] ^ __ldg(P.e2 + j * W + w));
-  return d <= 4;
+  for (int w = 0; w < W; ++w) {
+    uint64_t i1 = e1A[w] & ~e1B[w], i2 = e2A[w] & ~e2B[w];
+    uint64_t j1 = e1B[w] & ~e1A[w], j2 = e2B[w] & ~e2A[w];
+    uint64_t u = i1 | i2;
+    while (u) {
+      int b = __ffsll((long long)u) - 1;
+      u &= u - 1;
+      int mult = (int)((i1 >> b) & 1ull) + (int)((i2 >> b) & 1ull);
+      for (int q = 0; q < mult; ++q) { if (ni < 2) ex[ni] = 64 * w + b; ++ni; }
+    }
+    u = j1 | j2;
+    while (u) {
+      int b = __ffsll((long long)u) - 1;
+      u &= u - 1;
+      int mult = (int)((j1 >> b) & 1ull) + (int)((j2 >> b) & 1ull);
+      for (int q = 0; q < mult; ++q) { if (nj < 2) jy[nj] = 64 * w + b; ++nj; }
+    }
+  }
+  return ni;
 }
 
-// MODE 0: count neighbours into cnt[i]; MODE 1: write sorted lists at nbroff[i].
+// Screen, stage 1: configurations within two excitations of i (sum |occ_i - occ_j| <= 4,
+// the orbmap test of PsociGADeterminants.C:2249-2277).  One thread per row configuration;
+// tiles of column configurations are staged in shared memory and read by broadcast, so each
+// thread's candidate list comes out sorted.  blockIdx.y selects a contiguous range of
+// column configurations [y*chunk, (y+1)*chunk) so small problems still fill the GPU; MODE 0
+// counts per (range, row), MODE 1 writes each range's candidates after the earlier ranges'.
+constexpr int SCR_THREADS = 256;
+constexpr int SCR_TILE = 512;
+
 template <int W, int MODE>
-__global__ void k_screen(Params P, int64_t *cnt) {
-  int lane = threadIdx.x & 31;
-  int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+__global__ void __launch_bounds__(SCR_THREADS) k_screen(Params P, int64_t *cnt, const int64_t *soff, int64_t chunk,
+                                                        const int64_t *candoff, int32_t *cand) {
+  __shared__ uint64_t t1[SCR_TILE * W], t2[SCR_TILE * W];
+  const int64_t i = (int64_t)blockIdx.x * SCR_THREADS + threadIdx.x;
+  const bool active = i < P.nconf;
+  uint64_t a1[W], a2[W];
+#pragma unroll
+  for (int w = 0; w < W; ++w) {
+    a1[w] = active ? P.e1[i * W + w] : 0ull;
+    a2[w] = active ? P.e2[i * W + w] : 0ull;
+  }
+  const int64_t jbeg = (int64_t)blockIdx.y * chunk;
+  const int64_t jend = min((int64_t)P.nconf, jbeg + chunk);
+  int64_t n = 0;
+  const int64_t out = (MODE == 1 && active) ? candoff[i] + soff[(int64_t)blockIdx.y * P.nconf + i] : 0;
+  for (int64_t j0 = jbeg; j0 < jend; j0 += SCR_TILE) {
+    const int nt = (int)min((int64_t)SCR_TILE, jend - j0);
+    __syncthreads();
+    for (int e = threadIdx.x; e < nt * W; e += SCR_THREADS) {
+      t1[e] = P.e1[j0 * W + e];
+      t2[e] = P.e2[j0 * W + e];
+    }
+    __syncthreads();
+    if (!active) continue;
+    for (int jj = 0; jj < nt; ++jj) {
+      int d = 0;
+#pragma unroll
+      for (int w = 0; w < W; ++w) d += __popcll(a1[w] ^ t1[jj * W + w]) + __popcll(a2[w] ^ t2[jj * W + w]);
+      if (d <= 4) {
+        if (MODE == 1) cand[out + n] = (int32_t)(j0 + jj);
+        ++n;
+      }
+    }
+  }
+  if (MODE == 0 && active) cnt[(int64_t)blockIdx.y * P.nconf + i] = n;
+}
+
+// Screen, stage 2: drop candidates whose block the reference evaluates to zero from its
+// integral prefactors alone — double excitations with (i0 j0|i1 j1) = (i0 j1|i1 j0) = 0
+// (PsociHamiltonian.C:180-185) and spin-orbit singles with SO_ij = 0 (:227); both tests are
+// symmetric in (i, j).  One warp per row configuration, candidates in order, ballot
+// compaction; MODE 0 counts, MODE 1 writes.
+template <int W, int MODE>
+__global__ void k_prune(Params P, const int64_t *candoff, const int32_t *cand, int64_t *cnt) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
   for (int64_t i = warp; i < P.nconf; i += nwarps) {
     uint64_t a1[W], a2[W];
 #pragma unroll
     for (int w = 0; w < W; ++w) { a1[w] = P.e1[i * W + w]; a2[w] = P.e2[i * W + w]; }
+    const int js_i = P.jsym[i];
+    const int64_t c0 = candoff[i], c1 = candoff[i + 1];
     int64_t n = 0;
-    int64_t out = (MODE == 1) ? P.nbroff[i] : 0;
-    for (int64_t j0 = 0; j0 < P.nconf; j0 += 32) {
-      int64_t j = j0 + lane;
-      bool ok = (j < P.nconf) && within_two<W>(P, a1, a2, j);
-      unsigned b = __ballot_sync(0xffffffffu, ok);
-      if (MODE == 1 && ok) P.nbr[out + n + __popc(b & ((1u << lane) - 1u))] = (int32_t)j;
+    const int64_t out = (MODE == 1) ? P.nbroff[i] : 0;
+    for (int64_t t0 = c0; t0 < c1; t0 += 32) {
+      const int64_t t = t0 + lane;
+      bool keep = false;
+      int32_t j = 0;
+      if (t < c1) {
+        j = cand[t];
+        keep = true;
+        if (j != i) {
+          uint64_t b1[W], b2[W];
+#pragma unroll
+          for (int w = 0; w < W; ++w) { b1[w] = __ldg(P.e1 + (int64_t)j * W + w); b2[w] = __ldg(P.e2 + (int64_t)j * W + w); }
+          int ex[2], jy[2];
+          int ni = (j <= i) ? excitation<W>(a1, a2, b1, b2, ex, jy) : excitation<W>(b1, b2, a1, a2, ex, jy);
+          if (ni == 2) {
+            keep = (__ldg(P.eri + canon4(ex[0], jy[0], ex[1], jy[1])) != 0.0) ||
+                   (__ldg(P.eri + canon4(ex[0], jy[1], ex[1], jy[0])) != 0.0);
+          } else if (ni == 1 && __ldg(P.jsym + j) != js_i) {
+            keep = __ldg(P.one + tri64(ex[0], jy[0])) != 0.0;
+          }
+        }
+      }
+      const unsigned b = __ballot_sync(0xffffffffu, keep);
+      if (MODE == 1 && keep) P.nbr[out + n + __popc(b & ((1u << lane) - 1u))] = j;
       n += __popc(b);
     }
     if (MODE == 0 && lane == 0) cnt[i] = n;
   }
+}
+
+// per row configuration: exclusive offsets of its column ranges and its total
+__global__ void k_screen_offsets(int nconf, int nsplit, const int64_t *cnt, int64_t *soff, int64_t *tot) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nconf) return;
+  int64_t run = 0;
+  for (int sp = 0; sp < nsplit; ++sp) {
+    int64_t v = cnt[(int64_t)sp * nconf + i];
+    soff[(int64_t)sp * nconf + i] = run;
+    run += v;
+  }
+  tot[i] = run;
 }
 
 // per configuration: number of segments and segment-row slots
@@ -215,10 +324,11 @@ __global__ void k_seg_rowscan(int nconf, const int64_t *sefoff, const int64_t *s
 // ------------------------------------------------------------------------------------
 // per-pair set-up (one lane per neighbour)
 // ------------------------------------------------------------------------------------
+// Set up the pair (A, B) in the reference's roles (A = "iconf" of generateSOCIblocks);
+// J is the configuration whose SEFs are the CSR columns.
 template <int W>
-__device__ void pair_setup(const Params &P, int I, int J, PairInfo &pi, double *Kd) {
-  int A = (J <= I) ? I : J, B = (J <= I) ? J : I;
-  pi.A = A; pi.B = B; pi.swap = (J > I);
+__device__ void pair_setup_ab(const Params &P, int A, int B, int J, int swap, PairInfo &pi, double *Kd) {
+  pi.A = A; pi.B = B; pi.swap = swap;
   pi.detA = P.detoff[A]; pi.detB = P.detoff[B];
   pi.colbase = P.sefoff[J];
   pi.nsefJ = (int)(P.sefoff[J + 1] - P.sefoff[J]);
@@ -359,6 +469,12 @@ __device__ void pair_setup(const Params &P, int I, int J, PairInfo &pi, double *
     return;
   }
   pi.kind = K_NONE;
+}
+
+template <int W>
+__device__ void pair_setup(const Params &P, int I, int J, PairInfo &pi, double *Kd) {
+  if (J <= I) pair_setup_ab<W>(P, I, J, J, 0, pi, Kd);
+  else pair_setup_ab<W>(P, J, I, J, 1, pi, Kd);
 }
 
 // ------------------------------------------------------------------------------------
@@ -555,15 +671,12 @@ __global__ void __launch_bounds__(WARPS_PER_CTA * 32) k_hbuild(Params P) {
           k = lo;
           t = q - ws->itemoff[k];
           const PairInfo &pi = ws->pi[k];
-          bool diag_blk = (pi.kind == K_DIAG);
-          if (diag_blk) {
-            // lower half as computed by the reference, upper half mirrored
-            v = (t <= r) ? sef_elem<W>(P, pi, ws->K, r, t) : sef_elem<W>(P, pi, ws->K, t, r);
-            keep = (fabs(v) >= PSOCI_MIN_VALUE) || (t == r);
-          } else {
-            v = pi.swap ? sef_elem<W>(P, pi, ws->K, t, r) : sef_elem<W>(P, pi, ws->K, r, t);
-            keep = fabs(v) >= PSOCI_MIN_VALUE;
-          }
+          // lower half of a diagonal block as the reference computes it, upper half mirrored;
+          // block (J, I) transposed for J > I
+          const bool diag_blk = (pi.kind == K_DIAG);
+          const bool flip = diag_blk ? (t > r) : (pi.swap != 0);
+          v = sef_elem<W>(P, pi, ws->K, flip ? t : r, flip ? r : t);
+          keep = (fabs(v) >= PSOCI_MIN_VALUE) || (diag_blk && t == r);
         }
         unsigned b = __ballot_sync(0xffffffffu, keep);
         if (PASS == 1 && keep) {
@@ -582,6 +695,249 @@ __global__ void __launch_bounds__(WARPS_PER_CTA * 32) k_hbuild(Params P) {
   }
 }
 
+// ------------------------------------------------------------------------------------
+// Fast segment kernel for configurations of at most 32 determinants (<= 6 open shells with
+// an even electron count, <= 5 with an odd one; at most 16 SEFs).  A SEF block is sparse:
+// a determinant couples only to determinants within two spin-orbital substitutions with
+// the same spin projection (one substitution, any spin, for spin-orbit pairs).  Each lane
+// owns one neighbour J and first marks, per row SEF r of I, the column SEFs t whose
+// determinants pass that test; only marked elements are then evaluated, with the same
+// element function (and operation order) as the generic kernel.  An unmarked element is
+// a combination of zero determinant elements and therefore exactly zero.
+// ------------------------------------------------------------------------------------
+constexpr int FAST_MAXDET = 32;
+constexpr int FAST_MAXSEF = 16;
+
+template <int W>
+struct FastSmem {
+  PairInfo pi[PSOCI_SEG];
+  double K[MAXK];
+  uint64_t ra[FAST_MAXDET * W], rb[FAST_MAXDET * W];
+  uint8_t rna[FAST_MAXDET];
+};
+
+// may det (aA, bA) of A and det (aB, bB) of B have a non-zero element?
+template <int W>
+__device__ __forceinline__ bool det_connected(bool so, const uint64_t *aA, const uint64_t *bA, int naA,
+                                              const uint64_t *aB, const uint64_t *bB, int naB) {
+  int ua = 0, ub = 0;
+#pragma unroll
+  for (int w = 0; w < W; ++w) { ua += __popcll(aB[w] & ~aA[w]); ub += __popcll(bB[w] & ~bA[w]); }
+  if (so) return ua <= 1 && ua + ub <= 1;
+  return naA == naB && ua + ub <= 2;
+}
+
+template <int W>
+__global__ void __launch_bounds__(WARPS_PER_CTA * 32) k_hbuild_fast(Params P) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  FastSmem<W> *ws = reinterpret_cast<FastSmem<W> *>(smem_raw) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  const bool odd = P.nelec & 1;
+  for (int64_t s = warp; s < P.nseg; s += nwarps) {
+    const int I = P.seg_cfg[s];
+    const int64_t k0 = P.seg_k0[s];
+    const int n = P.seg_n[s];
+    const int nsefI = (int)(P.sefoff[I + 1] - P.sefoff[I]);
+    const int64_t d0I = P.detoff[I];
+    const int ndI = (int)(P.detoff[I + 1] - d0I);
+    const int nopI = P.nopen[I];
+    if (lane < n) pair_setup<W>(P, I, P.nbr[k0 + lane], ws->pi[lane], ws->K);
+    for (int d = lane; d < ndI; d += 32) {
+#pragma unroll
+      for (int w = 0; w < W; ++w) {
+        ws->ra[d * W + w] = P.alpha[(d0I + d) * W + w];
+        ws->rb[d * W + w] = P.beta[(d0I + d) * W + w];
+      }
+      ws->rna[d] = P.nalpha[d0I + d];
+    }
+    __syncwarp();
+    // phase 1: candidate masks M[r] (bit t) for this lane's neighbour
+    uint32_t M[FAST_MAXSEF];
+    for (int r = 0; r < FAST_MAXSEF; ++r) M[r] = 0u;
+    if (lane < n) {
+      const PairInfo &pi = ws->pi[lane];
+      if (pi.kind != K_NONE) {
+        const bool so = (pi.kind == K_SO);
+        const int64_t d0J = pi.swap ? pi.detA : pi.detB;
+        const int nopJ = pi.swap ? pi.nopenA : pi.nopenB;
+        const int ndJ = 1 << (nopJ > 1 ? nopJ - 1 : 0);
+        for (int b = 0; b < ndJ; ++b) {
+          uint64_t ja[W], jb[W];
+#pragma unroll
+          for (int w = 0; w < W; ++w) { ja[w] = __ldg(P.alpha + (d0J + b) * W + w); jb[w] = __ldg(P.beta + (d0J + b) * W + w); }
+          const int jna = __ldg(P.nalpha + d0J + b);
+          const int t = odd ? b : (nopJ ? (b >> 1) : 0);
+          for (int a = 0; a < ndI; ++a) {
+            const uint64_t *ia = &ws->ra[a * W], *ib = &ws->rb[a * W];
+            const int ina = ws->rna[a];
+            bool c = pi.swap ? det_connected<W>(so, ja, jb, jna, ia, ib, ina)
+                             : det_connected<W>(so, ia, ib, ina, ja, jb, jna);
+            if (c) M[odd ? a : (nopI ? (a >> 1) : 0)] |= 1u << t;
+          }
+        }
+      }
+    }
+    // phase 2: evaluate marked elements row by row; rows keep ascending column order
+    for (int r = 0; r < nsefI; ++r) {
+      uint32_t keepm = 0u;
+      double vals[FAST_MAXSEF];
+      if (lane < n) {
+        const PairInfo &pi = ws->pi[lane];
+        uint32_t m = M[r];
+        while (m) {
+          const int t = __ffs(m) - 1;
+          m &= m - 1;
+          // reference roles: the lower half of a diagonal block, block (J, I) for J > I
+          const bool diag_blk = (pi.kind == K_DIAG);
+          const bool flip = diag_blk ? (t > r) : (pi.swap != 0);
+          const double v = sef_elem<W>(P, pi, ws->K, flip ? t : r, flip ? r : t);
+          const bool keep = (fabs(v) >= PSOCI_MIN_VALUE) || (diag_blk && t == r);
+          if (keep) {
+            keepm |= 1u << t;
+            vals[t] = v;
+          }
+        }
+      }
+      const int c = __popc(keepm);
+      int incl = c;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        int v = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += v;
+      }
+      const int tot = __shfl_sync(0xffffffffu, incl, 31);
+      unsigned long long base = 0;
+      if (lane == 0 && tot > 0) base = atomicAdd(P.slab_counter, (unsigned long long)tot);
+      base = __shfl_sync(0xffffffffu, base, 0);
+      if (lane == 0) {
+        P.seg_cnt[P.seg_rowoff[s] + r] = tot;
+        P.seg_slot[P.seg_rowoff[s] + r] = (int64_t)base;
+      }
+      // entries beyond the slab capacity are counted but not written; the host sees the
+      // final counter, enlarges the slab and evaluates again
+      if (lane < n && (int64_t)(base + tot) <= P.slab_cap) {
+        const PairInfo &pi = ws->pi[lane];
+        int64_t pos = (int64_t)base + (incl - c);
+        uint32_t m = keepm;
+        while (m) {
+          const int t = __ffs(m) - 1;
+          m &= m - 1;
+          P.slab_col[pos] = (int32_t)(pi.colbase + t);
+          P.slab_val[pos] = vals[t];
+          ++pos;
+        }
+      }
+    }
+    __syncwarp();
+  }
+}
+
+// per configuration: exclusive offsets over its segments of the per-row counts (into off),
+// totals per SEF row into row_nnz
+__global__ void k_seg_rowscan2(int nconf, const int64_t *sefoff, const int64_t *segoff, const int64_t *seg_rowoff,
+                               const int64_t *seg_cnt, int64_t *seg_off, int64_t *row_nnz) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nconf) return;
+  int64_t nsef = sefoff[i + 1] - sefoff[i];
+  for (int64_t r = 0; r < nsef; ++r) {
+    int64_t run = 0;
+    for (int64_t s = segoff[i]; s < segoff[i + 1]; ++s) {
+      seg_off[seg_rowoff[s] + r] = run;
+      run += seg_cnt[seg_rowoff[s] + r];
+    }
+    row_nnz[sefoff[i] + r] = run;
+  }
+}
+
+// slab slots -> final CSR positions (segment order, so rows stay in column order)
+__global__ void k_slab_copy(Params P, const int64_t *seg_off) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t s = warp; s < P.nseg; s += nwarps) {
+    const int I = P.seg_cfg[s];
+    const int64_t row0 = P.sefoff[I];
+    const int nsefI = (int)(P.sefoff[I + 1] - row0);
+    for (int r = 0; r < nsefI; ++r) {
+      const int64_t slot = P.seg_rowoff[s] + r;
+      const int64_t cnt = P.seg_cnt[slot], src = P.seg_slot[slot];
+      const int64_t dst = P.rowptr[row0 + r] + seg_off[slot];
+      for (int64_t e = lane; e < cnt; e += 32) {
+        const int32_t cc = P.slab_col[src + e];
+        const double v = P.slab_val[src + e];
+        P.col[dst + e] = cc;
+        P.val[dst + e] = v;
+        if (P.val32) P.val32[dst + e] = (float)v;
+        if (cc == row0 + r) P.diag[row0 + r] = v;
+      }
+    }
+  }
+}
+
+// generateSOCIblocks for an explicit list of (A, B) pairs: the full nsef_A x nsef_B block,
+// row-major, at out + outoff[p] (reference roles, no transposition or mirroring)
+template <int W>
+__global__ void __launch_bounds__(WARPS_PER_CTA * 32) k_blocks(Params P, int npairs, const int32_t *pa,
+                                                               const int32_t *pb, const int64_t *outoff,
+                                                               double *out) {
+  __shared__ PairInfo spi[WARPS_PER_CTA];
+  __shared__ double sK[WARPS_PER_CTA][MAXK];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t q = warp; q < npairs; q += nwarps) {
+    const int A = pa[q], B = pb[q];
+    if (lane == 0) pair_setup_ab<W>(P, A, B, B, 0, spi[wib], sK[wib]);
+    __syncwarp();
+    const int na = (int)(P.sefoff[A + 1] - P.sefoff[A]), nb = (int)(P.sefoff[B + 1] - P.sefoff[B]);
+    for (int e = lane; e < na * nb; e += 32) {
+      int a = e / nb, b = e - a * nb;
+      out[outoff[q] + e] = sef_elem<W>(P, spi[wib], sK[wib], a, b);
+    }
+    __syncwarp();
+  }
+}
+
+template <int W>
+psoci_status run_blocks(psoci_ctx *c, int npairs, const int32_t *hA, const int32_t *hB, double *hout) {
+  std::vector<int64_t> off(npairs + 1, 0);
+  for (int q = 0; q < npairs; ++q) {
+    if (hA[q] < 0 || hA[q] >= c->nconf || hB[q] < 0 || hB[q] >= c->nconf)
+      return psoci_fail(c, PSOCI_ERR_INVALID_ARG, "blocks: configuration index out of range");
+    int64_t na = c->h_sefoff[hA[q] + 1] - c->h_sefoff[hA[q]], nb = c->h_sefoff[hB[q] + 1] - c->h_sefoff[hB[q]];
+    off[q + 1] = off[q] + na * nb;
+  }
+  Params P = {};
+  P.nconf = c->nconf; P.nbf = c->nbf; P.nelec = c->nelec; P.ksym = c->ksym;
+  P.e1 = c->d_e1; P.e2 = c->d_e2; P.jsym = c->d_jsym; P.nopen = c->d_nopen;
+  P.sefoff = c->d_sefoff; P.detoff = c->d_detoff;
+  P.alpha = c->d_alpha; P.beta = c->d_beta; P.phase = c->d_phase; P.nalpha = c->d_nalpha;
+  P.one = c->d_one; P.eri = c->d_eri;
+  int32_t *dA = nullptr, *dB = nullptr;
+  int64_t *doff = nullptr;
+  double *dout = nullptr;
+  psoci_status s;
+  if ((s = psoci_alloc(c, &dA, npairs)) || (s = psoci_alloc(c, &dB, npairs)) || (s = psoci_alloc(c, &doff, npairs + 1)) ||
+      (s = psoci_alloc(c, &dout, off[npairs]))) {
+    psoci_free(dA); psoci_free(dB); psoci_free(doff); psoci_free(dout);
+    return s;
+  }
+  cudaStream_t st = c->stream;
+  cudaMemcpyAsync(dA, hA, sizeof(int32_t) * npairs, cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(dB, hB, sizeof(int32_t) * npairs, cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(doff, off.data(), sizeof(int64_t) * (npairs + 1), cudaMemcpyHostToDevice, st);
+  int blocks = (int)std::max<int64_t>(1, std::min<int64_t>((npairs + WARPS_PER_CTA - 1) / WARPS_PER_CTA, 152 * 16));
+  k_blocks<W><<<blocks, WARPS_PER_CTA * 32, 0, st>>>(P, npairs, dA, dB, doff, dout);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaMemcpyAsync(hout, dout, sizeof(double) * off[npairs], cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  psoci_free(dA); psoci_free(dB); psoci_free(doff); psoci_free(dout);
+  if (e != cudaSuccess) return psoci_cuda_fail(c, e, "blocks");
+  return PSOCI_OK;
+}
+
 template <int W>
 psoci_status run_build(psoci_ctx *c, psoci_hmode mode, int64_t *nnz_out) {
   cudaStream_t st = c->stream;
@@ -597,7 +953,15 @@ psoci_status run_build(psoci_ctx *c, psoci_hmode mode, int64_t *nnz_out) {
   int64_t *d_cnt = nullptr, *d_nbroff = nullptr, *d_nseg = nullptr, *d_nrow = nullptr, *d_segoff = nullptr,
           *d_rowslot = nullptr, *d_segk0 = nullptr, *d_segrow = nullptr, *d_segcnt = nullptr, *d_rownnz = nullptr;
   int32_t *d_nbr = nullptr, *d_segcfg = nullptr, *d_segn = nullptr;
+  int64_t *d_soff = nullptr, *d_tot = nullptr, *d_segslot = nullptr, *d_segofs = nullptr, *d_candoff = nullptr;
+  int32_t *d_cand = nullptr;
+  unsigned long long *d_counter = nullptr;
+  int32_t *d_slabcol = nullptr;
+  double *d_slabval = nullptr;
   auto cleanup = [&]() {
+    psoci_free(d_soff); psoci_free(d_tot); psoci_free(d_segslot); psoci_free(d_segofs); psoci_free(d_counter);
+    psoci_free(d_candoff); psoci_free(d_cand);
+    psoci_free(d_slabcol); psoci_free(d_slabval);
     psoci_free(d_cnt); psoci_free(d_nbroff); psoci_free(d_nseg); psoci_free(d_nrow); psoci_free(d_segoff);
     psoci_free(d_rowslot); psoci_free(d_segk0); psoci_free(d_segrow); psoci_free(d_segcnt); psoci_free(d_rownnz);
     psoci_free(d_nbr); psoci_free(d_segcfg); psoci_free(d_segn);
@@ -620,20 +984,45 @@ psoci_status run_build(psoci_ctx *c, psoci_hmode mode, int64_t *nnz_out) {
     }                                           \
   } while (0)
 
-  const int warp_threads = 256;
-  const int blocks_cfg = (int)std::max<int64_t>(1, std::min<int64_t>(((int64_t)n * 32 + warp_threads - 1) / warp_threads, 152 * 32));
+  auto tnow = [&]() {
+    if (c->verbose) cudaStreamSynchronize(st);
+    return std::chrono::steady_clock::now();
+  };
+  auto t_a = tnow();
   // 1. screen
-  TRY(psoci_alloc(c, &d_cnt, n + 1));
+  const int scr_rows = (n + SCR_THREADS - 1) / SCR_THREADS;
+  int nsplit = (int)std::max<int64_t>(1, std::min<int64_t>(64, (152 * 8 + scr_rows - 1) / scr_rows));
+  int64_t chunk = ((int64_t)n + nsplit - 1) / nsplit;
+  chunk = std::max<int64_t>(chunk, SCR_TILE);
+  nsplit = (int)((n + chunk - 1) / chunk);
+  TRY(psoci_alloc(c, &d_cnt, (size_t)nsplit * n + 1));
+  TRY(psoci_alloc(c, &d_soff, (size_t)nsplit * n + 1));
+  TRY(psoci_alloc(c, &d_tot, n + 1));
+  TRY(psoci_alloc(c, &d_candoff, n + 1));
   TRY(psoci_alloc(c, &d_nbroff, n + 1));
-  k_screen<W, 0><<<blocks_cfg, warp_threads, 0, st>>>(P, d_cnt);
+  dim3 scr_grid(scr_rows, nsplit);
+  k_screen<W, 0><<<scr_grid, SCR_THREADS, 0, st>>>(P, d_cnt, nullptr, chunk, nullptr, nullptr);
+  TRYC(cudaGetLastError());
+  k_screen_offsets<<<(n + 255) / 256, 256, 0, st>>>(n, nsplit, d_cnt, d_soff, d_tot);
+  TRYC(cudaGetLastError());
+  int64_t ncand = 0;
+  TRY(psoci_scan_i64(c, d_tot, d_candoff, n, &ncand));
+  TRY(psoci_alloc(c, &d_cand, ncand));
+  k_screen<W, 1><<<scr_grid, SCR_THREADS, 0, st>>>(P, nullptr, d_soff, chunk, d_candoff, d_cand);
+  TRYC(cudaGetLastError());
+  const int prune_blocks = (int)std::max<int64_t>(1, std::min<int64_t>(((int64_t)n * 32 + 255) / 256, 152 * 32));
+  k_prune<W, 0><<<prune_blocks, 256, 0, st>>>(P, d_candoff, d_cand, d_tot);
   TRYC(cudaGetLastError());
   int64_t npairs = 0;
-  TRY(psoci_scan_i64(c, d_cnt, d_nbroff, n, &npairs));
+  TRY(psoci_scan_i64(c, d_tot, d_nbroff, n, &npairs));
   TRY(psoci_alloc(c, &d_nbr, npairs));
   P.nbroff = d_nbroff; P.nbr = d_nbr;
-  k_screen<W, 1><<<blocks_cfg, warp_threads, 0, st>>>(P, nullptr);
+  k_prune<W, 1><<<prune_blocks, 256, 0, st>>>(P, d_candoff, d_cand, nullptr);
   TRYC(cudaGetLastError());
+  psoci_free(d_cand);
+  c->ncand = ncand;
   c->npairs = npairs;
+  auto t_b = tnow();
 
   // 2. segments
   TRY(psoci_alloc(c, &d_nseg, n + 1));
@@ -658,31 +1047,94 @@ psoci_status run_build(psoci_ctx *c, psoci_hmode mode, int64_t *nnz_out) {
   P.seg_cnt = d_segcnt;
 
   // 3. count
-  const size_t smem = sizeof(WarpSmem) * WARPS_PER_CTA;
-  TRYC(cudaFuncSetAttribute(k_hbuild<W, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  TRYC(cudaFuncSetAttribute(k_hbuild<W, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  const bool fast = c->max_ndet <= FAST_MAXDET;
   int hb_blocks = (int)std::max<int64_t>(1, std::min<int64_t>((nseg + WARPS_PER_CTA - 1) / WARPS_PER_CTA, 152 * 16));
-  k_hbuild<W, 0><<<hb_blocks, WARPS_PER_CTA * 32, smem, st>>>(P);
-  TRYC(cudaGetLastError());
-
-  // 4. offsets
   const int64_t N = c->nsef_total;
-  TRY(psoci_alloc(c, &d_rownnz, N + 1));
-  k_seg_rowscan<<<(n + 127) / 128, 128, 0, st>>>(n, c->d_sefoff, d_segoff, d_segrow, d_segcnt, d_rownnz);
-  TRYC(cudaGetLastError());
-  TRY(psoci_alloc(c, &c->d_rowptr, N + 1));
   int64_t nnz = 0;
-  TRY(psoci_scan_i64(c, d_rownnz, c->d_rowptr, N, &nnz));
-  TRY(psoci_alloc(c, &c->d_col, nnz));
-  TRY(psoci_alloc(c, &c->d_val, nnz));
-  if (mode == PSOCI_HMODE_CSR_BOTH) TRY(psoci_alloc(c, &c->d_val32, nnz));
-  TRY(psoci_alloc(c, &c->d_diag, N));
-  P.rowptr = c->d_rowptr; P.col = c->d_col; P.val = c->d_val; P.val32 = c->d_val32; P.diag = c->d_diag;
-
-  // 5. fill
-  k_hbuild<W, 1><<<hb_blocks, WARPS_PER_CTA * 32, smem, st>>>(P);
-  TRYC(cudaGetLastError());
-  TRYC(cudaStreamSynchronize(st));
+  auto t_c = tnow();
+  auto t_d = t_c, t_e = t_c;
+  if (fast) {
+    // 3. evaluate once: kept entries go to slab slots
+    const size_t smem = sizeof(FastSmem<W>) * WARPS_PER_CTA;
+    TRYC(cudaFuncSetAttribute(k_hbuild_fast<W>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    TRY(psoci_alloc(c, &d_segslot, nslots));
+    TRY(psoci_alloc(c, &d_counter, 1));
+    size_t freeb = 0, totb = 0;
+    TRYC(cudaMemGetInfo(&freeb, &totb));
+    // first guess from the pair count (observed 2-4 kept elements per pair); an overflow is
+    // detected by the kernel's counter and the evaluation repeats with the exact size
+    int64_t cap = std::min<int64_t>((int64_t)(freeb * 0.35) / 12, 8 * npairs + (1 << 20));
+    for (int attempt = 0; attempt < 2; ++attempt) {
+      TRY(psoci_alloc(c, &d_slabcol, cap));
+      TRY(psoci_alloc(c, &d_slabval, cap));
+      TRYC(cudaMemsetAsync(d_counter, 0, sizeof(unsigned long long), st));
+      P.seg_slot = d_segslot; P.slab_counter = d_counter; P.slab_cap = cap;
+      P.slab_col = d_slabcol; P.slab_val = d_slabval;
+      k_hbuild_fast<W><<<hb_blocks, WARPS_PER_CTA * 32, smem, st>>>(P);
+      TRYC(cudaGetLastError());
+      unsigned long long used = 0;
+      TRYC(cudaMemcpyAsync(&used, d_counter, sizeof(used), cudaMemcpyDeviceToHost, st));
+      TRYC(cudaStreamSynchronize(st));
+      nnz = (int64_t)used;
+      if (nnz <= cap) break;
+      psoci_free(d_slabcol);
+      psoci_free(d_slabval);
+      cap = nnz;
+      if (attempt == 1) TRY(psoci_fail(c, PSOCI_ERR_NOMEM, "H build: element slab overflow"));
+    }
+    t_d = tnow();
+    // 4. offsets
+    TRY(psoci_alloc(c, &d_rownnz, N + 1));
+    TRY(psoci_alloc(c, &d_segofs, nslots));
+    k_seg_rowscan2<<<(n + 127) / 128, 128, 0, st>>>(n, c->d_sefoff, d_segoff, d_segrow, d_segcnt, d_segofs, d_rownnz);
+    TRYC(cudaGetLastError());
+    TRY(psoci_alloc(c, &c->d_rowptr, N + 1));
+    int64_t nnz2 = 0;
+    TRY(psoci_scan_i64(c, d_rownnz, c->d_rowptr, N, &nnz2));
+    if (nnz2 != nnz) TRY(psoci_fail(c, PSOCI_ERR_CUDA, "H build: slab and row counts differ"));
+    TRY(psoci_alloc(c, &c->d_col, nnz));
+    TRY(psoci_alloc(c, &c->d_val, nnz));
+    if (mode == PSOCI_HMODE_CSR_BOTH) TRY(psoci_alloc(c, &c->d_val32, nnz));
+    TRY(psoci_alloc(c, &c->d_diag, N));
+    P.rowptr = c->d_rowptr; P.col = c->d_col; P.val = c->d_val; P.val32 = c->d_val32; P.diag = c->d_diag;
+    t_e = tnow();
+    // 5. ordered copy
+    k_slab_copy<<<hb_blocks * 4, 256, 0, st>>>(P, d_segofs);
+    TRYC(cudaGetLastError());
+    TRYC(cudaStreamSynchronize(st));
+  } else {
+    const size_t smem = sizeof(WarpSmem) * WARPS_PER_CTA;
+    TRYC(cudaFuncSetAttribute(k_hbuild<W, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    TRYC(cudaFuncSetAttribute(k_hbuild<W, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    // 3. count
+    k_hbuild<W, 0><<<hb_blocks, WARPS_PER_CTA * 32, smem, st>>>(P);
+    TRYC(cudaGetLastError());
+    t_d = tnow();
+    // 4. offsets
+    TRY(psoci_alloc(c, &d_rownnz, N + 1));
+    k_seg_rowscan<<<(n + 127) / 128, 128, 0, st>>>(n, c->d_sefoff, d_segoff, d_segrow, d_segcnt, d_rownnz);
+    TRYC(cudaGetLastError());
+    TRY(psoci_alloc(c, &c->d_rowptr, N + 1));
+    TRY(psoci_scan_i64(c, d_rownnz, c->d_rowptr, N, &nnz));
+    TRY(psoci_alloc(c, &c->d_col, nnz));
+    TRY(psoci_alloc(c, &c->d_val, nnz));
+    if (mode == PSOCI_HMODE_CSR_BOTH) TRY(psoci_alloc(c, &c->d_val32, nnz));
+    TRY(psoci_alloc(c, &c->d_diag, N));
+    P.rowptr = c->d_rowptr; P.col = c->d_col; P.val = c->d_val; P.val32 = c->d_val32; P.diag = c->d_diag;
+    t_e = tnow();
+    // 5. fill
+    k_hbuild<W, 1><<<hb_blocks, WARPS_PER_CTA * 32, smem, st>>>(P);
+    TRYC(cudaGetLastError());
+    TRYC(cudaStreamSynchronize(st));
+  }
+  auto t_f = std::chrono::steady_clock::now();
+  if (c->verbose) {
+    auto d = [](auto a, auto b) { return std::chrono::duration<double>(b - a).count(); };
+    fprintf(stderr,
+            "psoci: H build phases (%s kernel, %d column ranges): screen %.4f s, segments %.4f s, evaluate %.4f s, "
+            "offsets %.4f s, fill/copy %.4f s\n",
+            fast ? "fast" : "generic", nsplit, d(t_a, t_b), d(t_b, t_c), d(t_c, t_d), d(t_d, t_e), d(t_e, t_f));
+  }
   cleanup();
   c->nnz = nnz;
   *nnz_out = nnz;
@@ -703,6 +1155,14 @@ void psoci_h_release(psoci_ctx *c) {
   c->nnz = 0;
 }
 
+psoci_status psoci_h_blocks(psoci_ctx *c, int npairs, const int32_t *A, const int32_t *B, double *out) {
+  if (!c->have_ints) return psoci_fail(c, PSOCI_ERR_STATE, "blocks: no integrals set");
+  if (!c->have_dets) return psoci_fail(c, PSOCI_ERR_STATE, "blocks: determinants not built");
+  if (npairs < 0 || (npairs > 0 && (!A || !B || !out))) return psoci_fail(c, PSOCI_ERR_INVALID_ARG, "blocks: bad arguments");
+  if (npairs == 0) return PSOCI_OK;
+  return (c->words == 1) ? run_blocks<1>(c, npairs, A, B, out) : run_blocks<2>(c, npairs, A, B, out);
+}
+
 psoci_status psoci_h_build(psoci_ctx *c, psoci_hmode mode, int64_t *nnz) {
   if (!c->have_ints) return psoci_fail(c, PSOCI_ERR_STATE, "psoci_build_hamiltonian: no integrals set");
   if (!c->have_dets) return psoci_fail(c, PSOCI_ERR_STATE, "psoci_build_hamiltonian: determinants not built");
@@ -718,7 +1178,8 @@ psoci_status psoci_h_build(psoci_ctx *c, psoci_hmode mode, int64_t *nnz) {
   c->build_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
   c->have_h = true;
   if (c->verbose)
-    fprintf(stderr, "psoci: H build N=%lld nnz=%lld pairs=%lld segments=%lld %.3f s\n", (long long)c->nsef_total,
-            (long long)c->nnz, (long long)c->npairs, (long long)c->nseg, c->build_seconds);
+    fprintf(stderr, "psoci: H build N=%lld nnz=%lld candidates=%lld pairs=%lld segments=%lld %.3f s\n",
+            (long long)c->nsef_total, (long long)c->nnz, (long long)c->ncand, (long long)c->npairs, (long long)c->nseg,
+            c->build_seconds);
   return PSOCI_OK;
 }

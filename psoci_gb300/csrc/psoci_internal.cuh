@@ -63,13 +63,17 @@ struct psoci_ctx {
   // Hamiltonian
   bool have_h = false;
   int64_t nnz = 0;
-  int64_t npairs = 0, nseg = 0;
+  int64_t npairs = 0, nseg = 0, ncand = 0;
   int64_t *d_rowptr = nullptr;
   int32_t *d_col = nullptr;
   double *d_val = nullptr;
   float *d_val32 = nullptr;
   double *d_diag = nullptr;
   double build_seconds = 0.0;
+
+  // initial guess for the next Davidson run (root-major, guess_k x nsef)
+  std::vector<double> guess;
+  int guess_k = 0;
 
   // scratch for host-pointer sigma
   double *d_x = nullptr, *d_y = nullptr;
@@ -116,6 +120,7 @@ psoci_status psoci_sigma_launch(psoci_ctx *c, int k, const double *dX, int ldx, 
 // determinant templates (dets.cu)
 psoci_status psoci_dets_build(psoci_ctx *c);
 psoci_status psoci_h_build(psoci_ctx *c, psoci_hmode mode, int64_t *nnz);
+psoci_status psoci_h_blocks(psoci_ctx *c, int npairs, const int32_t *A, const int32_t *B, double *out);
 void psoci_h_release(psoci_ctx *c);
 void psoci_dets_release(psoci_ctx *c);
 

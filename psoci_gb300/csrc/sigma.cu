@@ -8,7 +8,9 @@
 // one row of the block in one or two 32-byte sectors) and reduces k sums across lanes.
 //
 //   FP64 : FP64 elements, FP64 products and sums.
-//   MIXED: FP32 elements and FP32 inputs, FP32 products, FP64 accumulation.
+//   MIXED: FP32 elements and FP32 inputs, FP32 products, compensated FP32 (Kahan / float-
+//          float) accumulation, FP64 result.  On GB300 the FP64 pipe issues ~2 FMA/clk/SM,
+//          so a kernel that adds in FP64 per element is bound by that pipe, not by HBM.
 #include <algorithm>
 
 #include "psoci_internal.cuh"
@@ -20,19 +22,61 @@ constexpr int SIG_THREADS = 256;
 template <typename T>
 __device__ __forceinline__ T ldg_stream(const T *p) { return __ldcs(p); }
 
-// transpose-reduce: after this, lane q (< K) holds the warp sum of acc[q]
-template <int K>
-__device__ __forceinline__ double warp_reduce_vec(double (&acc)[K], int lane) {
+// Reduce-scatter of 8 per-lane partial sums across a warp: three halving exchanges
+// (offsets 16, 8, 4) leave each lane one partial, two butterflies (2, 1) finish the sum.
+// Afterwards lanes 4q..4q+3 hold the total of value q.  9 shuffles instead of 40.
+template <typename T, typename Add>
+__device__ __forceinline__ T reduce_scatter8(T (&v)[8], int lane, Add add) {
+  T a[4], b[2], c;
 #pragma unroll
-  for (int q = 0; q < K; ++q) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) acc[q] += __shfl_xor_sync(0xffffffffu, acc[q], o);
+  for (int i = 0; i < 4; ++i) {
+    const bool hi = lane & 16;
+    T send = hi ? v[i] : v[i + 4];
+    T keep = hi ? v[i + 4] : v[i];
+    a[i] = add(keep, __shfl_xor_sync(0xffffffffu, send, 16));
   }
-  double mine = 0.0;
 #pragma unroll
-  for (int q = 0; q < K; ++q)
-    if (lane == q) mine = acc[q];
-  return mine;
+  for (int i = 0; i < 2; ++i) {
+    const bool hi = lane & 8;
+    T send = hi ? a[i] : a[i + 2];
+    T keep = hi ? a[i + 2] : a[i];
+    b[i] = add(keep, __shfl_xor_sync(0xffffffffu, send, 8));
+  }
+  {
+    const bool hi = lane & 4;
+    T send = hi ? b[0] : b[1];
+    T keep = hi ? b[1] : b[0];
+    c = add(keep, __shfl_xor_sync(0xffffffffu, send, 4));
+  }
+  c = add(c, __shfl_xor_sync(0xffffffffu, c, 2));
+  c = add(c, __shfl_xor_sync(0xffffffffu, c, 1));
+  return c;
+}
+
+// float-float pair (hi + lo) and its error-free addition (TwoSum, then renormalise)
+struct ff2 {
+  float h, l;
+};
+__device__ __forceinline__ ff2 ff_add(ff2 a, ff2 b) {
+  float s = __fadd_rn(a.h, b.h);
+  float bp = __fsub_rn(s, a.h);
+  float e = __fadd_rn(__fsub_rn(a.h, __fsub_rn(s, bp)), __fsub_rn(b.h, bp));
+  e = __fadd_rn(e, __fadd_rn(a.l, b.l));
+  float h = __fadd_rn(s, e);
+  return ff2{h, __fsub_rn(e, __fsub_rn(h, s))};
+}
+__device__ __forceinline__ ff2 shfl_ff(ff2 v, int o) {
+  return ff2{__shfl_xor_sync(0xffffffffu, v.h, o), __shfl_xor_sync(0xffffffffu, v.l, o)};
+}
+
+template <int K>
+__device__ __forceinline__ void store_reduced_f64(double (&acc)[K], int lane, double *yr) {
+  double v[8];
+#pragma unroll
+  for (int q = 0; q < 8; ++q) v[q] = (q < K) ? acc[q] : 0.0;
+  double tot = reduce_scatter8(v, lane, [](double x, double y) { return x + y; });
+  const int q = lane >> 2;
+  if ((lane & 3) == 0 && q < K) yr[q] = tot;
 }
 
 template <int K>
@@ -40,7 +84,7 @@ __global__ void __launch_bounds__(SIG_THREADS) k_spmm_f64(int64_t nrows, const i
                                                           const int32_t *__restrict__ col,
                                                           const double *__restrict__ val,
                                                           const double *__restrict__ x, int ldx,
-                                                          double *__restrict__ y, int ldy) {
+                                                          double *__restrict__ y, int ldy, bool vec2) {
   const int lane = threadIdx.x & 31;
   const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
@@ -53,14 +97,26 @@ __global__ void __launch_bounds__(SIG_THREADS) k_spmm_f64(int64_t nrows, const i
       const int c = ldg_stream(col + t);
       const double v = ldg_stream(val + t);
       const double *xr = x + (int64_t)c * ldx;
+      if (K % 2 == 0 && vec2) {
 #pragma unroll
-      for (int q = 0; q < K; ++q) acc[q] = fma(v, __ldg(xr + q), acc[q]);
+        for (int q = 0; q < K; q += 2) {
+          const double2 xx = __ldg(reinterpret_cast<const double2 *>(xr + q));
+          acc[q] = fma(v, xx.x, acc[q]);
+          acc[q + 1] = fma(v, xx.y, acc[q + 1]);
+        }
+      } else {
+#pragma unroll
+        for (int q = 0; q < K; ++q) acc[q] = fma(v, __ldg(xr + q), acc[q]);
+      }
     }
-    double s = warp_reduce_vec<K>(acc, lane);
-    if (lane < K) y[r * ldy + lane] = s;
+    store_reduced_f64<K>(acc, lane, y + r * ldy);
   }
 }
 
+// MIXED: FP32 element x FP32 input products.  Each lane keeps a compensated FP32 sum per
+// vector (Kahan: the rounding error of every addition is carried in c and fed back), so
+// no FP64 arithmetic runs in the streaming loop — on GB300 the FP64 pipe, not HBM, would
+// otherwise bound the kernel.  The 32 lane sums (value + compensation) are combined in FP64.
 template <int K>
 __global__ void __launch_bounds__(SIG_THREADS) k_spmm_mixed(int64_t nrows, const int64_t *__restrict__ rowptr,
                                                             const int32_t *__restrict__ col,
@@ -71,30 +127,66 @@ __global__ void __launch_bounds__(SIG_THREADS) k_spmm_mixed(int64_t nrows, const
   const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
   for (int64_t r = warp; r < nrows; r += nwarps) {
-    double acc[K];
+    float s[K], cmp[K];
 #pragma unroll
-    for (int q = 0; q < K; ++q) acc[q] = 0.0;
+    for (int q = 0; q < K; ++q) { s[q] = 0.f; cmp[q] = 0.f; }
     const int64_t e = rowptr[r + 1];
     for (int64_t t = rowptr[r] + lane; t < e; t += 32) {
       const int c = ldg_stream(col + t);
       const float v = ldg_stream(val + t);
       const float *xr = x + (int64_t)c * ldx;
+      float xv[K];
+      if (K == 8) {
+        // the 8 inputs of one row are 32 contiguous, 32-byte-aligned bytes: one 256-bit load
+        // (sm_100+), i.e. one L1 wavefront per gathered row instead of two
+        asm("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+            : "=f"(xv[0]), "=f"(xv[1]), "=f"(xv[2]), "=f"(xv[3]), "=f"(xv[4]), "=f"(xv[5]), "=f"(xv[6]),
+              "=f"(xv[7])
+            : "l"(xr));
+      } else {
 #pragma unroll
-      for (int q = 0; q < K; ++q) acc[q] += (double)__fmul_rn(v, __ldg(xr + q));
+        for (int q = 0; q < K; ++q) xv[q] = __ldg(xr + q);
+      }
+#pragma unroll
+      for (int q = 0; q < K; ++q) {
+        float yv = __fsub_rn(__fmul_rn(v, xv[q]), cmp[q]);
+        float tt = __fadd_rn(s[q], yv);
+        cmp[q] = __fsub_rn(__fsub_rn(tt, s[q]), yv);
+        s[q] = tt;
+      }
     }
-    double s = warp_reduce_vec<K>(acc, lane);
-    if (lane < K) y[r * ldy + lane] = s;
+    // Kahan leaves sum = s - cmp; reduce (s, -cmp) as float-float pairs, FP64 only at the end
+    ff2 v[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) v[q] = (q < K) ? ff2{s[q], -cmp[q]} : ff2{0.f, 0.f};
+    ff2 a[4], b[2], cc;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const bool hi = lane & 16;
+      a[i] = ff_add(hi ? v[i + 4] : v[i], shfl_ff(hi ? v[i] : v[i + 4], 16));
+    }
+#pragma unroll
+    for (int i = 0; i < 2; ++i) {
+      const bool hi = lane & 8;
+      b[i] = ff_add(hi ? a[i + 2] : a[i], shfl_ff(hi ? a[i] : a[i + 2], 8));
+    }
+    {
+      const bool hi = lane & 4;
+      cc = ff_add(hi ? b[1] : b[0], shfl_ff(hi ? b[0] : b[1], 4));
+    }
+    cc = ff_add(cc, shfl_ff(cc, 2));
+    cc = ff_add(cc, shfl_ff(cc, 1));
+    const int qq = lane >> 2;
+    if ((lane & 3) == 0 && qq < K) y[r * ldy + qq] = (double)cc.h + (double)cc.l;
   }
 }
 
-// X (FP64, leading dim ldx) -> X32 (FP32, leading dim k)
+// X (FP64, leading dim ldx) -> X32 (FP32, leading dim k); one thread per row
 __global__ void k_to_f32(int64_t n, int k, const double *__restrict__ x, int ldx, float *__restrict__ x32) {
-  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  int64_t tot = n * k;
-  for (; i < tot; i += (int64_t)gridDim.x * blockDim.x) {
-    int64_t r = i / k;
-    int q = (int)(i - r * k);
-    x32[i] = (float)x[r * ldx + q];
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+    const double *src = x + r * ldx;
+    float *dst = x32 + r * k;
+    for (int q = 0; q < k; ++q) dst[q] = (float)src[q];
   }
 }
 
@@ -105,7 +197,8 @@ void launch_k(psoci_ctx *c, int64_t n, const double *dX, int ldx, double *dY, in
   int blocks = (int)std::min<int64_t>((warps * 32 + SIG_THREADS - 1) / SIG_THREADS, 152 * 8 * 4);
   if (blocks < 1) blocks = 1;
   if (prec == PSOCI_PREC_FP64)
-    k_spmm_f64<K><<<blocks, SIG_THREADS, 0, c->stream>>>(n, c->d_rowptr, c->d_col, c->d_val, dX, ldx, dY, ldy);
+    k_spmm_f64<K><<<blocks, SIG_THREADS, 0, c->stream>>>(n, c->d_rowptr, c->d_col, c->d_val, dX, ldx, dY, ldy,
+                                                         ((uintptr_t)dX % 16 == 0) && (ldx % 2 == 0));
   else
     k_spmm_mixed<K><<<blocks, SIG_THREADS, 0, c->stream>>>(n, c->d_rowptr, c->d_col, c->d_val32, x32, ld32, dY, ldy);
 }
@@ -128,7 +221,7 @@ psoci_status psoci_sigma_launch(psoci_ctx *c, int k, const double *dX, int ldx, 
     const float *x32 = nullptr;
     if (prec == PSOCI_PREC_MIXED) {
       if (!dX32) return psoci_fail(c, PSOCI_ERR_INVALID_ARG, "sigma: MIXED without FP32 staging");
-      int blocks = (int)std::min<int64_t>((n * kk + 255) / 256, 152 * 16);
+      int blocks = (int)std::min<int64_t>((n + 255) / 256, 152 * 16);
       k_to_f32<<<std::max(blocks, 1), 256, 0, c->stream>>>(n, kk, xs, ldx, dX32);
       x32 = dX32;
     }

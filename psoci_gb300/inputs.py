@@ -285,6 +285,17 @@ def read_config_file(path: str, allow_all_open: bool = True):
     return nbf, nelec, ksym, mx_open, jsym, occ
 
 
+def write_integral_file(path: str, p: Problem) -> None:
+    """Binary integral file for the C++ driver: "PSOCIINT", int32 nbf, float64 ecore,
+    packed one-electron table (SO folded in), canonical two-electron table."""
+    with open(path, "wb") as f:
+        f.write(b"PSOCIINT")
+        f.write(np.int32(p.nbf).tobytes())
+        f.write(np.float64(p.ecore).tobytes())
+        f.write(np.ascontiguousarray(p.one_packed(), np.float64).tobytes())
+        f.write(np.ascontiguousarray(p.eri, np.float64).tobytes())
+
+
 def named_workload(name: str, seed: int = 0, ksym: int = 1) -> Problem:
     """The workloads the benchmark configurations name."""
     table = {

@@ -135,3 +135,19 @@ def test_end_to_end_solve(oracle_mod):
     ref = sla.eigvalsh(lower_to_full(rp, ci, va, O.num_sefs()).toarray())
     res = api.solve(p, nroots=6, mixed=True, rtol=1e-7)
     assert np.abs(res.evals - ref[:6]).max() <= EIG_TOL_MIXED
+
+
+@pytest.mark.parametrize("name,ksym", [("fci_6e8o", 1), ("fci_5e6o", 2)])
+def test_blocks_any_pair(oracle_mod, name, ksym):
+    """psoci_blocks = generateSOCIblocks for arbitrary (A, B), both orders and the diagonal."""
+    p = small_problem(name, ksym)
+    O = oracle_mod.Oracle(p)
+    c = _ctx(p)
+    rng = np.random.default_rng(2)
+    A = rng.integers(0, p.nconf, 400).astype(np.int32)
+    B = rng.integers(0, p.nconf, 400).astype(np.int32)
+    A[:20] = B[:20]
+    got = c.blocks(A, B, p.nsef())
+    for a, b, g in zip(A, B, got):
+        st, ref = O.block(int(a), int(b))
+        assert np.abs(g - ref).max() <= H_TOL, (a, b)
