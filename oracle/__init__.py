@@ -119,6 +119,13 @@ class Oracle(_Base):
             self.ctx, _p(rp, _c_long_p), _p(ci, _c_int_p), _p(va, _c_dbl_p))
         return rp, ci[:nnz], va[:nnz]
 
+    def build_rows(self, rows, nthreads=0):
+        """Lower-triangle rows of the given configurations only; returns the stored count."""
+        nthreads = nthreads or os.cpu_count() or 1
+        r = np.ascontiguousarray(rows, np.int32)
+        f = self._fn("build_rows", ctypes.c_long, [ctypes.c_void_p, ctypes.c_int, _c_int_p, ctypes.c_int])
+        return f(self.ctx, nthreads, _p(r, _c_int_p), len(r))
+
     def diag(self):
         d = np.zeros(self.num_sefs())
         self._fn("diag", None, [ctypes.c_void_p, _c_dbl_p])(self.ctx, _p(d, _c_dbl_p))

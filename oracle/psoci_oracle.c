@@ -524,6 +524,7 @@ static void rb_push(rowbuf *r, int col, double v) {
 
 typedef struct {
   orc_ctx *c; int tid, nth; rowbuf *rows; uint64_t *e1, *e2; int words;
+  const int *only; int nonly;  /* optional list of row configurations */
 } build_arg;
 
 static void *build_worker(void *p) {
@@ -533,7 +534,9 @@ static void *build_worker(void *p) {
   double *sc = (double *)malloc(sizeof(double) * ORC_MAXDET * ORC_MAXDET);
   double *blk = (double *)malloc(sizeof(double) * ORC_MAXDET * ORC_MAXDET);
   int W = a->words;
-  for (int i = a->tid; i < c->nconf; i += a->nth) {
+  int count = a->only ? a->nonly : c->nconf;
+  for (int ii = a->tid; ii < count; ii += a->nth) {
+    int i = a->only ? a->only[ii] : ii;
     const orc_cfg *gi = &c->cfg[i];
     long isef = c->sefoff[i];
     for (int j = 0; j <= i; ++j) {
@@ -577,6 +580,7 @@ long orc_build_lower(orc_ctx *c, int nthreads) {
   for (int t = 0; t < nthreads; ++t) {
     args[t].c = c; args[t].tid = t; args[t].nth = nthreads; args[t].rows = rows;
     args[t].e1 = e1; args[t].e2 = e2; args[t].words = W;
+    args[t].only = NULL; args[t].nonly = 0;
     pthread_create(&th[t], NULL, build_worker, &args[t]);
   }
   for (int t = 0; t < nthreads; ++t) pthread_join(th[t], NULL);
@@ -603,6 +607,34 @@ void orc_copy_lower(const orc_ctx *c, long *rowptr, int *cols, double *vals) {
   memcpy(rowptr, c->rowptr, sizeof(long) * (N + 1));
   memcpy(cols, c->cols, sizeof(int) * c->nnz);
   memcpy(vals, c->vals, sizeof(double) * c->nnz);
+}
+
+/* Rows of a subset of configurations only (each against all j <= i), for timing samples.
+ * Returns the stored element count; the rows are not kept. */
+long orc_build_rows(orc_ctx *c, int nthreads, const int *rows, int nrows) {
+  if (nthreads < 1) nthreads = 1;
+  long N = c->sefoff[c->nconf];
+  int W = (c->nbf + 63) / 64;
+  uint64_t *e1 = (uint64_t *)calloc((size_t)c->nconf * W, 8), *e2 = (uint64_t *)calloc((size_t)c->nconf * W, 8);
+  for (int i = 0; i < c->nconf; ++i)
+    for (int p = 0; p < c->nbf; ++p) {
+      unsigned char o = c->occ[(size_t)i * c->nbf + p];
+      if (o >= 1) e1[(size_t)i * W + p / 64] |= 1ull << (p % 64);
+      if (o == 2) e2[(size_t)i * W + p / 64] |= 1ull << (p % 64);
+    }
+  rowbuf *rb = (rowbuf *)calloc(N, sizeof(rowbuf));
+  pthread_t *th = (pthread_t *)malloc(sizeof(pthread_t) * nthreads);
+  build_arg *args = (build_arg *)malloc(sizeof(build_arg) * nthreads);
+  for (int t = 0; t < nthreads; ++t) {
+    args[t].c = c; args[t].tid = t; args[t].nth = nthreads; args[t].rows = rb;
+    args[t].e1 = e1; args[t].e2 = e2; args[t].words = W; args[t].only = rows; args[t].nonly = nrows;
+    pthread_create(&th[t], NULL, build_worker, &args[t]);
+  }
+  for (int t = 0; t < nthreads; ++t) pthread_join(th[t], NULL);
+  long nnz = 0;
+  for (long r = 0; r < N; ++r) { nnz += rb[r].n; free(rb[r].col); free(rb[r].val); }
+  free(rb); free(th); free(args); free(e1); free(e2);
+  return nnz;
 }
 
 /* diagonal H_rr (the reference keeps it last in each row, g_diag_sef) */

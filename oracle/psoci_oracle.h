@@ -25,6 +25,7 @@ double orc_fetch2e(const orc_ctx *c, int i, int j, int k, int l);
 int orc_block(const orc_ctx *c, int i, int j, double *out);
 long orc_build_lower(orc_ctx *c, int nthreads);
 void orc_copy_lower(const orc_ctx *c, long *rowptr, int *cols, double *vals);
+long orc_build_rows(orc_ctx *c, int nthreads, const int *rows, int nrows);
 void orc_diag(const orc_ctx *c, double *diag);
 void orc_sigma_lower(long n, const long *rowptr, const int *cols, const double *vals, int k,
                      const double *x, double *y, int nthreads);

@@ -44,11 +44,12 @@ struct PairInfo {
   int64_t colbase;      // first SEF of the neighbour J
   int A, B;             // configurations in the reference's roles (A = "iconf")
   int kind, swap;       // swap: J > I, element (t, r) of block (J, I)
-  int iex0, iex1, jex0; // excitation orbitals of A -> B (ascending, with multiplicity)
+  int iex0, iex1, jex0, jex1; // excitation orbitals of A -> B (ascending, with multiplicity)
   int nopenA, nopenB, jsA, jsB, nsefJ;
   double v0, v1;
   double X[PSOCI_MAX_OPEN];  // single: (iex0 s|s jex0) over the open shells s of A
   uint64_t SA[PSOCI_MAX_WORDS];
+  uint64_t SB[PSOCI_MAX_WORDS];  // open shells of B
 };
 
 struct WarpSmem {
@@ -65,6 +66,7 @@ struct Params {
   const uint64_t *alpha, *beta;
   const uint8_t *phase, *nalpha;
   const double *one, *eri;
+  const int8_t *tinv;       // alpha open-shell mask -> det index (<= 6 open shells)
   // screen
   const int64_t *nbroff;
   int32_t *nbr;
@@ -175,23 +177,29 @@ __device__ __forceinline__ int excitation(const uint64_t *e1A, const uint64_t *e
 // counts per (range, row), MODE 1 writes each range's candidates after the earlier ranges'.
 constexpr int SCR_THREADS = 256;
 constexpr int SCR_TILE = 512;
+constexpr int SCR_ROWS = 4;  // row configurations per thread: one shared-memory load serves four tests
 
 template <int W, int MODE>
 __global__ void __launch_bounds__(SCR_THREADS) k_screen(Params P, int64_t *cnt, const int64_t *soff, int64_t chunk,
                                                         const int64_t *candoff, int32_t *cand) {
   __shared__ uint64_t t1[SCR_TILE * W], t2[SCR_TILE * W];
-  const int64_t i = (int64_t)blockIdx.x * SCR_THREADS + threadIdx.x;
-  const bool active = i < P.nconf;
-  uint64_t a1[W], a2[W];
+  uint64_t a1[SCR_ROWS][W], a2[SCR_ROWS][W];
+  int64_t n[SCR_ROWS], out[SCR_ROWS];
+  bool act[SCR_ROWS];
 #pragma unroll
-  for (int w = 0; w < W; ++w) {
-    a1[w] = active ? P.e1[i * W + w] : 0ull;
-    a2[w] = active ? P.e2[i * W + w] : 0ull;
+  for (int q = 0; q < SCR_ROWS; ++q) {
+    const int64_t i = (int64_t)blockIdx.x * (SCR_THREADS * SCR_ROWS) + q * SCR_THREADS + threadIdx.x;
+    act[q] = i < P.nconf;
+#pragma unroll
+    for (int w = 0; w < W; ++w) {
+      a1[q][w] = act[q] ? P.e1[i * W + w] : ~0ull;  // inactive rows match nothing
+      a2[q][w] = act[q] ? P.e2[i * W + w] : ~0ull;
+    }
+    n[q] = 0;
+    out[q] = (MODE == 1 && act[q]) ? candoff[i] + soff[(int64_t)blockIdx.y * P.nconf + i] : 0;
   }
   const int64_t jbeg = (int64_t)blockIdx.y * chunk;
   const int64_t jend = min((int64_t)P.nconf, jbeg + chunk);
-  int64_t n = 0;
-  const int64_t out = (MODE == 1 && active) ? candoff[i] + soff[(int64_t)blockIdx.y * P.nconf + i] : 0;
   for (int64_t j0 = jbeg; j0 < jend; j0 += SCR_TILE) {
     const int nt = (int)min((int64_t)SCR_TILE, jend - j0);
     __syncthreads();
@@ -200,18 +208,30 @@ __global__ void __launch_bounds__(SCR_THREADS) k_screen(Params P, int64_t *cnt, 
       t2[e] = P.e2[j0 * W + e];
     }
     __syncthreads();
-    if (!active) continue;
     for (int jj = 0; jj < nt; ++jj) {
-      int d = 0;
+      uint64_t b1[W], b2[W];
 #pragma unroll
-      for (int w = 0; w < W; ++w) d += __popcll(a1[w] ^ t1[jj * W + w]) + __popcll(a2[w] ^ t2[jj * W + w]);
-      if (d <= 4) {
-        if (MODE == 1) cand[out + n] = (int32_t)(j0 + jj);
-        ++n;
+      for (int w = 0; w < W; ++w) { b1[w] = t1[jj * W + w]; b2[w] = t2[jj * W + w]; }
+#pragma unroll
+      for (int q = 0; q < SCR_ROWS; ++q) {
+        int d = __popcll(a1[q][0] ^ b1[0]) + __popcll(a2[q][0] ^ b2[0]);
+#pragma unroll
+        for (int w = 1; w < W; ++w)
+          if (d <= 4) d += __popcll(a1[q][w] ^ b1[w]) + __popcll(a2[q][w] ^ b2[w]);
+        if (d <= 4 && act[q]) {
+          if (MODE == 1) cand[out[q] + n[q]] = (int32_t)(j0 + jj);
+          ++n[q];
+        }
       }
     }
   }
-  if (MODE == 0 && active) cnt[(int64_t)blockIdx.y * P.nconf + i] = n;
+  if (MODE == 0) {
+#pragma unroll
+    for (int q = 0; q < SCR_ROWS; ++q) {
+      const int64_t i = (int64_t)blockIdx.x * (SCR_THREADS * SCR_ROWS) + q * SCR_THREADS + threadIdx.x;
+      if (act[q]) cnt[(int64_t)blockIdx.y * P.nconf + i] = n[q];
+    }
+  }
 }
 
 // Screen, stage 2: drop candidates whose block the reference evaluates to zero from its
@@ -342,9 +362,10 @@ __device__ void pair_setup_ab(const Params &P, int A, int B, int J, int swap, Pa
     im1[w] = e1A[w] & ~e1B[w]; im2[w] = e2A[w] & ~e2B[w];
     jm1[w] = e1B[w] & ~e1A[w]; jm2[w] = e2B[w] & ~e2A[w];
     pi.SA[w] = e1A[w] & ~e2A[w];
+    pi.SB[w] = e1B[w] & ~e2B[w];
   }
   pi.v0 = 0.0; pi.v1 = 0.0;
-  pi.iex0 = pi.iex1 = pi.jex0 = -1;
+  pi.iex0 = pi.iex1 = pi.jex0 = pi.jex1 = -1;
   int ni = popc_w<W>(im1) + popc_w<W>(im2);
   if (A == B) {
     pi.kind = K_DIAG;
@@ -459,7 +480,7 @@ __device__ void pair_setup_ab(const Params &P, int A, int B, int J, int swap, Pa
         }
       }
     }
-    pi.iex0 = ex[0]; pi.iex1 = ex[1]; pi.jex0 = jy[0];
+    pi.iex0 = ex[0]; pi.iex1 = ex[1]; pi.jex0 = jy[0]; pi.jex1 = jy[1];
     // processDoubleExcitation (PsociHamiltonian.C:180-184)
     double v0 = g2(P, ex[0], jy[0], ex[1], jy[1]);
     double v1 = g2(P, ex[0], jy[1], ex[1], jy[0]);
@@ -708,6 +729,43 @@ __global__ void __launch_bounds__(WARPS_PER_CTA * 32) k_hbuild(Params P) {
 constexpr int FAST_MAXDET = 32;
 constexpr int FAST_MAXSEF = 16;
 
+// ------------------------------------------------------------------------------------
+// Candidate enumeration for the fast kernel: the determinants of J that a determinant a of
+// I can couple to, generated from the allowed spin-orbital substitutions and located
+// through the inverse template table (alpha open-shell mask -> determinant index).
+//   same configuration : a itself, and a with one alpha and one beta open shell swapped;
+//   single r -> s      : (r,sg) -> (s,sg); or (r,sg) -> (s,~sg) with an open shell p
+//                        flipped ~sg -> sg (keeps the spin projection);
+//   double r0 r1 -> s0 s1: two removals and two additions with equal alpha counts;
+//   spin-orbit r -> s  : (r,sg) -> (s,tau), any spins.
+// det_connected() admits exactly these pairs, so the masks are unchanged — only cheaper.
+// ------------------------------------------------------------------------------------
+__device__ __forceinline__ int det_class_dev(int parity, int jsym, int ksym) {
+  if (parity == 1) return ((((jsym + 1) / 2) % 2) == 0) ? 3 : 2;
+  return ((jsym + 1) / 2 == (ksym + 1) / 2) ? 0 : 1;
+}
+
+template <int W>
+__device__ __forceinline__ int lookup_det(const uint64_t *ab, const uint64_t *SJ, const int8_t *inv) {
+  uint32_t m = 0;
+  int t = 0;
+#pragma unroll
+  for (int w = 0; w < W; ++w) {
+    uint64_t s = SJ[w];
+    while (s) {
+      const int b = __ffsll((long long)s) - 1;
+      s &= s - 1;
+      if ((ab[w] >> b) & 1ull) m |= 1u << t;
+      ++t;
+    }
+  }
+  return inv[m];
+}
+
+__device__ __forceinline__ bool tbit(const uint64_t *x, int p) { return (x[p >> 6] >> (p & 63)) & 1ull; }
+__device__ __forceinline__ void setb(uint64_t *x, int p) { x[p >> 6] |= 1ull << (p & 63); }
+__device__ __forceinline__ void clrb(uint64_t *x, int p) { x[p >> 6] &= ~(1ull << (p & 63)); }
+
 template <int W>
 struct FastSmem {
   PairInfo pi[PSOCI_SEG];
@@ -731,6 +789,9 @@ template <int W>
 __global__ void __launch_bounds__(WARPS_PER_CTA * 32) k_hbuild_fast(Params P) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   FastSmem<W> *ws = reinterpret_cast<FastSmem<W> *>(smem_raw) + (threadIdx.x >> 5);
+  __shared__ int8_t ws_tinv[4 * PSOCI_TINV_PER_CLASS];
+  for (int e = threadIdx.x; e < 4 * PSOCI_TINV_PER_CLASS; e += blockDim.x) ws_tinv[e] = P.tinv[e];
+  __syncthreads();
   const int lane = threadIdx.x & 31;
   const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
@@ -753,7 +814,35 @@ __global__ void __launch_bounds__(WARPS_PER_CTA * 32) k_hbuild_fast(Params P) {
       ws->rna[d] = P.nalpha[d0I + d];
     }
     __syncwarp();
-    // phase 1: candidate masks M[r] (bit t) for this lane's neighbour
+    // phase 1: candidate masks M[r] (bit t) for this lane's neighbour, bit-parallel over the
+    // row determinants.  With m_a the alpha pattern of row det a on I's open shells, a column
+    // det b (alpha ab, beta bb) differs from a in
+    //   c(a) = F + #{p in x : p not in m_a} + #{p in y : p in m_a}
+    // spin-orbitals of b, where x, y are b's alpha / beta patterns on I's open shells and F
+    // counts b's electrons in orbitals empty in I.  Non-spin-orbit pairs need c(a) <= 2 and
+    // equal alpha counts, spin-orbit pairs c(a) <= 1 (det_connected's test).  The sets
+    // {a : p in m_a} and {a : |m_a| = k} are warp ballots; c(a) is kept as a saturating
+    // bit-sliced counter over all row dets at once.
+    uint32_t Ap[PSOCI_MAX_OPEN], Nk[PSOCI_MAX_OPEN + 1];
+    int sI[PSOCI_MAX_OPEN];
+    uint64_t occI[W];
+    {
+      uint64_t SI[W];
+      int ns = 0;
+#pragma unroll
+      for (int w = 0; w < W; ++w) {
+        occI[w] = P.e1[(int64_t)I * W + w];
+        SI[w] = occI[w] & ~P.e2[(int64_t)I * W + w];
+        uint64_t t = SI[w];
+        while (t && ns < PSOCI_MAX_OPEN) { sI[ns++] = 64 * w + __ffsll((long long)t) - 1; t &= t - 1; }
+      }
+      uint32_t ma = 0u;
+      if (lane < ndI)
+        for (int p = 0; p < nopI; ++p) ma |= (uint32_t)tbit(&ws->ra[lane * W], sI[p]) << p;
+      for (int p = 0; p < PSOCI_MAX_OPEN; ++p) Ap[p] = __ballot_sync(0xffffffffu, (lane < ndI) && ((ma >> p) & 1u));
+      for (int k = 0; k <= PSOCI_MAX_OPEN; ++k) Nk[k] = __ballot_sync(0xffffffffu, (lane < ndI) && __popc(ma) == k);
+    }
+    const int ndblI = P.nelec - 2 * 0 - nopI;  // electrons in I's doubly occupied orbitals (2 x count)
     uint32_t M[FAST_MAXSEF];
     for (int r = 0; r < FAST_MAXSEF; ++r) M[r] = 0u;
     if (lane < n) {
@@ -763,18 +852,46 @@ __global__ void __launch_bounds__(WARPS_PER_CTA * 32) k_hbuild_fast(Params P) {
         const int64_t d0J = pi.swap ? pi.detA : pi.detB;
         const int nopJ = pi.swap ? pi.nopenA : pi.nopenB;
         const int ndJ = 1 << (nopJ > 1 ? nopJ - 1 : 0);
+        const int thr = so ? 1 : 2;
         for (int b = 0; b < ndJ; ++b) {
           uint64_t ja[W], jb[W];
 #pragma unroll
           for (int w = 0; w < W; ++w) { ja[w] = __ldg(P.alpha + (d0J + b) * W + w); jb[w] = __ldg(P.beta + (d0J + b) * W + w); }
-          const int jna = __ldg(P.nalpha + d0J + b);
+          int F = 0;
+#pragma unroll
+          for (int w = 0; w < W; ++w) F += __popcll(ja[w] & ~occI[w]) + __popcll(jb[w] & ~occI[w]);
+          if (F > thr) continue;
+          // saturating counter over the row dets: S0 (c'=0), S1, S2, S3 (>= 3)
+          uint32_t S0 = 0xffffffffu, S1 = 0u, S2 = 0u;
+          for (int p = 0; p < nopI; ++p) {
+            const bool xa = tbit(ja, sI[p]), yb = tbit(jb, sI[p]);
+            if (xa) {  // mismatch where row det has beta on p
+              const uint32_t T = ~Ap[p];
+              S2 = (S2 & ~T) | (S1 & T);
+              S1 = (S1 & ~T) | (S0 & T);
+              S0 &= ~T;
+            }
+            if (yb) {  // mismatch where row det has alpha on p
+              const uint32_t T = Ap[p];
+              S2 = (S2 & ~T) | (S1 & T);
+              S1 = (S1 & ~T) | (S0 & T);
+              S0 &= ~T;
+            }
+          }
+          uint32_t ok = (thr - F >= 2) ? (S0 | S1 | S2) : (thr - F == 1) ? (S0 | S1) : S0;
+          if (!so) {
+            int na = 0;
+#pragma unroll
+            for (int w = 0; w < W; ++w) na += __popcll(ja[w]);
+            const int need = na - (ndblI / 2);
+            ok &= (need >= 0 && need <= nopI) ? Nk[need] : 0u;
+          }
+          ok &= (ndI >= 32) ? 0xffffffffu : ((1u << ndI) - 1u);
           const int t = odd ? b : (nopJ ? (b >> 1) : 0);
-          for (int a = 0; a < ndI; ++a) {
-            const uint64_t *ia = &ws->ra[a * W], *ib = &ws->rb[a * W];
-            const int ina = ws->rna[a];
-            bool c = pi.swap ? det_connected<W>(so, ja, jb, jna, ia, ib, ina)
-                             : det_connected<W>(so, ia, ib, ina, ja, jb, jna);
-            if (c) M[odd ? a : (nopI ? (a >> 1) : 0)] |= 1u << t;
+          while (ok) {
+            const int a = __ffs(ok) - 1;
+            ok &= ok - 1;
+            M[odd ? a : (nopI ? (a >> 1) : 0)] |= 1u << t;
           }
         }
       }
@@ -948,6 +1065,7 @@ psoci_status run_build(psoci_ctx *c, psoci_hmode mode, int64_t *nnz_out) {
   P.sefoff = c->d_sefoff; P.detoff = c->d_detoff;
   P.alpha = c->d_alpha; P.beta = c->d_beta; P.phase = c->d_phase; P.nalpha = c->d_nalpha;
   P.one = c->d_one; P.eri = c->d_eri;
+  P.tinv = c->d_tinv;
 
   psoci_status s;
   int64_t *d_cnt = nullptr, *d_nbroff = nullptr, *d_nseg = nullptr, *d_nrow = nullptr, *d_segoff = nullptr,
@@ -990,7 +1108,7 @@ psoci_status run_build(psoci_ctx *c, psoci_hmode mode, int64_t *nnz_out) {
   };
   auto t_a = tnow();
   // 1. screen
-  const int scr_rows = (n + SCR_THREADS - 1) / SCR_THREADS;
+  const int scr_rows = (n + SCR_THREADS * SCR_ROWS - 1) / (SCR_THREADS * SCR_ROWS);
   int nsplit = (int)std::max<int64_t>(1, std::min<int64_t>(64, (152 * 8 + scr_rows - 1) / scr_rows));
   int64_t chunk = ((int64_t)n + nsplit - 1) / nsplit;
   chunk = std::max<int64_t>(chunk, SCR_TILE);
