@@ -122,6 +122,21 @@ PSOCI_API psoci_status psoci_sigma(psoci_ctx *ctx, int k, const double *X, doubl
 PSOCI_API psoci_status psoci_sigma_device(psoci_ctx *ctx, int k, const double *dX, int ldx, double *dY,
                                 int ldy, psoci_prec prec);
 
+/* Mixed-precision sigma that allocates no device memory, for callers that cannot call
+ * cudaMalloc while they run: work issued inside a CUDA stream capture, host programs whose
+ * own allocator owns the whole GPU memory budget, loops that must not take an allocation's
+ * implicit synchronisation.  Same arguments and result as psoci_sigma_device with
+ * PSOCI_PREC_MIXED, but the FP32 copy of the input is staged in a fixed 16 MiB device array
+ * compiled into the library (held by every device that loads it) instead of a buffer grown
+ * with cudaMalloc.  Limit: N * 8 <= 4 Mi floats, i.e. at most 524,288 SEFs; larger problems
+ * get PSOCI_ERR_UNSUPPORTED.  All calls on a device share the array (each call overwrites
+ * what it reads first, so nothing must start at zero); calls that overlap on the GPU race
+ * and must be serialised by the caller.  The first call on a device looks up the array's
+ * address and caches it: make that first call before any stream capture begins.
+ * No counterpart in the reference. */
+PSOCI_API psoci_status psoci_sigma_mixed_noalloc(psoci_ctx *ctx, int k, const double *dX, int ldx, double *dY,
+                                                 int ldy);
+
 typedef struct {
   int nroots;          /* roots wanted                                                  */
   int max_subspace;    /* basis size that triggers a collapse (reference: 4*nroots)      */

@@ -74,6 +74,8 @@ SIGNATURES = {
     "psoci_davidson": (ctypes.c_int, [_P, ctypes.POINTER(DavOpts), _DP, _DP, _DP, ctypes.POINTER(DavStats)]),
     "psoci_core_energy": (ctypes.c_double, [_P]),
     "psoci_stream": (ctypes.c_void_p, [_P]),
+    "psoci_sigma_mixed_noalloc": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
+                                                 ctypes.c_int]),
     "psoci_set_guess": (ctypes.c_int, [_P, ctypes.c_int, _DP]),
     "psoci_write_vectors": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int, ctypes.c_int64, ctypes.c_int, _DP,
                                            ctypes.c_char_p]),

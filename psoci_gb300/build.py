@@ -17,7 +17,7 @@ CSRC = os.path.join(HERE, "csrc")
 LIBDIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(LIBDIR, "libpsoci_gpu.so")
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
-SOURCES = ["util.cu", "dets.cu", "hbuild.cu", "sigma.cu", "davidson.cu", "capi.cu", "io.cu"]
+SOURCES = ["util.cu", "dets.cu", "hbuild.cu", "sigma.cu", "davidson.cu", "capi.cu", "io.cu", "noalloc.cu"]
 PER_FILE = {"hbuild.cu": ["--fmad=false"]}
 
 
