@@ -198,6 +198,11 @@ PSOCI_API psoci_status psoci_load_hamiltonian(psoci_ctx *ctx, const char *path);
  * that time or order work around the library's calls.  No reference counterpart. */
 PSOCI_API void *psoci_stream(const psoci_ctx *ctx);
 
+/* Number of kernels this library has launched in this process, over all contexts, so that
+ * a caller can count the launches a call makes (difference of two readings).  No reference
+ * counterpart. */
+PSOCI_API unsigned long long psoci_launch_count(void);
+
 /* Core energy passed to psoci_set_integrals (PsociIntegrals::fetchCoreEnergy). */
 PSOCI_API double psoci_core_energy(const psoci_ctx *ctx);
 

@@ -74,6 +74,7 @@ SIGNATURES = {
     "psoci_davidson": (ctypes.c_int, [_P, ctypes.POINTER(DavOpts), _DP, _DP, _DP, ctypes.POINTER(DavStats)]),
     "psoci_core_energy": (ctypes.c_double, [_P]),
     "psoci_stream": (ctypes.c_void_p, [_P]),
+    "psoci_launch_count": (ctypes.c_ulonglong, []),
     "psoci_sigma_mixed_noalloc": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
                                                  ctypes.c_int]),
     "psoci_set_guess": (ctypes.c_int, [_P, ctypes.c_int, _DP]),
@@ -291,6 +292,10 @@ class Context:
     def stream_handle(self) -> int:
         """cudaStream_t of this context (for CUDA events on the launching stream)."""
         return int(self.lib.psoci_stream(self.ctx) or 0)
+
+    def launch_count(self) -> int:
+        """Kernels the library has launched in this process so far (all contexts)."""
+        return int(self.lib.psoci_launch_count())
 
 
 def write_vectors(path: str, vecs: np.ndarray, binary: bool = False, title: str = ""):

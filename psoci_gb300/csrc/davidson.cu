@@ -391,7 +391,9 @@ psoci_status tn(Work &w, const double *A, int lda, int a0, int m, const double *
   psoci_ctx *c = w.c;
   if (m * k > TN_THREADS * TN_MAXOUT) return psoci_fail(c, PSOCI_ERR_INVALID_ARG, "tn: block too large");
   size_t smem = sizeof(double) * TN_ROWS * (m + k);
+  psoci_note_launch();
   k_tn<<<w.nblk, TN_THREADS, smem, c->stream>>>(w.N, A, lda, a0, m, B, ldb, b0, k, w.partial, w.rows_per_blk);
+  psoci_note_launch();
   k_reduce_partials<<<(m * k + 127) / 128, 128, 0, c->stream>>>(w.partial, w.nblk, m, k, C, ldc, c0);
   PSOCI_CUDA(c, cudaGetLastError());
   return PSOCI_OK;
@@ -402,6 +404,7 @@ psoci_status nn(Work &w, const double *A, int lda, int a0, int m, const double *
   psoci_ctx *c = w.c;
   size_t smem = sizeof(double) * (m * k + 32 * m);
   int blocks = (int)std::min<int64_t>((w.N + 31) / 32, 152 * 8);
+  psoci_note_launch();
   k_nn<<<std::max(blocks, 1), NN_THREADS, smem, c->stream>>>(w.N, A, lda, a0, m, Y, ldy, y0, k, alpha, beta, Out, ldo,
                                                              o0);
   PSOCI_CUDA(c, cudaGetLastError());
@@ -441,6 +444,7 @@ psoci_status orthonormalize(Work &w, int m, int b, int *bk) {
     const double *src = (pass == 0) ? w.T : w.tmp;
     int srcld = (pass == 0) ? tld : w.nr;
     if ((s = tn(w, src, srcld, 0, nk, src, srcld, 0, nk, w.small, nk, 0))) return s;
+    psoci_note_launch();
     k_cholqr_factor<<<1, 32, 0, c->stream>>>(w.small, nk, pass == 0 ? ref : nullptr, b, 1e-10, w.F, w.ibuf);
     PSOCI_CUDA(c, cudaGetLastError());
     int nk2 = 0;
@@ -535,12 +539,14 @@ psoci_status psoci_davidson_impl(psoci_ctx *c, const psoci_dav_opts *o, double *
     PSOCI_CUDA(c, cudaStreamSynchronize(st));
   } else {
     PSOCI_CUDA(c, cudaMemcpyAsync(w.idx, order.data(), sizeof(int64_t) * nr, cudaMemcpyHostToDevice, st));
+    psoci_note_launch();
     k_set_unit<<<1, 32, 0, st>>>(w.V, ld, 0, w.idx, nr);
   }
   int iters = 0, sigma_calls = 0, collapses = 0, refine_iters = 0;
   if ((s = sigma_block(w, w.V, ld, w.HV, ld, m, prec))) return s;
   sigma_calls += m;
   if ((s = tn(w, w.V, ld, 0, m, w.HV, ld, 0, m, w.G, ld, 0))) return s;
+  psoci_note_launch();
   k_symmetrize<<<1, 256, 0, st>>>(w.G, ld, 0, m);
 
   std::vector<double> h_norm(nr), h_theta(ld);
@@ -552,13 +558,16 @@ psoci_status psoci_davidson_impl(psoci_ctx *c, const psoci_dav_opts *o, double *
     if (iters >= max_iter) { result = PSOCI_ERR_NOT_CONVERGED; break; }
     ++iters;
     if (refine_phase && prec != o->prec) ++refine_iters;
+    psoci_note_launch();
     k_jacobi<<<1, 256, jac_smem, st>>>(w.G, ld, m, w.theta, w.Y, 60, w.ibuf);
     PSOCI_CUDA(c, cudaGetLastError());
     // Ritz vectors, their images and residuals
     if ((s = nn(w, w.V, ld, 0, m, w.Y, ld, 0, nr, 1.0, 0.0, w.X, nr, 0))) return s;
     if ((s = nn(w, w.HV, ld, 0, m, w.Y, ld, 0, nr, 1.0, 0.0, w.HX, nr, 0))) return s;
     int rb = (int)std::min<int64_t>((N + 255) / 256, 152 * 4);
+    psoci_note_launch();
     k_residual<<<rb, 256, 0, st>>>(N, nr, w.X, w.HX, w.theta, w.R, w.partial);
+    psoci_note_launch();
     k_sum_cols<<<1, 32, 0, st>>>(w.partial, rb, nr, w.norms);
     PSOCI_CUDA(c, cudaGetLastError());
     PSOCI_CUDA(c, cudaMemcpyAsync(h_norm.data(), w.norms, sizeof(double) * nr, cudaMemcpyDeviceToHost, st));
@@ -593,6 +602,7 @@ psoci_status psoci_davidson_impl(psoci_ctx *c, const psoci_dav_opts *o, double *
         if ((s = sigma_block(w, w.V, ld, w.HV, ld, m, prec))) return s;
         sigma_calls += m;
         if ((s = tn(w, w.V, ld, 0, m, w.HV, ld, 0, m, w.G, ld, 0))) return s;
+        psoci_note_launch();
         k_symmetrize<<<1, 256, 0, st>>>(w.G, ld, 0, m);
         continue;
       }
@@ -601,6 +611,7 @@ psoci_status psoci_davidson_impl(psoci_ctx *c, const psoci_dav_opts *o, double *
     }
     int nsel = (int)sel.size();
     PSOCI_CUDA(c, cudaMemcpyAsync(w.sel, sel.data(), sizeof(int) * nsel, cudaMemcpyHostToDevice, st));
+    psoci_note_launch();
     k_precond<<<(int)std::min<int64_t>((N * nsel + 255) / 256, 152 * 16), 256, 0, st>>>(N, nr, w.R, c->d_diag, w.theta,
                                                                                          w.sel, nsel, dmin, w.T, nr);
     PSOCI_CUDA(c, cudaGetLastError());
@@ -608,9 +619,12 @@ psoci_status psoci_davidson_impl(psoci_ctx *c, const psoci_dav_opts *o, double *
       // collapse onto the lowest keep Ritz vectors (reference: 2*nroots), V and HV alike
       int keep = std::min(m, std::max(nr, std::min(2 * nr, maxsub - nsel)));
       if ((s = nn(w, w.V, ld, 0, m, w.Y, ld, 0, keep, 1.0, 0.0, w.tmp, 2 * nr, 0))) return s;
+      psoci_note_launch();
       k_copy_cols<<<152 * 8, 256, 0, st>>>(N, w.tmp, 2 * nr, 0, w.V, ld, 0, keep);
       if ((s = nn(w, w.HV, ld, 0, m, w.Y, ld, 0, keep, 1.0, 0.0, w.tmp, 2 * nr, 0))) return s;
+      psoci_note_launch();
       k_copy_cols<<<152 * 8, 256, 0, st>>>(N, w.tmp, 2 * nr, 0, w.HV, ld, 0, keep);
+      psoci_note_launch();
       k_diag_g<<<1, 256, 0, st>>>(w.G, ld, keep, w.theta);
       PSOCI_CUDA(c, cudaGetLastError());
       m = keep;
@@ -622,6 +636,7 @@ psoci_status psoci_davidson_impl(psoci_ctx *c, const psoci_dav_opts *o, double *
     if ((s = sigma_block(w, w.V + m, ld, w.HV + m, ld, bk, prec))) return s;
     sigma_calls += bk;
     if ((s = tn(w, w.V, ld, 0, m + bk, w.HV, ld, m, bk, w.G, ld, m))) return s;
+    psoci_note_launch();
     k_symmetrize<<<1, 256, 0, st>>>(w.G, ld, m, m + bk);
     PSOCI_CUDA(c, cudaGetLastError());
     m += bk;

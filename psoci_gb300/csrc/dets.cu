@@ -178,7 +178,6 @@ void psoci_dets_release(psoci_ctx *c) {
   psoci_free(c->d_tmpl);
   psoci_free(c->d_tmpl_ms);
   psoci_free(c->d_tmpl_off);
-  psoci_free(c->d_tinv);
   c->have_dets = false;
 }
 
@@ -222,16 +221,6 @@ psoci_status psoci_dets_build(psoci_ctx *c) {
       }
     }
   toff[NCLS * NOPEN_SLOTS] = (int32_t)tm.size();
-  // inverse table for configurations of up to 6 open shells: alpha mask over the open
-  // positions -> determinant index (or -1), per class; used by the fast element kernel
-  std::vector<int8_t> inv(NCLS * PSOCI_TINV_PER_CLASS, (int8_t)-1);
-  for (int cls = 0; cls < NCLS; ++cls)
-    for (int no = 0; no <= PSOCI_TINV_MAXOPEN; ++no) {
-      template_run(cls, no, run);
-      for (size_t d = 0; d < run.size(); ++d)
-        inv[cls * PSOCI_TINV_PER_CLASS + ((1 << no) - 1) + run[d].amask] = (int8_t)d;
-    }
-
   psoci_status st;
   if ((st = psoci_alloc(c, &c->d_sefoff, n + 1)) || (st = psoci_alloc(c, &c->d_detoff, n + 1)) ||
       (st = psoci_alloc(c, &c->d_alpha, (size_t)c->ndet_total * c->words)) ||
@@ -239,8 +228,7 @@ psoci_status psoci_dets_build(psoci_ctx *c) {
       (st = psoci_alloc(c, &c->d_phase, (size_t)c->ndet_total)) ||
       (st = psoci_alloc(c, &c->d_nalpha, (size_t)c->ndet_total)) ||
       (st = psoci_alloc(c, &c->d_ms, (size_t)c->ndet_total)) || (st = psoci_alloc(c, &c->d_tmpl, tm.size())) ||
-      (st = psoci_alloc(c, &c->d_tmpl_ms, tms.size())) || (st = psoci_alloc(c, &c->d_tmpl_off, toff.size())) ||
-      (st = psoci_alloc(c, &c->d_tinv, inv.size())))
+      (st = psoci_alloc(c, &c->d_tmpl_ms, tms.size())) || (st = psoci_alloc(c, &c->d_tmpl_off, toff.size())))
     return st;
   cudaStream_t s = c->stream;
   PSOCI_CUDA(c, cudaMemcpyAsync(c->d_sefoff, c->h_sefoff.data(), sizeof(int64_t) * (n + 1), cudaMemcpyHostToDevice, s));
@@ -249,12 +237,12 @@ psoci_status psoci_dets_build(psoci_ctx *c) {
   PSOCI_CUDA(c, cudaMemcpyAsync(c->d_tmpl, tm.data(), sizeof(uint32_t) * tm.size(), cudaMemcpyHostToDevice, s));
   PSOCI_CUDA(c, cudaMemcpyAsync(c->d_tmpl_ms, tms.data(), sizeof(int32_t) * tms.size(), cudaMemcpyHostToDevice, s));
   PSOCI_CUDA(c, cudaMemcpyAsync(c->d_tmpl_off, toff.data(), sizeof(int32_t) * toff.size(), cudaMemcpyHostToDevice, s));
-  PSOCI_CUDA(c, cudaMemcpyAsync(c->d_tinv, inv.data(), inv.size(), cudaMemcpyHostToDevice, s));
 
   int threads = 256;
   int64_t warps = n;
   int blocks = (int)std::min<int64_t>((warps * 32 + threads - 1) / threads, 152 * 64);
   if (blocks < 1) blocks = 1;
+  psoci_note_launch();
   if (c->words == 1)
     k_build_dets<1><<<blocks, threads, 0, s>>>(n, c->nelec, c->ksym, c->mx_open / 2, c->d_e1, c->d_e2, c->d_jsym,
                                                 c->d_nopen, c->d_detoff, c->d_tmpl, c->d_tmpl_ms, c->d_tmpl_off,

@@ -13,16 +13,24 @@
 // Storage.  The reference keeps the lower triangle and runs a symmetric product.  On one
 // GPU the full matrix in CSR streams twice the bytes but needs no scattered atomics in
 // sigma, so both triangles are stored.  Every off-diagonal element is the reference's
-// lower-triangle value: a block (I, J) with J > I is evaluated as the reference's block
-// (J, I) and transposed, and the upper half of a diagonal block mirrors its lower half.
-// Rows are written in ascending column order, deterministically, without atomics:
+// lower-triangle value: only the blocks (I, J <= I) are evaluated, as the reference does,
+// and the upper half of the matrix is their mirror image.  Rows are written in ascending
+// column order, deterministically:
 //
-//   1. screen:  per configuration, the sorted list of configurations within two
-//               excitations (XOR + popcount on occupancy bit-planes);
-//   2. segments of <= 32 neighbours per row configuration, one warp each;
-//   3. count:   each warp evaluates its SEF elements and counts kept ones per row;
-//   4. scan:    per-row totals -> rowptr; per-segment row offsets;
-//   5. fill:    the same evaluation writes columns and values at those offsets.
+//   1. screen:   per configuration, the sorted list of configurations within two
+//                excitations (XOR + popcount on occupancy bit-planes), then the blocks
+//                that the integrals alone make zero are dropped;
+//   2. segments: the lower neighbours (J <= I) of each row configuration in groups of <= 32,
+//                one warp each;
+//   3. evaluate: each warp marks the SEF elements that determinant connectivity allows and
+//                evaluates them; kept values go to slab slots, per (pair, row SEF) a mask of
+//                kept columns (fast path, <= 32 determinants per configuration);
+//   4. rows:     full row lengths = lower counts + the mirrored columns of upper neighbours;
+//   5. assemble: columns and values in order, the FP32 copy and the diagonal.
+//
+// Configurations with more than 32 determinants (7-11 open shells) take the generic path:
+// every block (I, J) of the full neighbour list is evaluated in a count pass and again in
+// a fill pass (a block with J > I as the reference's block (J, I), transposed).
 //
 // Floating point follows the reference's operation order; this file is compiled with
 // --fmad=false so products and sums round as the reference's do.
@@ -66,7 +74,6 @@ struct Params {
   const uint64_t *alpha, *beta;
   const uint8_t *phase, *nalpha;
   const double *one, *eri;
-  const int8_t *tinv;       // alpha open-shell mask -> det index (<= 6 open shells)
   // screen
   const int64_t *nbroff;
   int32_t *nbr;
@@ -77,11 +84,15 @@ struct Params {
   const int32_t *seg_n;
   const int64_t *seg_rowoff;
   int64_t *seg_cnt;        // count pass output / fill pass row offsets (local)
-  // single-pass fast build: kept entries are appended to slab slots, then copied in order
+  // single-pass fast build over the lower pairs (J <= I): kept values are appended to slab
+  // slots; per (pair, row SEF) a mask of kept columns and the pair's offset in the slot
+  const int64_t *segoff;   // first segment of each configuration
+  const int64_t *nlow;     // neighbours J <= I
+  const int64_t *pr_off;   // first (pair, row) mask of each configuration
+  uint32_t *prm;           // bits 0-15: kept column SEFs t; bits 16-31: offset in the slot
   int64_t *seg_slot;       // slab position of each (segment, row)
   unsigned long long *slab_counter;
   int64_t slab_cap;
-  int32_t *slab_col;
   double *slab_val;
   const int64_t *rowptr;
   int32_t *col;
@@ -134,6 +145,20 @@ __device__ __forceinline__ int second_bit(const uint64_t *x) {
   return lowest_bit<W>(y);
 }
 __device__ __forceinline__ bool bit_at(const uint64_t *x, int p) { return (x[p >> 6] >> (p & 63)) & 1ull; }
+// register-array forms: word selection by value, so that the arrays stay in registers
+template <int W>
+__device__ __forceinline__ bool bit_w(const uint64_t (&x)[W], int p) {
+  uint64_t v = x[0];
+#pragma unroll
+  for (int w = 1; w < W; ++w)
+    if ((p >> 6) == w) v = x[w];
+  return (v >> (p & 63)) & 1ull;
+}
+template <int W>
+__device__ __forceinline__ void sel_w(uint64_t (&d)[W], bool c, const uint64_t (&a)[W], const uint64_t (&b)[W]) {
+#pragma unroll
+  for (int w = 0; w < W; ++w) d[w] = c ? a[w] : b[w];
+}
 
 __device__ __forceinline__ double g2(const Params &P, int i, int j, int k, int l) { return __ldg(P.eri + canon4(i, j, k, l)); }
 __device__ __forceinline__ double g1(const Params &P, int i, int j) { return __ldg(P.one + tri64(i, j)); }
@@ -294,23 +319,24 @@ __global__ void k_screen_offsets(int nconf, int nsplit, const int64_t *cnt, int6
   tot[i] = run;
 }
 
-// per configuration: number of segments and segment-row slots
-__global__ void k_seg_counts(int nconf, const int64_t *nbroff, const int64_t *sefoff, int64_t *nseg_i,
-                             int64_t *nrow_i) {
+// per configuration: number of segments and segment-row slots over its first nlen[i]
+// neighbours (all of them when nlen is null)
+__global__ void k_seg_counts(int nconf, const int64_t *nbroff, const int64_t *nlen, const int64_t *sefoff,
+                             int64_t *nseg_i, int64_t *nrow_i) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nconf) return;
-  int64_t nn = nbroff[i + 1] - nbroff[i];
+  int64_t nn = nlen ? nlen[i] : nbroff[i + 1] - nbroff[i];
   int64_t ns = (nn + PSOCI_SEG - 1) / PSOCI_SEG;
   nseg_i[i] = ns;
   nrow_i[i] = ns * (sefoff[i + 1] - sefoff[i]);
 }
 
-__global__ void k_seg_init(int nconf, const int64_t *nbroff, const int64_t *sefoff, const int64_t *segoff,
-                           const int64_t *rowslot, int32_t *seg_cfg, int64_t *seg_k0, int32_t *seg_n,
-                           int64_t *seg_rowoff) {
+__global__ void k_seg_init(int nconf, const int64_t *nbroff, const int64_t *nlen, const int64_t *sefoff,
+                           const int64_t *segoff, const int64_t *rowslot, int32_t *seg_cfg, int64_t *seg_k0,
+                           int32_t *seg_n, int64_t *seg_rowoff) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nconf) return;
-  int64_t nn = nbroff[i + 1] - nbroff[i];
+  int64_t nn = nlen ? nlen[i] : nbroff[i + 1] - nbroff[i];
   int64_t s0 = segoff[i], ns = segoff[i + 1] - s0;
   int64_t nsef = sefoff[i + 1] - sefoff[i];
   for (int64_t s = 0; s < ns; ++s) {
@@ -320,6 +346,21 @@ __global__ void k_seg_init(int nconf, const int64_t *nbroff, const int64_t *sefo
     seg_n[s0 + s] = (int32_t)(left < PSOCI_SEG ? left : PSOCI_SEG);
     seg_rowoff[s0 + s] = rowslot[i] + s * nsef;
   }
+}
+
+// per configuration: nlow = neighbours J <= i (the lists are sorted ascending) and the
+// number of (lower pair, row SEF) mask slots, nlow * nsef_i
+__global__ void k_lower_counts(int nconf, const int64_t *nbroff, const int32_t *nbr, const int64_t *sefoff,
+                               int64_t *nlow, int64_t *prrows) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nconf) return;
+  int64_t lo = nbroff[i], hi = nbroff[i + 1];
+  while (lo < hi) {  // first entry > i
+    int64_t mid = (lo + hi) >> 1;
+    if (nbr[mid] <= (int32_t)i) lo = mid + 1; else hi = mid;
+  }
+  nlow[i] = lo - nbroff[i];
+  prrows[i] = nlow[i] * (sefoff[i + 1] - sefoff[i]);
 }
 
 // per configuration: exclusive scan over its segments of the per-row counts (in place),
@@ -344,6 +385,25 @@ __global__ void k_seg_rowscan(int nconf, const int64_t *sefoff, const int64_t *s
 // ------------------------------------------------------------------------------------
 // per-pair set-up (one lane per neighbour)
 // ------------------------------------------------------------------------------------
+// The first two positions of the multiset m1 + m2 (a position in both counts twice),
+// ascending.
+template <int W>
+__device__ __forceinline__ void two_positions(const uint64_t (&m1)[W], const uint64_t (&m2)[W], int &p0, int &p1) {
+  int nd = 0;
+#pragma unroll
+  for (int w = 0; w < W; ++w) {
+    uint64_t u = m1[w] | m2[w];
+    while (u && nd < 2) {
+      const int b = __ffsll((long long)u) - 1;
+      u &= u - 1;
+      const int p = 64 * w + b;
+      const int mult = (int)((m1[w] >> b) & 1ull) + (int)((m2[w] >> b) & 1ull);
+      if (nd == 0) { p0 = p; nd = 1; if (mult == 2) { p1 = p; nd = 2; } }
+      else { p1 = p; nd = 2; }
+    }
+  }
+}
+
 // Set up the pair (A, B) in the reference's roles (A = "iconf" of generateSOCIblocks);
 // J is the configuration whose SEFs are the CSR columns.
 template <int W>
@@ -386,7 +446,7 @@ __device__ void pair_setup_ab(const Params &P, int A, int B, int J, int swap, Pa
       while (oi) {
         int ib = 64 * wi + __ffsll((long long)oi) - 1;
         oi &= oi - 1;
-        int occi = 1 + (int)bit_at(e2A, ib);
+        int occi = 1 + (int)bit_w<W>(e2A, ib);
         if (occi == 1) v += g1(P, ib, ib);
         else v += 2.0 * g1(P, ib, ib) + g2(P, ib, ib, ib, ib);
 #pragma unroll
@@ -396,7 +456,7 @@ __device__ void pair_setup_ab(const Params &P, int A, int B, int J, int swap, Pa
             int jb = 64 * wj + __ffsll((long long)oj) - 1;
             oj &= oj - 1;
             if (jb >= ib) break;
-            int ninj = occi * (1 + (int)bit_at(e2A, jb));
+            int ninj = occi * (1 + (int)bit_w<W>(e2A, jb));
             if (ninj == 1) v += g2(P, ib, ib, jb, jb);
             else {
               double buf = 2.0 * g2(P, ib, ib, jb, jb);
@@ -440,9 +500,9 @@ __device__ void pair_setup_ab(const Params &P, int A, int B, int J, int swap, Pa
         o &= o - 1;
         double buf = g2(P, ie, je, p, p);
         v += buf;
-        bool dA = bit_at(e2A, p);
+        bool dA = bit_w<W>(e2A, p);
         if (dA) v += buf;
-        if (dA && bit_at(e2B, p)) v -= g2(P, ie, p, p, je);
+        if (dA && bit_w<W>(e2B, p)) v -= g2(P, ie, p, p, je);
       }
     }
     if (v == 0.0) { pi.kind = K_NONE; return; }
@@ -462,25 +522,11 @@ __device__ void pair_setup_ab(const Params &P, int A, int B, int J, int swap, Pa
   }
   if (ni == 2) {
     // ascending with multiplicity: a position in both masks appears twice
-    int ex[2], ney = 0, jy[2], nj = 0;
-    for (int pass = 0; pass < 2; ++pass) {
-      const uint64_t *m1 = pass == 0 ? im1 : jm1;
-      const uint64_t *m2 = pass == 0 ? im2 : jm2;
-      int *dst = pass == 0 ? ex : jy;
-      int &nd = pass == 0 ? ney : nj;
-#pragma unroll
-      for (int w = 0; w < W; ++w) {
-        uint64_t u = m1[w] | m2[w];
-        while (u && nd < 2) {
-          int b = __ffsll((long long)u) - 1;
-          u &= u - 1;
-          int p = 64 * w + b;
-          int mult = (int)((m1[w] >> b) & 1ull) + (int)((m2[w] >> b) & 1ull);
-          for (int q = 0; q < mult && nd < 2; ++q) dst[nd++] = p;
-        }
-      }
-    }
-    pi.iex0 = ex[0]; pi.iex1 = ex[1]; pi.jex0 = jy[0]; pi.jex1 = jy[1];
+    int ex0 = -1, ex1 = -1, jy0 = -1, jy1 = -1;
+    two_positions<W>(im1, im2, ex0, ex1);
+    two_positions<W>(jm1, jm2, jy0, jy1);
+    const int ex[2] = {ex0, ex1}, jy[2] = {jy0, jy1};
+    pi.iex0 = ex0; pi.iex1 = ex1; pi.jex0 = jy0; pi.jex1 = jy1;
     // processDoubleExcitation (PsociHamiltonian.C:180-184)
     double v0 = g2(P, ex[0], jy[0], ex[1], jy[1]);
     double v1 = g2(P, ex[0], jy[1], ex[1], jy[0]);
@@ -501,8 +547,19 @@ __device__ void pair_setup(const Params &P, int I, int J, PairInfo &pi, double *
 // ------------------------------------------------------------------------------------
 // determinant element <det a of A | H | det b of B>
 // ------------------------------------------------------------------------------------
+// The determinant tables and integrals det_elem reads, passed by value so that the
+// out-of-line function takes them in registers.
+struct DetTabs {
+  const uint64_t *alpha, *beta;
+  const uint8_t *phase, *nalpha;
+  const double *eri;
+};
+
+// Kept out of line: sef_elem calls it four times, and four inlined copies of this body
+// overflow the instruction cache of the evaluation kernels.
 template <int W>
-__device__ double det_elem(const Params &P, const PairInfo &pi, const double *Kd, int64_t da, int64_t db) {
+__device__ __noinline__ double det_elem(const DetTabs P, const PairInfo &pi, const double *Kd, int64_t da,
+                                        int64_t db) {
   uint64_t aa[W], ba[W], ab[W], bb[W];
 #pragma unroll
   for (int w = 0; w < W; ++w) {
@@ -534,7 +591,9 @@ __device__ double det_elem(const Params &P, const PairInfo &pi, const double *Kd
       if (pi.jsA % 2 == 1) ++ncount;
       if (abs(ie - je) > 1) {
         int lo = min(ie, je) + 1, hi = max(ie, je) - 1;
-        ncount += popc_range<W>(nmarka != 0 ? aa : ba, lo, hi);
+        uint64_t sp[W];
+        sel_w<W>(sp, nmarka != 0, aa, ba);
+        ncount += popc_range<W>(sp, lo, hi);
       }
     }
     return (ncount & 1) ? -pi.v0 : pi.v0;
@@ -554,17 +613,18 @@ __device__ double det_elem(const Params &P, const PairInfo &pi, const double *Kd
     }
     int mm = 0;
     for (int io = 1; io < ns; ++io) {
-      bool si = bit_at(aa, sing[io]);
+      bool si = bit_w<W>(aa, sing[io]);
       for (int jo = 0; jo < io; ++jo) {
         ++mm;
-        if (si == bit_at(aa, sing[jo])) v -= Kd[mm];
+        if (si == bit_w<W>(aa, sing[jo])) v -= Kd[mm];
       }
     }
     return v;
   }
   if (nmarkb == 1) {
     // one spin-orbital excitation within spin (nmarka == 1: alpha, else beta)
-    const uint64_t *sp = (nmarka != 0) ? aa : ba;
+    uint64_t sp[W];
+    sel_w<W>(sp, nmarka != 0, aa, ba);
     int ncount = pha + phb;
     if (abs(ie - je) > 1) ncount += popc_range<W>(sp, min(ie, je) + 1, max(ie, je) - 1);
     double v = pi.v0;
@@ -594,29 +654,32 @@ __device__ double det_elem(const Params &P, const PairInfo &pi, const double *Kd
     int ncount = pha + phb;
     if (abs(iex2 - iex3) > 1) ncount += popc_range<W>(aa, min(iex2, iex3) + 1, max(iex2, iex3) - 1);
     if (abs(jex2 - jex3) > 1) ncount += popc_range<W>(ba, min(jex2, jex3) + 1, max(jex2, jex3) - 1);
-    double v = g2(P, jex2, jex3, iex2, iex3);
+    double v = __ldg(P.eri + canon4(jex2, jex3, iex2, iex3));
     return (ncount & 1) ? -v : v;
   }
   // same-spin double (nmarka == 2: alpha, nmarka == 0: beta)
   if (pi.kind != K_DOUBLE) return 0.0;
-  const uint64_t *spb = (nmarka == 2) ? ab : bb;
-  const uint64_t *u = (nmarka == 2) ? ua : ub;
+  uint64_t spb[W], u[W], sa[W];
+  sel_w<W>(spb, nmarka == 2, ab, bb);
+  sel_w<W>(u, nmarka == 2, ua, ub);
+  sel_w<W>(sa, nmarka != 0, aa, ba);
   int u0 = lowest_bit<W>(u), u1 = second_bit<W>(u);
   int ncount = pha + phb + popc_range<W>(spb, u0 + 1, u1 - 1);
-  if (pi.iex1 - pi.iex0 > 1) ncount += popc_range<W>((nmarka != 0) ? aa : ba, pi.iex0 + 1, pi.iex1 - 1);
+  if (pi.iex1 - pi.iex0 > 1) ncount += popc_range<W>(sa, pi.iex0 + 1, pi.iex1 - 1);
   double v = pi.v0 - pi.v1;
   return (ncount & 1) ? -v : v;
 }
 
 // SEF element (a, b) of the reference block (A, B): ciout / transformCDCt
 template <int W>
-__device__ double sef_elem(const Params &P, const PairInfo &pi, const double *Kd, int a, int b) {
+__device__ double sef_elem(const Params &PP, const PairInfo &pi, const double *Kd, int a, int b) {
   if (pi.kind == K_NONE) return 0.0;
-  if (P.nelec & 1) return det_elem<W>(P, pi, Kd, pi.detA + a, pi.detB + b);
+  const DetTabs P = {PP.alpha, PP.beta, PP.phase, PP.nalpha, PP.eri};
+  if (PP.nelec & 1) return det_elem<W>(P, pi, Kd, pi.detA + a, pi.detB + b);
   const double r = sqrt(0.5);
   const bool oa = pi.nopenA != 0, ob = pi.nopenB != 0;
-  const double mA = (pi.jsA % 2 != P.ksym % 2) ? -1.0 : 1.0;
-  const double mB = (pi.jsB % 2 != P.ksym % 2) ? -1.0 : 1.0;
+  const double mA = (pi.jsA % 2 != PP.ksym % 2) ? -1.0 : 1.0;
+  const double mB = (pi.jsB % 2 != PP.ksym % 2) ? -1.0 : 1.0;
   int64_t a0 = pi.detA + (oa ? 2 * a : 0), a1 = a0 + 1;
   int64_t b0 = pi.detB + (ob ? 2 * b : 0), b1 = b0 + 1;
   double ds0, ds1 = 0.0;
@@ -728,43 +791,10 @@ __global__ void __launch_bounds__(WARPS_PER_CTA * 32) k_hbuild(Params P) {
 // ------------------------------------------------------------------------------------
 constexpr int FAST_MAXDET = 32;
 constexpr int FAST_MAXSEF = 16;
-
-// ------------------------------------------------------------------------------------
-// Candidate enumeration for the fast kernel: the determinants of J that a determinant a of
-// I can couple to, generated from the allowed spin-orbital substitutions and located
-// through the inverse template table (alpha open-shell mask -> determinant index).
-//   same configuration : a itself, and a with one alpha and one beta open shell swapped;
-//   single r -> s      : (r,sg) -> (s,sg); or (r,sg) -> (s,~sg) with an open shell p
-//                        flipped ~sg -> sg (keeps the spin projection);
-//   double r0 r1 -> s0 s1: two removals and two additions with equal alpha counts;
-//   spin-orbit r -> s  : (r,sg) -> (s,tau), any spins.
-// det_connected() admits exactly these pairs, so the masks are unchanged — only cheaper.
-// ------------------------------------------------------------------------------------
-__device__ __forceinline__ int det_class_dev(int parity, int jsym, int ksym) {
-  if (parity == 1) return ((((jsym + 1) / 2) % 2) == 0) ? 3 : 2;
-  return ((jsym + 1) / 2 == (ksym + 1) / 2) ? 0 : 1;
-}
-
-template <int W>
-__device__ __forceinline__ int lookup_det(const uint64_t *ab, const uint64_t *SJ, const int8_t *inv) {
-  uint32_t m = 0;
-  int t = 0;
-#pragma unroll
-  for (int w = 0; w < W; ++w) {
-    uint64_t s = SJ[w];
-    while (s) {
-      const int b = __ffsll((long long)s) - 1;
-      s &= s - 1;
-      if ((ab[w] >> b) & 1ull) m |= 1u << t;
-      ++t;
-    }
-  }
-  return inv[m];
-}
+constexpr int FAST_MAXOPEN = 6;  // 2^(6-1) = 32 determinants
+constexpr int SLAB_CHUNK = 4096; // slab slots a warp takes at a time
 
 __device__ __forceinline__ bool tbit(const uint64_t *x, int p) { return (x[p >> 6] >> (p & 63)) & 1ull; }
-__device__ __forceinline__ void setb(uint64_t *x, int p) { x[p >> 6] |= 1ull << (p & 63); }
-__device__ __forceinline__ void clrb(uint64_t *x, int p) { x[p >> 6] &= ~(1ull << (p & 63)); }
 
 template <int W>
 struct FastSmem {
@@ -772,6 +802,10 @@ struct FastSmem {
   double K[MAXK];
   uint64_t ra[FAST_MAXDET * W], rb[FAST_MAXDET * W];
   uint8_t rna[FAST_MAXDET];
+  // phase 2, per row: marked columns of each neighbour, their exclusive prefix, kept columns
+  uint32_t mrow[PSOCI_SEG];
+  int pre[PSOCI_SEG];
+  uint32_t keep[PSOCI_SEG];
 };
 
 // may det (aA, bA) of A and det (aB, bB) of B have a non-zero element?
@@ -789,13 +823,11 @@ template <int W>
 __global__ void __launch_bounds__(WARPS_PER_CTA * 32) k_hbuild_fast(Params P) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   FastSmem<W> *ws = reinterpret_cast<FastSmem<W> *>(smem_raw) + (threadIdx.x >> 5);
-  __shared__ int8_t ws_tinv[4 * PSOCI_TINV_PER_CLASS];
-  for (int e = threadIdx.x; e < 4 * PSOCI_TINV_PER_CLASS; e += blockDim.x) ws_tinv[e] = P.tinv[e];
-  __syncthreads();
   const int lane = threadIdx.x & 31;
   const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
   const bool odd = P.nelec & 1;
+  unsigned long long cursor = 0, chunk_end = 0;  // this warp's slab chunk
   for (int64_t s = warp; s < P.nseg; s += nwarps) {
     const int I = P.seg_cfg[s];
     const int64_t k0 = P.seg_k0[s];
@@ -823,26 +855,36 @@ __global__ void __launch_bounds__(WARPS_PER_CTA * 32) k_hbuild_fast(Params P) {
     // equal alpha counts, spin-orbit pairs c(a) <= 1 (det_connected's test).  The sets
     // {a : p in m_a} and {a : |m_a| = k} are warp ballots; c(a) is kept as a saturating
     // bit-sliced counter over all row dets at once.
-    uint32_t Ap[PSOCI_MAX_OPEN], Nk[PSOCI_MAX_OPEN + 1];
-    int sI[PSOCI_MAX_OPEN];
+    uint32_t Ap[FAST_MAXOPEN], Nk[FAST_MAXOPEN + 1];
+    int sI[FAST_MAXOPEN];
     uint64_t occI[W];
     {
       uint64_t SI[W];
-      int ns = 0;
 #pragma unroll
       for (int w = 0; w < W; ++w) {
         occI[w] = P.e1[(int64_t)I * W + w];
         SI[w] = occI[w] & ~P.e2[(int64_t)I * W + w];
-        uint64_t t = SI[w];
-        while (t && ns < PSOCI_MAX_OPEN) { sI[ns++] = 64 * w + __ffsll((long long)t) - 1; t &= t - 1; }
+      }
+      // open shells of I, ascending (fixed-size loops keep these arrays in registers)
+#pragma unroll
+      for (int p = 0; p < FAST_MAXOPEN; ++p) {
+        sI[p] = lowest_bit<W>(SI);
+        bool done = false;
+#pragma unroll
+        for (int w = 0; w < W; ++w)
+          if (!done && SI[w]) { SI[w] &= SI[w] - 1; done = true; }
       }
       uint32_t ma = 0u;
       if (lane < ndI)
-        for (int p = 0; p < nopI; ++p) ma |= (uint32_t)tbit(&ws->ra[lane * W], sI[p]) << p;
-      for (int p = 0; p < PSOCI_MAX_OPEN; ++p) Ap[p] = __ballot_sync(0xffffffffu, (lane < ndI) && ((ma >> p) & 1u));
-      for (int k = 0; k <= PSOCI_MAX_OPEN; ++k) Nk[k] = __ballot_sync(0xffffffffu, (lane < ndI) && __popc(ma) == k);
+#pragma unroll
+        for (int p = 0; p < FAST_MAXOPEN; ++p)
+          if (p < nopI) ma |= (uint32_t)tbit(&ws->ra[lane * W], sI[p]) << p;
+#pragma unroll
+      for (int p = 0; p < FAST_MAXOPEN; ++p) Ap[p] = __ballot_sync(0xffffffffu, (lane < ndI) && ((ma >> p) & 1u));
+#pragma unroll
+      for (int k = 0; k <= FAST_MAXOPEN; ++k) Nk[k] = __ballot_sync(0xffffffffu, (lane < ndI) && __popc(ma) == k);
     }
-    const int ndblI = P.nelec - 2 * 0 - nopI;  // electrons in I's doubly occupied orbitals (2 x count)
+    const int ndblI = P.nelec - nopI;  // electrons in I's doubly occupied orbitals
     uint32_t M[FAST_MAXSEF];
     for (int r = 0; r < FAST_MAXSEF; ++r) M[r] = 0u;
     if (lane < n) {
@@ -863,8 +905,10 @@ __global__ void __launch_bounds__(WARPS_PER_CTA * 32) k_hbuild_fast(Params P) {
           if (F > thr) continue;
           // saturating counter over the row dets: S0 (c'=0), S1, S2, S3 (>= 3)
           uint32_t S0 = 0xffffffffu, S1 = 0u, S2 = 0u;
-          for (int p = 0; p < nopI; ++p) {
-            const bool xa = tbit(ja, sI[p]), yb = tbit(jb, sI[p]);
+#pragma unroll
+          for (int p = 0; p < FAST_MAXOPEN; ++p) {
+            if (p >= nopI) break;
+            const bool xa = bit_w<W>(ja, sI[p]), yb = bit_w<W>(jb, sI[p]);
             if (xa) {  // mismatch where row det has beta on p
               const uint32_t T = ~Ap[p];
               S2 = (S2 & ~T) | (S1 & T);
@@ -884,7 +928,11 @@ __global__ void __launch_bounds__(WARPS_PER_CTA * 32) k_hbuild_fast(Params P) {
 #pragma unroll
             for (int w = 0; w < W; ++w) na += __popcll(ja[w]);
             const int need = na - (ndblI / 2);
-            ok &= (need >= 0 && need <= nopI) ? Nk[need] : 0u;
+            uint32_t nk = 0u;
+#pragma unroll
+            for (int k = 0; k <= FAST_MAXOPEN; ++k)
+              if (k == need) nk = Nk[k];
+            ok &= (need <= nopI) ? nk : 0u;
           }
           ok &= (ndI >= 32) ? 0xffffffffu : ((1u << ndI) - 1u);
           const int t = odd ? b : (nopJ ? (b >> 1) : 0);
@@ -896,98 +944,222 @@ __global__ void __launch_bounds__(WARPS_PER_CTA * 32) k_hbuild_fast(Params P) {
         }
       }
     }
-    // phase 2: evaluate marked elements row by row; rows keep ascending column order
+    // phase 2, row by row: the marked elements of the row, in (neighbour, column) order, are
+    // numbered e = 0..T-1 and lane e % 32 evaluates element e, so the lanes share the work
+    // whatever the spread of marks over the neighbours.  Kept values are compacted in the
+    // same order, so each row stays in ascending column order.  Each warp takes slab space
+    // in chunks and advances through a chunk by the kept count of each row.
+    const int64_t prbase = P.pr_off[I] + (k0 - P.nbroff[I]) * nsefI;
     for (int r = 0; r < nsefI; ++r) {
-      uint32_t keepm = 0u;
-      double vals[FAST_MAXSEF];
-      if (lane < n) {
-        const PairInfo &pi = ws->pi[lane];
-        uint32_t m = M[r];
-        while (m) {
+      const uint32_t mr = (lane < n) ? M[r] : 0u;
+      const int cm = __popc(mr);
+      int inclm = cm;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int v = __shfl_up_sync(0xffffffffu, inclm, o);
+        if (lane >= o) inclm += v;
+      }
+      const int T = __shfl_sync(0xffffffffu, inclm, 31);
+      ws->pre[lane] = inclm - cm;
+      ws->mrow[lane] = mr;
+      ws->keep[lane] = 0u;
+      if (cursor + T > chunk_end) {  // room for every marked element of the row
+        const unsigned long long len = (unsigned long long)max(T, SLAB_CHUNK);
+        unsigned long long b = 0;
+        if (lane == 0) b = atomicAdd(P.slab_counter, len);
+        cursor = __shfl_sync(0xffffffffu, b, 0);
+        chunk_end = cursor + len;
+      }
+      const unsigned long long base = cursor;
+      // chunks beyond the slab capacity are counted but not written; the host sees the
+      // final counter, enlarges the slab and evaluates again
+      const bool fits = (int64_t)chunk_end <= P.slab_cap;
+      __syncwarp();
+      int kc = 0;
+      for (int e0 = 0; e0 < T; e0 += 32) {
+        const int e = e0 + lane;
+        bool keep = false;
+        double v = 0.0;
+        if (e < T) {
+          int o = 0;  // the neighbour owning element e: last lane whose prefix is <= e
+#pragma unroll
+          for (int step = 16; step > 0; step >>= 1)
+            if (ws->pre[o + step] <= e) o += step;
+          uint32_t m = ws->mrow[o];
+          for (int q = e - ws->pre[o]; q > 0; --q) m &= m - 1;
           const int t = __ffs(m) - 1;
-          m &= m - 1;
+          const PairInfo &pi = ws->pi[o];
           // reference roles: the lower half of a diagonal block, block (J, I) for J > I
           const bool diag_blk = (pi.kind == K_DIAG);
           const bool flip = diag_blk ? (t > r) : (pi.swap != 0);
-          const double v = sef_elem<W>(P, pi, ws->K, flip ? t : r, flip ? r : t);
-          const bool keep = (fabs(v) >= PSOCI_MIN_VALUE) || (diag_blk && t == r);
-          if (keep) {
-            keepm |= 1u << t;
-            vals[t] = v;
-          }
+          v = sef_elem<W>(P, pi, ws->K, flip ? t : r, flip ? r : t);
+          keep = (fabs(v) >= PSOCI_MIN_VALUE) || (diag_blk && t == r);
+          if (keep) atomicOr(&ws->keep[o], 1u << t);
         }
+        const unsigned kb = __ballot_sync(0xffffffffu, keep);
+        if (keep && fits) P.slab_val[(int64_t)base + kc + __popc(kb & ((1u << lane) - 1u))] = v;
+        kc += __popc(kb);
       }
+      __syncwarp();
+      const uint32_t keepm = (lane < n) ? ws->keep[lane] : 0u;
       const int c = __popc(keepm);
       int incl = c;
 #pragma unroll
       for (int o = 1; o < 32; o <<= 1) {
-        int v = __shfl_up_sync(0xffffffffu, incl, o);
+        const int v = __shfl_up_sync(0xffffffffu, incl, o);
         if (lane >= o) incl += v;
       }
-      const int tot = __shfl_sync(0xffffffffu, incl, 31);
-      unsigned long long base = 0;
-      if (lane == 0 && tot > 0) base = atomicAdd(P.slab_counter, (unsigned long long)tot);
-      base = __shfl_sync(0xffffffffu, base, 0);
       if (lane == 0) {
-        P.seg_cnt[P.seg_rowoff[s] + r] = tot;
+        P.seg_cnt[P.seg_rowoff[s] + r] = kc;
         P.seg_slot[P.seg_rowoff[s] + r] = (int64_t)base;
       }
-      // entries beyond the slab capacity are counted but not written; the host sees the
-      // final counter, enlarges the slab and evaluates again
-      if (lane < n && (int64_t)(base + tot) <= P.slab_cap) {
-        const PairInfo &pi = ws->pi[lane];
-        int64_t pos = (int64_t)base + (incl - c);
-        uint32_t m = keepm;
-        while (m) {
-          const int t = __ffs(m) - 1;
-          m &= m - 1;
-          P.slab_col[pos] = (int32_t)(pi.colbase + t);
-          P.slab_val[pos] = vals[t];
-          ++pos;
-        }
-      }
+      if (lane < n) P.prm[prbase + (int64_t)lane * nsefI + r] = keepm | ((uint32_t)(incl - c) << 16);
+      cursor += (unsigned long long)kc;
+      __syncwarp();
     }
     __syncwarp();
   }
 }
 
-// per configuration: exclusive offsets over its segments of the per-row counts (into off),
-// totals per SEF row into row_nnz
-__global__ void k_seg_rowscan2(int nconf, const int64_t *sefoff, const int64_t *segoff, const int64_t *seg_rowoff,
-                               const int64_t *seg_cnt, int64_t *seg_off, int64_t *row_nnz) {
-  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= nconf) return;
-  int64_t nsef = sefoff[i + 1] - sefoff[i];
-  for (int64_t r = 0; r < nsef; ++r) {
-    int64_t run = 0;
-    for (int64_t s = segoff[i]; s < segoff[i + 1]; ++s) {
-      seg_off[seg_rowoff[s] + r] = run;
-      run += seg_cnt[seg_rowoff[s] + r];
-    }
-    row_nnz[sefoff[i] + r] = run;
-  }
-}
-
-// slab slots -> final CSR positions (segment order, so rows stay in column order)
-__global__ void k_slab_copy(Params P, const int64_t *seg_off) {
+// Full rows from the lower pairs.  Row r of configuration I holds, in ascending column order,
+// the kept entries of its lower pairs (J <= I, evaluated above; the diagonal block in full)
+// and, for every neighbour J > I, column r of the lower block (J, I): the entries whose
+// mask bit r is set in the (J, I) pair's rows t.  mk[k] is the position of I in J's list.
+//
+// One warp per configuration: row lengths, and I's position in each upper neighbour's list.
+__global__ void k_mirror_count(Params P, int64_t *row_nnz, int32_t *mk, int *err) {
   const int lane = threadIdx.x & 31;
   const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  for (int64_t s = warp; s < P.nseg; s += nwarps) {
-    const int I = P.seg_cfg[s];
+  for (int64_t I = warp; I < P.nconf; I += nwarps) {
+    const int64_t b0 = P.nbroff[I], nl = P.nlow[I], nn = P.nbroff[I + 1] - b0;
+    const int nsefI = (int)(P.sefoff[I + 1] - P.sefoff[I]);
+    int64_t low = 0;
+    if (lane < nsefI)
+      for (int64_t sg = P.segoff[I]; sg < P.segoff[I + 1]; ++sg) low += P.seg_cnt[P.seg_rowoff[sg] + lane];
+    int up[FAST_MAXSEF];
+#pragma unroll
+    for (int r = 0; r < FAST_MAXSEF; ++r) up[r] = 0;
+    for (int64_t k = nl + lane; k < nn; k += 32) {
+      const int J = P.nbr[b0 + k];
+      const int64_t jb = P.nbroff[J], je = jb + P.nlow[J];
+      int64_t lo = jb, hi = je;
+      while (lo < hi) {  // first entry >= I
+        const int64_t mid = (lo + hi) >> 1;
+        if (P.nbr[mid] < (int32_t)I) lo = mid + 1; else hi = mid;
+      }
+      if (lo >= je || P.nbr[lo] != (int32_t)I) {
+        atomicExch(err, 1);
+        mk[b0 + k] = -1;
+        continue;
+      }
+      mk[b0 + k] = (int32_t)(lo - jb);
+      const int nsefJ = (int)(P.sefoff[J + 1] - P.sefoff[J]);
+      const uint32_t *pm = P.prm + P.pr_off[J] + (lo - jb) * nsefJ;
+      for (int t = 0; t < nsefJ; ++t) {
+        const uint32_t m = pm[t];
+#pragma unroll
+        for (int r = 0; r < FAST_MAXSEF; ++r) up[r] += (int)((m >> r) & 1u);
+      }
+    }
+    int mine = 0;
+#pragma unroll
+    for (int r = 0; r < FAST_MAXSEF; ++r) {
+      int v = up[r];
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+      if (lane == r) mine = v;
+    }
+    if (lane < nsefI) row_nnz[P.sefoff[I] + lane] = low + mine;
+  }
+}
+
+// One warp per configuration: columns, values (and the FP32 copy and the diagonal) of its
+// rows; lane r carries the write position of row r.
+__global__ void k_assemble(Params P, const int32_t *mk) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t I = warp; I < P.nconf; I += nwarps) {
     const int64_t row0 = P.sefoff[I];
     const int nsefI = (int)(P.sefoff[I + 1] - row0);
-    for (int r = 0; r < nsefI; ++r) {
-      const int64_t slot = P.seg_rowoff[s] + r;
-      const int64_t cnt = P.seg_cnt[slot], src = P.seg_slot[slot];
-      const int64_t dst = P.rowptr[row0 + r] + seg_off[slot];
-      for (int64_t e = lane; e < cnt; e += 32) {
-        const int32_t cc = P.slab_col[src + e];
-        const double v = P.slab_val[src + e];
-        P.col[dst + e] = cc;
-        P.val[dst + e] = v;
-        if (P.val32) P.val32[dst + e] = (float)v;
-        if (cc == row0 + r) P.diag[row0 + r] = v;
+    const int64_t b0 = P.nbroff[I], nl = P.nlow[I], nn = P.nbroff[I + 1] - b0;
+    int64_t mypos = (lane < nsefI) ? P.rowptr[row0 + lane] : 0;
+    // lower pairs, segment by segment
+    for (int64_t sg = P.segoff[I]; sg < P.segoff[I + 1]; ++sg) {
+      const int64_t k0 = P.seg_k0[sg];
+      const int ns = P.seg_n[sg];
+      int J = -1;
+      int64_t colJ = 0;
+      if (lane < ns) { J = P.nbr[k0 + lane]; colJ = P.sefoff[J]; }
+      const uint32_t *pm = P.prm + P.pr_off[I] + (k0 - b0 + lane) * nsefI;
+      for (int r = 0; r < nsefI; ++r) {
+        const int64_t slot = P.seg_rowoff[sg] + r;
+        const int64_t dst = __shfl_sync(0xffffffffu, mypos, r);
+        if (lane < ns) {
+          const uint32_t w = pm[r];
+          uint32_t m = w & 0xffffu;
+          const int64_t src = P.seg_slot[slot] + (w >> 16), d0 = dst + (w >> 16);
+          int j = 0;
+          while (m) {
+            const int t = __ffs(m) - 1;
+            m &= m - 1;
+            const double v = P.slab_val[src + j];
+            P.col[d0 + j] = (int32_t)(colJ + t);
+            P.val[d0 + j] = v;
+            if (P.val32) P.val32[d0 + j] = (float)v;
+            if (J == (int)I && t == r) P.diag[row0 + r] = v;
+            ++j;
+          }
+        }
+        if (lane == r) mypos += P.seg_cnt[slot];
+      }
+    }
+    // upper neighbours, 32 at a time: column r of their lower block (J, I)
+    for (int64_t kc = nl; kc < nn; kc += 32) {
+      const int64_t k = kc + lane;
+      uint32_t mm[FAST_MAXSEF];
+#pragma unroll
+      for (int t = 0; t < FAST_MAXSEF; ++t) mm[t] = 0u;
+      int64_t colJ = 0, rowslotJ = 0;
+      if (k < nn) {
+        const int J = P.nbr[b0 + k];
+        const int kk = mk[b0 + k];
+        if (kk >= 0) {
+          const int nsefJ = (int)(P.sefoff[J + 1] - P.sefoff[J]);
+          colJ = P.sefoff[J];
+          rowslotJ = P.seg_rowoff[P.segoff[J] + kk / PSOCI_SEG];
+          const uint32_t *pm = P.prm + P.pr_off[J] + (int64_t)kk * nsefJ;
+#pragma unroll
+          for (int t = 0; t < FAST_MAXSEF; ++t)
+            if (t < nsefJ) mm[t] = pm[t];
+        }
+      }
+      for (int r = 0; r < nsefI; ++r) {
+        int cnt = 0;
+#pragma unroll
+        for (int t = 0; t < FAST_MAXSEF; ++t) cnt += (int)((mm[t] >> r) & 1u);
+        int incl = cnt;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const int v = __shfl_up_sync(0xffffffffu, incl, o);
+          if (lane >= o) incl += v;
+        }
+        const int tot = __shfl_sync(0xffffffffu, incl, 31);
+        int64_t d = __shfl_sync(0xffffffffu, mypos, r) + (incl - cnt);
+        const uint32_t below = (1u << r) - 1u;
+#pragma unroll
+        for (int t = 0; t < FAST_MAXSEF; ++t) {
+          if ((mm[t] >> r) & 1u) {
+            const int64_t src = P.seg_slot[rowslotJ + t] + (mm[t] >> 16) + __popc(mm[t] & below);
+            const double v = P.slab_val[src];
+            P.col[d] = (int32_t)(colJ + t);
+            P.val[d] = v;
+            if (P.val32) P.val32[d] = (float)v;
+            ++d;
+          }
+        }
+        if (lane == r) mypos += tot;
       }
     }
   }
@@ -1046,6 +1218,7 @@ psoci_status run_blocks(psoci_ctx *c, int npairs, const int32_t *hA, const int32
   cudaMemcpyAsync(dB, hB, sizeof(int32_t) * npairs, cudaMemcpyHostToDevice, st);
   cudaMemcpyAsync(doff, off.data(), sizeof(int64_t) * (npairs + 1), cudaMemcpyHostToDevice, st);
   int blocks = (int)std::max<int64_t>(1, std::min<int64_t>((npairs + WARPS_PER_CTA - 1) / WARPS_PER_CTA, 152 * 16));
+  psoci_note_launch();
   k_blocks<W><<<blocks, WARPS_PER_CTA * 32, 0, st>>>(P, npairs, dA, dB, doff, dout);
   cudaError_t e = cudaGetLastError();
   if (e == cudaSuccess) e = cudaMemcpyAsync(hout, dout, sizeof(double) * off[npairs], cudaMemcpyDeviceToHost, st);
@@ -1065,21 +1238,23 @@ psoci_status run_build(psoci_ctx *c, psoci_hmode mode, int64_t *nnz_out) {
   P.sefoff = c->d_sefoff; P.detoff = c->d_detoff;
   P.alpha = c->d_alpha; P.beta = c->d_beta; P.phase = c->d_phase; P.nalpha = c->d_nalpha;
   P.one = c->d_one; P.eri = c->d_eri;
-  P.tinv = c->d_tinv;
 
   psoci_status s;
   int64_t *d_cnt = nullptr, *d_nbroff = nullptr, *d_nseg = nullptr, *d_nrow = nullptr, *d_segoff = nullptr,
           *d_rowslot = nullptr, *d_segk0 = nullptr, *d_segrow = nullptr, *d_segcnt = nullptr, *d_rownnz = nullptr;
   int32_t *d_nbr = nullptr, *d_segcfg = nullptr, *d_segn = nullptr;
-  int64_t *d_soff = nullptr, *d_tot = nullptr, *d_segslot = nullptr, *d_segofs = nullptr, *d_candoff = nullptr;
-  int32_t *d_cand = nullptr;
+  int64_t *d_soff = nullptr, *d_tot = nullptr, *d_segslot = nullptr, *d_candoff = nullptr;
+  int64_t *d_nlow = nullptr, *d_prrows = nullptr, *d_proff = nullptr;
+  int32_t *d_cand = nullptr, *d_mk = nullptr;
+  uint32_t *d_prm = nullptr;
+  int *d_err = nullptr;
   unsigned long long *d_counter = nullptr;
-  int32_t *d_slabcol = nullptr;
   double *d_slabval = nullptr;
   auto cleanup = [&]() {
-    psoci_free(d_soff); psoci_free(d_tot); psoci_free(d_segslot); psoci_free(d_segofs); psoci_free(d_counter);
+    psoci_free(d_soff); psoci_free(d_tot); psoci_free(d_segslot); psoci_free(d_counter);
     psoci_free(d_candoff); psoci_free(d_cand);
-    psoci_free(d_slabcol); psoci_free(d_slabval);
+    psoci_free(d_nlow); psoci_free(d_prrows); psoci_free(d_proff); psoci_free(d_mk); psoci_free(d_prm);
+    psoci_free(d_err); psoci_free(d_slabval);
     psoci_free(d_cnt); psoci_free(d_nbroff); psoci_free(d_nseg); psoci_free(d_nrow); psoci_free(d_segoff);
     psoci_free(d_rowslot); psoci_free(d_segk0); psoci_free(d_segrow); psoci_free(d_segcnt); psoci_free(d_rownnz);
     psoci_free(d_nbr); psoci_free(d_segcfg); psoci_free(d_segn);
@@ -1119,22 +1294,27 @@ psoci_status run_build(psoci_ctx *c, psoci_hmode mode, int64_t *nnz_out) {
   TRY(psoci_alloc(c, &d_candoff, n + 1));
   TRY(psoci_alloc(c, &d_nbroff, n + 1));
   dim3 scr_grid(scr_rows, nsplit);
+  psoci_note_launch();
   k_screen<W, 0><<<scr_grid, SCR_THREADS, 0, st>>>(P, d_cnt, nullptr, chunk, nullptr, nullptr);
   TRYC(cudaGetLastError());
+  psoci_note_launch();
   k_screen_offsets<<<(n + 255) / 256, 256, 0, st>>>(n, nsplit, d_cnt, d_soff, d_tot);
   TRYC(cudaGetLastError());
   int64_t ncand = 0;
   TRY(psoci_scan_i64(c, d_tot, d_candoff, n, &ncand));
   TRY(psoci_alloc(c, &d_cand, ncand));
+  psoci_note_launch();
   k_screen<W, 1><<<scr_grid, SCR_THREADS, 0, st>>>(P, nullptr, d_soff, chunk, d_candoff, d_cand);
   TRYC(cudaGetLastError());
   const int prune_blocks = (int)std::max<int64_t>(1, std::min<int64_t>(((int64_t)n * 32 + 255) / 256, 152 * 32));
+  psoci_note_launch();
   k_prune<W, 0><<<prune_blocks, 256, 0, st>>>(P, d_candoff, d_cand, d_tot);
   TRYC(cudaGetLastError());
   int64_t npairs = 0;
   TRY(psoci_scan_i64(c, d_tot, d_nbroff, n, &npairs));
   TRY(psoci_alloc(c, &d_nbr, npairs));
   P.nbroff = d_nbroff; P.nbr = d_nbr;
+  psoci_note_launch();
   k_prune<W, 1><<<prune_blocks, 256, 0, st>>>(P, d_candoff, d_cand, nullptr);
   TRYC(cudaGetLastError());
   psoci_free(d_cand);
@@ -1142,12 +1322,28 @@ psoci_status run_build(psoci_ctx *c, psoci_hmode mode, int64_t *nnz_out) {
   c->npairs = npairs;
   auto t_b = tnow();
 
+  // fast path: only the lower pairs (J <= I) are evaluated; the rest are mirrored
+  const bool fast = c->max_ndet <= FAST_MAXDET;
+  int64_t nprm = 0;
+  if (fast) {
+    TRY(psoci_alloc(c, &d_nlow, n + 1));
+    TRY(psoci_alloc(c, &d_prrows, n + 1));
+    TRY(psoci_alloc(c, &d_proff, n + 1));
+    psoci_note_launch();
+    k_lower_counts<<<(n + 255) / 256, 256, 0, st>>>(n, d_nbroff, d_nbr, c->d_sefoff, d_nlow, d_prrows);
+    TRYC(cudaGetLastError());
+    TRY(psoci_scan_i64(c, d_prrows, d_proff, n, &nprm));
+    TRY(psoci_alloc(c, &d_prm, nprm));
+    P.nlow = d_nlow; P.pr_off = d_proff; P.prm = d_prm;
+  }
+
   // 2. segments
   TRY(psoci_alloc(c, &d_nseg, n + 1));
   TRY(psoci_alloc(c, &d_nrow, n + 1));
   TRY(psoci_alloc(c, &d_segoff, n + 1));
   TRY(psoci_alloc(c, &d_rowslot, n + 1));
-  k_seg_counts<<<(n + 255) / 256, 256, 0, st>>>(n, d_nbroff, c->d_sefoff, d_nseg, d_nrow);
+  psoci_note_launch();
+  k_seg_counts<<<(n + 255) / 256, 256, 0, st>>>(n, d_nbroff, d_nlow, c->d_sefoff, d_nseg, d_nrow);
   TRYC(cudaGetLastError());
   int64_t nseg = 0, nslots = 0;
   TRY(psoci_scan_i64(c, d_nseg, d_segoff, n, &nseg));
@@ -1157,67 +1353,78 @@ psoci_status run_build(psoci_ctx *c, psoci_hmode mode, int64_t *nnz_out) {
   TRY(psoci_alloc(c, &d_segn, nseg));
   TRY(psoci_alloc(c, &d_segrow, nseg));
   TRY(psoci_alloc(c, &d_segcnt, nslots));
-  k_seg_init<<<(n + 255) / 256, 256, 0, st>>>(n, d_nbroff, c->d_sefoff, d_segoff, d_rowslot, d_segcfg, d_segk0, d_segn,
-                                              d_segrow);
+  psoci_note_launch();
+  k_seg_init<<<(n + 255) / 256, 256, 0, st>>>(n, d_nbroff, d_nlow, c->d_sefoff, d_segoff, d_rowslot, d_segcfg, d_segk0,
+                                              d_segn, d_segrow);
   TRYC(cudaGetLastError());
   c->nseg = nseg;
   P.nseg = nseg; P.seg_cfg = d_segcfg; P.seg_k0 = d_segk0; P.seg_n = d_segn; P.seg_rowoff = d_segrow;
-  P.seg_cnt = d_segcnt;
+  P.seg_cnt = d_segcnt; P.segoff = d_segoff;
 
-  // 3. count
-  const bool fast = c->max_ndet <= FAST_MAXDET;
+  // 3. evaluate
   int hb_blocks = (int)std::max<int64_t>(1, std::min<int64_t>((nseg + WARPS_PER_CTA - 1) / WARPS_PER_CTA, 152 * 16));
   const int64_t N = c->nsef_total;
   int64_t nnz = 0;
   auto t_c = tnow();
   auto t_d = t_c, t_e = t_c;
   if (fast) {
-    // 3. evaluate once: kept entries go to slab slots
+    // 3. evaluate the lower pairs once: kept values go to slab slots, masks to prm
     const size_t smem = sizeof(FastSmem<W>) * WARPS_PER_CTA;
     TRYC(cudaFuncSetAttribute(k_hbuild_fast<W>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     TRY(psoci_alloc(c, &d_segslot, nslots));
     TRY(psoci_alloc(c, &d_counter, 1));
     size_t freeb = 0, totb = 0;
     TRYC(cudaMemGetInfo(&freeb, &totb));
-    // first guess from the pair count (observed 2-4 kept elements per pair); an overflow is
-    // detected by the kernel's counter and the evaluation repeats with the exact size
-    int64_t cap = std::min<int64_t>((int64_t)(freeb * 0.35) / 12, 8 * npairs + (1 << 20));
+    // slots hold the kept elements of the lower pairs plus the unused tails of the warps'
+    // chunks; first guess from the pair count (observed 2.5-5.5 kept elements per lower
+    // pair, about half the pairs lower); an overflow is detected by the kernel's counter
+    // and the evaluation repeats with the exact size
+    const int64_t tails = (int64_t)hb_blocks * WARPS_PER_CTA * SLAB_CHUNK;
+    int64_t cap = std::min<int64_t>((int64_t)(freeb * 0.35) / 8, 3 * npairs + tails);
+    int64_t nlower = 0;
     for (int attempt = 0; attempt < 2; ++attempt) {
-      TRY(psoci_alloc(c, &d_slabcol, cap));
       TRY(psoci_alloc(c, &d_slabval, cap));
       TRYC(cudaMemsetAsync(d_counter, 0, sizeof(unsigned long long), st));
-      P.seg_slot = d_segslot; P.slab_counter = d_counter; P.slab_cap = cap;
-      P.slab_col = d_slabcol; P.slab_val = d_slabval;
+      P.seg_slot = d_segslot; P.slab_counter = d_counter; P.slab_cap = cap; P.slab_val = d_slabval;
+      psoci_note_launch();
       k_hbuild_fast<W><<<hb_blocks, WARPS_PER_CTA * 32, smem, st>>>(P);
       TRYC(cudaGetLastError());
       unsigned long long used = 0;
       TRYC(cudaMemcpyAsync(&used, d_counter, sizeof(used), cudaMemcpyDeviceToHost, st));
       TRYC(cudaStreamSynchronize(st));
-      nnz = (int64_t)used;
-      if (nnz <= cap) break;
-      psoci_free(d_slabcol);
+      nlower = (int64_t)used;
+      if (c->verbose)
+        fprintf(stderr, "psoci: H build slab %lld of %lld slots used\n", (long long)nlower, (long long)cap);
+      if (nlower <= cap) break;
       psoci_free(d_slabval);
-      cap = nnz;
+      cap = nlower + tails;  // chunk tails differ from run to run
       if (attempt == 1) TRY(psoci_fail(c, PSOCI_ERR_NOMEM, "H build: element slab overflow"));
     }
     t_d = tnow();
-    // 4. offsets
+    // 4. full row lengths (lower counts + mirrored columns) and offsets
     TRY(psoci_alloc(c, &d_rownnz, N + 1));
-    TRY(psoci_alloc(c, &d_segofs, nslots));
-    k_seg_rowscan2<<<(n + 127) / 128, 128, 0, st>>>(n, c->d_sefoff, d_segoff, d_segrow, d_segcnt, d_segofs, d_rownnz);
+    TRY(psoci_alloc(c, &d_mk, npairs));
+    TRY(psoci_alloc(c, &d_err, 1));
+    TRYC(cudaMemsetAsync(d_err, 0, sizeof(int), st));
+    const int cfg_blocks = (int)std::max<int64_t>(1, std::min<int64_t>(((int64_t)n * 32 + 255) / 256, 152 * 32));
+    psoci_note_launch();
+    k_mirror_count<<<cfg_blocks, 256, 0, st>>>(P, d_rownnz, d_mk, d_err);
     TRYC(cudaGetLastError());
+    int herr = 0;
+    TRYC(cudaMemcpyAsync(&herr, d_err, sizeof(int), cudaMemcpyDeviceToHost, st));
     TRY(psoci_alloc(c, &c->d_rowptr, N + 1));
-    int64_t nnz2 = 0;
-    TRY(psoci_scan_i64(c, d_rownnz, c->d_rowptr, N, &nnz2));
-    if (nnz2 != nnz) TRY(psoci_fail(c, PSOCI_ERR_CUDA, "H build: slab and row counts differ"));
+    TRY(psoci_scan_i64(c, d_rownnz, c->d_rowptr, N, &nnz));
+    if (herr) TRY(psoci_fail(c, PSOCI_ERR_CUDA, "H build: neighbour lists are not symmetric"));
+    if (nnz < N) TRY(psoci_fail(c, PSOCI_ERR_CUDA, "H build: rows without their diagonal element"));
     TRY(psoci_alloc(c, &c->d_col, nnz));
     TRY(psoci_alloc(c, &c->d_val, nnz));
     if (mode == PSOCI_HMODE_CSR_BOTH) TRY(psoci_alloc(c, &c->d_val32, nnz));
     TRY(psoci_alloc(c, &c->d_diag, N));
     P.rowptr = c->d_rowptr; P.col = c->d_col; P.val = c->d_val; P.val32 = c->d_val32; P.diag = c->d_diag;
     t_e = tnow();
-    // 5. ordered copy
-    k_slab_copy<<<hb_blocks * 4, 256, 0, st>>>(P, d_segofs);
+    // 5. ordered assembly
+    psoci_note_launch();
+    k_assemble<<<cfg_blocks, 256, 0, st>>>(P, d_mk);
     TRYC(cudaGetLastError());
     TRYC(cudaStreamSynchronize(st));
   } else {
@@ -1225,11 +1432,13 @@ psoci_status run_build(psoci_ctx *c, psoci_hmode mode, int64_t *nnz_out) {
     TRYC(cudaFuncSetAttribute(k_hbuild<W, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     TRYC(cudaFuncSetAttribute(k_hbuild<W, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     // 3. count
+    psoci_note_launch();
     k_hbuild<W, 0><<<hb_blocks, WARPS_PER_CTA * 32, smem, st>>>(P);
     TRYC(cudaGetLastError());
     t_d = tnow();
     // 4. offsets
     TRY(psoci_alloc(c, &d_rownnz, N + 1));
+    psoci_note_launch();
     k_seg_rowscan<<<(n + 127) / 128, 128, 0, st>>>(n, c->d_sefoff, d_segoff, d_segrow, d_segcnt, d_rownnz);
     TRYC(cudaGetLastError());
     TRY(psoci_alloc(c, &c->d_rowptr, N + 1));
@@ -1241,6 +1450,7 @@ psoci_status run_build(psoci_ctx *c, psoci_hmode mode, int64_t *nnz_out) {
     P.rowptr = c->d_rowptr; P.col = c->d_col; P.val = c->d_val; P.val32 = c->d_val32; P.diag = c->d_diag;
     t_e = tnow();
     // 5. fill
+    psoci_note_launch();
     k_hbuild<W, 1><<<hb_blocks, WARPS_PER_CTA * 32, smem, st>>>(P);
     TRYC(cudaGetLastError());
     TRYC(cudaStreamSynchronize(st));

@@ -12,8 +12,6 @@
 #define PSOCI_MAX_WORDS 2     // nbf <= 128
 #define PSOCI_SEG 32          // neighbours per warp segment in the H build
 #define PSOCI_MIN_VALUE 1.0e-8  // packSefsef threshold (PsociHamiltonian.hpp:37)
-#define PSOCI_TINV_MAXOPEN 6    // inverse template table covers up to 6 open shells
-#define PSOCI_TINV_PER_CLASS 127  // sum over nopen 0..6 of 2^nopen entries
 
 // ------------------------------------------------------------------------------------
 // host-side context
@@ -61,7 +59,6 @@ struct psoci_ctx {
   uint32_t *d_tmpl = nullptr;   // packed: amask | bmask<<12 ; ms offset stored separately
   int32_t *d_tmpl_ms = nullptr;
   int32_t *d_tmpl_off = nullptr;  // [4*12+1] start of each (class, nopen) run
-  int8_t *d_tinv = nullptr;       // [4*127] alpha open-shell mask -> det index, nopen <= 6
 
   // Hamiltonian
   bool have_h = false;
@@ -114,6 +111,8 @@ void psoci_free(T *&p) {
 }
 
 // device-wide exclusive scan of int64 counts (in place allowed); returns total on host
+// counts one kernel launch (read back through psoci_launch_count)
+void psoci_note_launch();
 psoci_status psoci_scan_i64(psoci_ctx *c, const int64_t *d_in, int64_t *d_out, int64_t n, int64_t *total);
 
 // sigma (sigma.cu) — device pointers, row-major N x k with leading dims

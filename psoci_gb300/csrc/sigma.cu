@@ -196,6 +196,7 @@ void launch_k(psoci_ctx *c, int64_t n, const double *dX, int ldx, double *dY, in
   int64_t warps = n;
   int blocks = (int)std::min<int64_t>((warps * 32 + SIG_THREADS - 1) / SIG_THREADS, 152 * 8 * 4);
   if (blocks < 1) blocks = 1;
+  psoci_note_launch();
   if (prec == PSOCI_PREC_FP64)
     k_spmm_f64<K><<<blocks, SIG_THREADS, 0, c->stream>>>(n, c->d_rowptr, c->d_col, c->d_val, dX, ldx, dY, ldy,
                                                          ((uintptr_t)dX % 16 == 0) && (ldx % 2 == 0));
@@ -222,6 +223,7 @@ psoci_status psoci_sigma_launch(psoci_ctx *c, int k, const double *dX, int ldx, 
     if (prec == PSOCI_PREC_MIXED) {
       if (!dX32) return psoci_fail(c, PSOCI_ERR_INVALID_ARG, "sigma: MIXED without FP32 staging");
       int blocks = (int)std::min<int64_t>((n + 255) / 256, 152 * 16);
+      psoci_note_launch();
       k_to_f32<<<std::max(blocks, 1), 256, 0, c->stream>>>(n, kk, xs, ldx, dX32);
       x32 = dX32;
     }

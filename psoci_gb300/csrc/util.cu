@@ -1,7 +1,13 @@
 // Error helpers and the device-wide exclusive scan used by the builders.
+#include <atomic>
 #include <cstdio>
 
 #include "psoci_internal.cuh"
+
+// Process-wide count of kernels this library has launched (all contexts, all devices).
+static std::atomic<unsigned long long> g_launches{0};
+void psoci_note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+extern "C" unsigned long long psoci_launch_count(void) { return g_launches.load(std::memory_order_relaxed); }
 
 psoci_status psoci_fail(psoci_ctx *c, psoci_status s, const std::string &msg) {
   if (c) c->err = msg;
@@ -89,6 +95,7 @@ psoci_status psoci_scan_i64(psoci_ctx *c, const int64_t *d_in, int64_t *d_out, i
   if (st) return st;
   st = psoci_alloc(c, &d_bo, nb + 1);
   if (st) { psoci_free(d_bs); return st; }
+  psoci_note_launch();
   k_scan_chunk<<<(unsigned)nb, SCAN_T, 0, s>>>(d_in, nullptr, n, d_bs, nullptr);
   cudaError_t e = cudaGetLastError();
   if (e == cudaSuccess) {
@@ -101,10 +108,12 @@ psoci_status psoci_scan_i64(psoci_ctx *c, const int64_t *d_in, int64_t *d_out, i
     }
   }
   if (e == cudaSuccess && st == PSOCI_OK) {
+    psoci_note_launch();
     k_scan_chunk<<<(unsigned)nb, SCAN_T, 0, s>>>(d_in, d_out, n, nullptr, d_bo);
     e = cudaGetLastError();
   }
   if (e == cudaSuccess && st == PSOCI_OK) {
+    psoci_note_launch();
     k_write_total<<<1, 1, 0, s>>>(d_in, d_out, n, d_out + n);
     e = cudaGetLastError();
   }
