@@ -104,6 +104,25 @@ PSOCI_API psoci_status psoci_get_determinants(const psoci_ctx *ctx, uint64_t *al
  * (both triangles; each off-diagonal element is the reference's lower-triangle value), elements
  * with |x| >= 1e-8 or on the diagonal.  *nnz receives the stored count. */
 PSOCI_API psoci_status psoci_build_hamiltonian(psoci_ctx *ctx, psoci_hmode mode, int64_t *nnz);
+/* Counters and phase times of the last psoci_build_hamiltonian.  Times are CUDA-event
+ * intervals on the library stream, in milliseconds; the evaluation time covers the final
+ * attempt only (an undersized value slab makes the build evaluate twice).  The reference
+ * reports its build time through PsociTimer; there is no direct counterpart. */
+typedef struct {
+  int64_t candidates;    /* configuration pairs within two excitations (ordered)             */
+  int64_t pairs;         /* of those, pairs whose block is not zero from the integrals alone */
+  int64_t segments;      /* warp work items (<= 32 neighbours of one row configuration)      */
+  int64_t nnz;           /* stored elements, both triangles                                  */
+  int64_t nnz_lower;     /* the reference's lower-triangle count, (nnz + N) / 2              */
+  int64_t slab_slots;    /* value-slab slots taken by the evaluation                         */
+  int evaluations;       /* 1, or 2 after a slab overflow                                    */
+  int fast;              /* 1: lower blocks evaluated once and mirrored; 0: generic path      */
+  int lookup_screen;     /* 1: neighbours found by table lookup; 0: all-pairs test            */
+  int reserved;
+  double screen_ms, evaluate_ms, rows_ms, assemble_ms, total_ms;
+} psoci_build_info;
+PSOCI_API psoci_status psoci_build_stats(const psoci_ctx *ctx, psoci_build_info *info);
+
 /* Replaces PsociHamiltonian::generateSOCIblocks (PsociHamiltonian.C:401-558) for a batch of
  * configuration pairs: block q is the reference's nsef_A x nsef_B sefsef matrix for
  * (A[q], B[q]) in the reference's roles, row-major, stored consecutively in out (host) in

@@ -42,6 +42,10 @@ def main(argv=None):
         tb = time.perf_counter() - t0
         print(f"workload {a.workload}: configurations {p.nconf}, SEFs {c.nsef}, stored elements {nnz}, "
               f"build {tb:.3f} s")
+        if a.verbose:
+            b = c.build_stats()
+            print("build phases (CUDA events, ms): " + ", ".join(
+                f"{k[:-3]} {b[k]:.2f}" for k in ("screen_ms", "evaluate_ms", "rows_ms", "assemble_ms", "total_ms")))
         if a.sigma:
             X = np.random.default_rng(0).standard_normal((c.nsef, a.sigma))
             Y = c.sigma(X, prec=api.PREC_MIXED if mixed else api.PREC_FP64)

@@ -40,6 +40,18 @@ class DavOpts(ctypes.Structure):
                 ("precond_min", ctypes.c_double)]
 
 
+class BuildInfo(ctypes.Structure):
+    _fields_ = [("candidates", ctypes.c_int64), ("pairs", ctypes.c_int64), ("segments", ctypes.c_int64),
+                ("nnz", ctypes.c_int64), ("nnz_lower", ctypes.c_int64), ("slab_slots", ctypes.c_int64),
+                ("evaluations", ctypes.c_int), ("fast", ctypes.c_int), ("lookup_screen", ctypes.c_int),
+                ("reserved", ctypes.c_int),
+                ("screen_ms", ctypes.c_double), ("evaluate_ms", ctypes.c_double), ("rows_ms", ctypes.c_double),
+                ("assemble_ms", ctypes.c_double), ("total_ms", ctypes.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 class DavStats(ctypes.Structure):
     _fields_ = [("iterations", ctypes.c_int), ("sigma_calls", ctypes.c_int), ("collapses", ctypes.c_int),
                 ("refine_iters", ctypes.c_int), ("seconds", ctypes.c_double), ("sigma_seconds", ctypes.c_double)]
@@ -75,6 +87,7 @@ SIGNATURES = {
     "psoci_core_energy": (ctypes.c_double, [_P]),
     "psoci_stream": (ctypes.c_void_p, [_P]),
     "psoci_launch_count": (ctypes.c_ulonglong, []),
+    "psoci_build_stats": (ctypes.c_int, [_P, ctypes.POINTER(BuildInfo)]),
     "psoci_sigma_mixed_noalloc": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
                                                  ctypes.c_int]),
     "psoci_set_guess": (ctypes.c_int, [_P, ctypes.c_int, _DP]),
@@ -292,6 +305,12 @@ class Context:
     def stream_handle(self) -> int:
         """cudaStream_t of this context (for CUDA events on the launching stream)."""
         return int(self.lib.psoci_stream(self.ctx) or 0)
+
+    def build_stats(self) -> dict:
+        """Counters and CUDA-event phase times (ms) of the last Hamiltonian build."""
+        b = BuildInfo()
+        self._check(self.lib.psoci_build_stats(self.ctx, ctypes.byref(b)), "build_stats")
+        return b.as_dict()
 
     def launch_count(self) -> int:
         """Kernels the library has launched in this process so far (all contexts)."""

@@ -16,6 +16,7 @@ psoci_status set_device(psoci_ctx *c) {
 void release_all(psoci_ctx *c) {
   psoci_h_release(c);
   psoci_dets_release(c);
+  psoci_join_release(c);
   psoci_free(c->d_one);
   psoci_free(c->d_eri);
   psoci_free(c->d_e1);
@@ -84,6 +85,13 @@ void psoci_destroy(psoci_ctx *c) {
 }
 
 double psoci_core_energy(const psoci_ctx *c) { return c ? c->ecore : 0.0; }
+
+psoci_status psoci_build_stats(const psoci_ctx *c, psoci_build_info *info) {
+  if (!c || !info) return PSOCI_ERR_INVALID_ARG;
+  if (!c->have_h) return psoci_fail(const_cast<psoci_ctx *>(c), PSOCI_ERR_STATE, "build_stats: no Hamiltonian built");
+  *info = c->binfo;
+  return PSOCI_OK;
+}
 
 void *psoci_stream(const psoci_ctx *c) { return c ? (void *)c->stream : nullptr; }
 
@@ -161,8 +169,9 @@ psoci_status psoci_set_configs(psoci_ctx *c, int nbf, int nelec, int ksym, int m
   c->words = W;
   c->h_jsym.assign(jsym, jsym + nconf);
   c->h_occ.assign(occ, occ + (size_t)nconf * nbf);
+  c->slab_hint = 0;
   c->have_cfgs = true;
-  return PSOCI_OK;
+  return psoci_join_prepare(c);
 }
 
 psoci_status psoci_build_determinants(psoci_ctx *c) {

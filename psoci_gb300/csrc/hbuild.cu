@@ -37,6 +37,9 @@
 #include <algorithm>
 #include <chrono>
 #include <cstdio>
+#include <functional>
+#include <queue>
+#include <vector>
 
 #include "psoci_internal.cuh"
 
@@ -144,7 +147,6 @@ __device__ __forceinline__ int second_bit(const uint64_t *x) {
   }
   return lowest_bit<W>(y);
 }
-__device__ __forceinline__ bool bit_at(const uint64_t *x, int p) { return (x[p >> 6] >> (p & 63)) & 1ull; }
 // register-array forms: word selection by value, so that the arrays stay in registers
 template <int W>
 __device__ __forceinline__ bool bit_w(const uint64_t (&x)[W], int p) {
@@ -259,10 +261,17 @@ __global__ void __launch_bounds__(SCR_THREADS) k_screen(Params P, int64_t *cnt, 
   }
 }
 
-// Screen, stage 2: drop candidates whose block the reference evaluates to zero from its
-// integral prefactors alone — double excitations with (i0 j0|i1 j1) = (i0 j1|i1 j0) = 0
-// (PsociHamiltonian.C:180-185) and spin-orbit singles with SO_ij = 0 (:227); both tests are
-// symmetric in (i, j).  One warp per row configuration, candidates in order, ballot
+// A double-excitation block (PsociHamiltonian.C:180-185) has determinant elements +-v0,
+// +-v1 or +-(v0 - v1) with v0 = (i0 j0|i1 j1), v1 = (i0 j1|i1 j0), and each SEF element
+// combines at most four of them with weights +-1/2, so |element| <= 2 (|v0| + |v1|) (plus
+// rounding of a few ulps).  With |v0| + |v1| < 4e-9 every element is below the 1e-8 that
+// packSefsef stores (PsociGAhamiltonian.C:4077-4136): the block adds nothing to H and is
+// not evaluated.  This includes the blocks the reference skips outright (v0 = v1 = 0).
+__device__ __forceinline__ bool double_block_kept(double v0, double v1) { return fabs(v0) + fabs(v1) >= 4e-9; }
+
+// Screen, stage 2: drop candidates whose block stores nothing, judged from its integral
+// prefactors alone — double excitations as above and spin-orbit singles with SO_ij = 0
+// (PsociHamiltonian.C:227); both tests are symmetric in (i, j).  One warp per row configuration, candidates in order, ballot
 // compaction; MODE 0 counts, MODE 1 writes.
 template <int W, int MODE>
 __global__ void k_prune(Params P, const int64_t *candoff, const int32_t *cand, int64_t *cnt) {
@@ -291,8 +300,8 @@ __global__ void k_prune(Params P, const int64_t *candoff, const int32_t *cand, i
           int ex[2], jy[2];
           int ni = (j <= i) ? excitation<W>(a1, a2, b1, b2, ex, jy) : excitation<W>(b1, b2, a1, a2, ex, jy);
           if (ni == 2) {
-            keep = (__ldg(P.eri + canon4(ex[0], jy[0], ex[1], jy[1])) != 0.0) ||
-                   (__ldg(P.eri + canon4(ex[0], jy[1], ex[1], jy[0])) != 0.0);
+            keep = double_block_kept(__ldg(P.eri + canon4(ex[0], jy[0], ex[1], jy[1])),
+                                     __ldg(P.eri + canon4(ex[0], jy[1], ex[1], jy[0])));
           } else if (ni == 1 && __ldg(P.jsym + j) != js_i) {
             keep = __ldg(P.one + tri64(ex[0], jy[0])) != 0.0;
           }
@@ -303,6 +312,136 @@ __global__ void k_prune(Params P, const int64_t *candoff, const int32_t *cand, i
       n += __popc(b);
     }
     if (MODE == 0 && lane == 0) cnt[i] = n;
+  }
+}
+
+// ------------------------------------------------------------------------------------
+// Screen by lookup ("split join").  With the orbitals split at s so that every
+// configuration holds at most two electrons in the orbitals >= s, a configuration is a
+// (hi pattern g, lo pattern l) pair and its distance to another is d_hi + d_lo.  Any two
+// hi patterns of <= 2 electrons are within 4, so the neighbours of i are, for every hi
+// pattern h, the configurations T[h][l'] with d_lo(l_i, l') <= 4 - d_hi(g_i, h): one lookup
+// when the hi patterns are disjoint, a short list otherwise — work in proportion to the
+// neighbours instead of to all pairs.  Configurations are numbered in (g, l) order (checked
+// when the tables are built), so scanning h and then l' in ascending order yields sorted
+// lists.  The integral-based pruning of k_prune is applied to each candidate on the spot.
+// One warp per row configuration, one lane per hi pattern; MODE 0 counts (kept and all
+// candidates), MODE 1 writes the kept neighbours at off[i].
+// ------------------------------------------------------------------------------------
+struct JoinTabs {
+  int s, G, L;
+  const int32_t *gid, *lid, *T, *lnoff, *ln, *hdec;
+  const uint32_t *lokey;
+};
+
+template <int W>
+__device__ __forceinline__ void set_bit_w(uint64_t (&x)[W], int p) {
+#pragma unroll
+  for (int w = 0; w < W; ++w)
+    if ((p >> 6) == w) x[w] |= 1ull << (p & 63);
+}
+
+// occupancy bit-planes of hi pattern code (kind 0: empty, 1: one electron in a, 2: one
+// each in a < b, 3: two in a; positions relative to s)
+template <int W>
+__device__ __forceinline__ void hi_bits(int code, int s, uint64_t (&e1)[W], uint64_t (&e2)[W]) {
+#pragma unroll
+  for (int w = 0; w < W; ++w) e1[w] = e2[w] = 0ull;
+  const int kind = code & 3, a = (code >> 8) & 0xfff, b = (code >> 20) & 0xfff;
+  if (kind != 0) set_bit_w<W>(e1, s + a);
+  if (kind == 3) set_bit_w<W>(e2, s + a);
+  if (kind == 2) set_bit_w<W>(e1, s + b);
+}
+
+template <int W, int MODE>
+__global__ void __launch_bounds__(256) k_join(Params P, JoinTabs J, int64_t *cnt, int64_t *ncand, const int64_t *off) {
+  __shared__ int s_pre[8][33], s_q0[8][32], s_lp[8][32];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  const uint32_t lomask = (1u << J.s) - 1u;
+  for (int64_t i = warp; i < P.nconf; i += nwarps) {
+    uint64_t a1[W], a2[W], hi1[W], hi2[W];
+#pragma unroll
+    for (int w = 0; w < W; ++w) { a1[w] = P.e1[i * W + w]; a2[w] = P.e2[i * W + w]; }
+    const int li = J.lid[i], js_i = P.jsym[i];
+    hi_bits<W>(J.hdec[J.gid[i]], J.s, hi1, hi2);
+    int64_t nk = 0, nc = 0;
+    int64_t base = (MODE == 1) ? off[i] : 0;
+    for (int h0 = 0; h0 < J.G; h0 += 32) {
+      // this lane's hi pattern h: the lo patterns l' with d_lo <= 4 - d_hi, as a range of
+      // the neighbour list of l_i (or l_i alone when the hi patterns are disjoint)
+      const int h = h0 + lane;
+      int len = 0, q0 = 0, lp0 = li;
+      if (h < J.G) {
+        uint64_t g1[W], g2[W];
+        hi_bits<W>(J.hdec[h], J.s, g1, g2);
+        int d = 0;
+#pragma unroll
+        for (int w = 0; w < W; ++w) d += __popcll(hi1[w] ^ g1[w]) + __popcll(hi2[w] ^ g2[w]);
+        const int tau = 4 - d;
+        if (tau <= 0) { len = 1; q0 = -1; }
+        else {
+          q0 = J.lnoff[(tau - 1) * (J.L + 1) + li];
+          len = J.lnoff[(tau - 1) * (J.L + 1) + li + 1] - q0;
+        }
+      }
+      int incl = len;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int v = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += v;
+      }
+      const int tot = __shfl_sync(0xffffffffu, incl, 31);
+      s_pre[wib][lane] = incl - len;
+      s_q0[wib][lane] = q0;
+      s_lp[wib][lane] = lp0;
+      __syncwarp();
+      // the chunk's lookups, spread evenly over the lanes in (h, l') order
+      for (int e0 = 0; e0 < tot; e0 += 32) {
+        const int e = e0 + lane;
+        bool found = false, keep = false;
+        int j = -1;
+        if (e < tot) {
+          int o = 0;
+#pragma unroll
+          for (int st = 16; st > 0; st >>= 1)
+            if (s_pre[wib][o + st] <= e) o += st;
+          const int qo = s_q0[wib][o];
+          const int lp = (qo < 0) ? s_lp[wib][o] : J.ln[qo + (e - s_pre[wib][o])];
+          j = J.T[(int64_t)lp * J.G + (h0 + o)];
+          if (j >= 0) {
+            found = true;
+            keep = true;
+            if (j != (int)i) {
+              uint64_t b1[W], b2[W];
+              hi_bits<W>(J.hdec[h0 + o], J.s, b1, b2);
+              const uint32_t key = J.lokey[lp];
+              b1[0] |= key & lomask;
+              b2[0] |= key >> J.s;
+              int ex[2], jy[2];
+              const int ni = (j <= (int)i) ? excitation<W>(a1, a2, b1, b2, ex, jy) : excitation<W>(b1, b2, a1, a2, ex, jy);
+              if (ni == 2) {
+                keep = double_block_kept(__ldg(P.eri + canon4(ex[0], jy[0], ex[1], jy[1])),
+                                         __ldg(P.eri + canon4(ex[0], jy[1], ex[1], jy[0])));
+              } else if (ni == 1 && __ldg(P.jsym + j) != js_i) {
+                keep = __ldg(P.one + tri64(ex[0], jy[0])) != 0.0;
+              }
+            }
+          }
+        }
+        const unsigned kb = __ballot_sync(0xffffffffu, keep);
+        if (MODE == 0) {
+          nc += __popc(__ballot_sync(0xffffffffu, found));
+          nk += __popc(kb);
+        } else {
+          if (keep) P.nbr[base + __popc(kb & ((1u << lane) - 1u))] = j;
+          base += __popc(kb);
+        }
+      }
+      __syncwarp();
+    }
+    if (MODE == 0 && lane == 0) { cnt[i] = nk; ncand[i] = nc; }
   }
 }
 
@@ -670,12 +809,16 @@ __device__ __noinline__ double det_elem(const DetTabs P, const PairInfo &pi, con
   return (ncount & 1) ? -v : v;
 }
 
-// SEF element (a, b) of the reference block (A, B): ciout / transformCDCt
+// SEF element (a, b) of the reference block (A, B): ciout / transformCDCt.  conn bit
+// (x << 1 | y) says whether determinant x of SEF a and determinant y of SEF b can couple;
+// a determinant element that cannot is exactly zero and is not evaluated (adding the zero
+// it would return leaves every partial sum unchanged).
 template <int W>
-__device__ double sef_elem(const Params &PP, const PairInfo &pi, const double *Kd, int a, int b) {
+__device__ double sef_elem(const Params &PP, const PairInfo &pi, const double *Kd, int a, int b,
+                           unsigned conn = 0xFu) {
   if (pi.kind == K_NONE) return 0.0;
   const DetTabs P = {PP.alpha, PP.beta, PP.phase, PP.nalpha, PP.eri};
-  if (PP.nelec & 1) return det_elem<W>(P, pi, Kd, pi.detA + a, pi.detB + b);
+  if (PP.nelec & 1) return (conn & 1u) ? det_elem<W>(P, pi, Kd, pi.detA + a, pi.detB + b) : 0.0;
   const double r = sqrt(0.5);
   const bool oa = pi.nopenA != 0, ob = pi.nopenB != 0;
   const double mA = (pi.jsA % 2 != PP.ksym % 2) ? -1.0 : 1.0;
@@ -684,17 +827,17 @@ __device__ double sef_elem(const Params &PP, const PairInfo &pi, const double *K
   int64_t b0 = pi.detB + (ob ? 2 * b : 0), b1 = b0 + 1;
   double ds0, ds1 = 0.0;
   if (ob) {
-    double t = det_elem<W>(P, pi, Kd, a0, b0);
-    t += mB * det_elem<W>(P, pi, Kd, a0, b1);
+    double t = (conn & 1u) ? det_elem<W>(P, pi, Kd, a0, b0) : 0.0;
+    t += mB * ((conn & 2u) ? det_elem<W>(P, pi, Kd, a0, b1) : 0.0);
     ds0 = t * r;
     if (oa) {
-      double u = det_elem<W>(P, pi, Kd, a1, b0);
-      u += mB * det_elem<W>(P, pi, Kd, a1, b1);
+      double u = (conn & 4u) ? det_elem<W>(P, pi, Kd, a1, b0) : 0.0;
+      u += mB * ((conn & 8u) ? det_elem<W>(P, pi, Kd, a1, b1) : 0.0);
       ds1 = u * r;
     }
   } else {
-    ds0 = det_elem<W>(P, pi, Kd, a0, b0);
-    if (oa) ds1 = det_elem<W>(P, pi, Kd, a1, b0);
+    ds0 = (conn & 1u) ? det_elem<W>(P, pi, Kd, a0, b0) : 0.0;
+    if (oa) ds1 = (conn & 4u) ? det_elem<W>(P, pi, Kd, a1, b0) : 0.0;
   }
   if (oa) {
     double t = r * ds0;
@@ -806,6 +949,7 @@ struct FastSmem {
   uint32_t mrow[PSOCI_SEG];
   int pre[PSOCI_SEG];
   uint32_t keep[PSOCI_SEG];
+  uint64_t cm[PSOCI_SEG];  // connectivity of the row's marked elements (see below)
 };
 
 // may det (aA, bA) of A and det (aB, bB) of B have a non-zero element?
@@ -846,7 +990,7 @@ __global__ void __launch_bounds__(WARPS_PER_CTA * 32) k_hbuild_fast(Params P) {
       ws->rna[d] = P.nalpha[d0I + d];
     }
     __syncwarp();
-    // phase 1: candidate masks M[r] (bit t) for this lane's neighbour, bit-parallel over the
+    // phase 1: connectivity masks C[r] for this lane's neighbour, bit-parallel over the
     // row determinants.  With m_a the alpha pattern of row det a on I's open shells, a column
     // det b (alpha ab, beta bb) differs from a in
     //   c(a) = F + #{p in x : p not in m_a} + #{p in y : p in m_a}
@@ -885,8 +1029,10 @@ __global__ void __launch_bounds__(WARPS_PER_CTA * 32) k_hbuild_fast(Params P) {
       for (int k = 0; k <= FAST_MAXOPEN; ++k) Nk[k] = __ballot_sync(0xffffffffu, (lane < ndI) && __popc(ma) == k);
     }
     const int ndblI = P.nelec - nopI;  // electrons in I's doubly occupied orbitals
-    uint32_t M[FAST_MAXSEF];
-    for (int r = 0; r < FAST_MAXSEF; ++r) M[r] = 0u;
+    // C[r]: for row SEF r and column SEF t, bit t + 16 (x << 1 | y) says that determinant x
+    // of SEF r and determinant y of SEF t can couple; the SEF element is marked when any can.
+    uint64_t C[FAST_MAXSEF];
+    for (int r = 0; r < FAST_MAXSEF; ++r) C[r] = 0ull;
     if (lane < n) {
       const PairInfo &pi = ws->pi[lane];
       if (pi.kind != K_NONE) {
@@ -895,6 +1041,7 @@ __global__ void __launch_bounds__(WARPS_PER_CTA * 32) k_hbuild_fast(Params P) {
         const int nopJ = pi.swap ? pi.nopenA : pi.nopenB;
         const int ndJ = 1 << (nopJ > 1 ? nopJ - 1 : 0);
         const int thr = so ? 1 : 2;
+        const uint32_t rows_valid = (ndI >= 32) ? 0xffffffffu : ((1u << ndI) - 1u);
         for (int b = 0; b < ndJ; ++b) {
           uint64_t ja[W], jb[W];
 #pragma unroll
@@ -903,43 +1050,48 @@ __global__ void __launch_bounds__(WARPS_PER_CTA * 32) k_hbuild_fast(Params P) {
 #pragma unroll
           for (int w = 0; w < W; ++w) F += __popcll(ja[w] & ~occI[w]) + __popcll(jb[w] & ~occI[w]);
           if (F > thr) continue;
-          // saturating counter over the row dets: S0 (c'=0), S1, S2, S3 (>= 3)
-          uint32_t S0 = 0xffffffffu, S1 = 0u, S2 = 0u;
+          uint32_t ok = 0u;
+          {
+            // saturating counter over the row dets: S0 (c'=0), S1, S2, S3 (>= 3)
+            uint32_t S0 = 0xffffffffu, S1 = 0u, S2 = 0u;
 #pragma unroll
-          for (int p = 0; p < FAST_MAXOPEN; ++p) {
-            if (p >= nopI) break;
-            const bool xa = bit_w<W>(ja, sI[p]), yb = bit_w<W>(jb, sI[p]);
-            if (xa) {  // mismatch where row det has beta on p
-              const uint32_t T = ~Ap[p];
-              S2 = (S2 & ~T) | (S1 & T);
-              S1 = (S1 & ~T) | (S0 & T);
-              S0 &= ~T;
+            for (int p = 0; p < FAST_MAXOPEN; ++p) {
+              if (p >= nopI) break;
+              const bool xa = bit_w<W>(ja, sI[p]), yb = bit_w<W>(jb, sI[p]);
+              if (xa) {  // mismatch where row det has beta on p
+                const uint32_t T = ~Ap[p];
+                S2 = (S2 & ~T) | (S1 & T);
+                S1 = (S1 & ~T) | (S0 & T);
+                S0 &= ~T;
+              }
+              if (yb) {  // mismatch where row det has alpha on p
+                const uint32_t T = Ap[p];
+                S2 = (S2 & ~T) | (S1 & T);
+                S1 = (S1 & ~T) | (S0 & T);
+                S0 &= ~T;
+              }
             }
-            if (yb) {  // mismatch where row det has alpha on p
-              const uint32_t T = Ap[p];
-              S2 = (S2 & ~T) | (S1 & T);
-              S1 = (S1 & ~T) | (S0 & T);
-              S0 &= ~T;
-            }
+            ok = (thr - F >= 2) ? (S0 | S1 | S2) : (thr - F == 1) ? (S0 | S1) : S0;
           }
-          uint32_t ok = (thr - F >= 2) ? (S0 | S1 | S2) : (thr - F == 1) ? (S0 | S1) : S0;
-          if (!so) {
-            int na = 0;
+          int na = 0;
 #pragma unroll
-            for (int w = 0; w < W; ++w) na += __popcll(ja[w]);
-            const int need = na - (ndblI / 2);
+          for (int w = 0; w < W; ++w) na += __popcll(ja[w]);
+          const int need = na - (ndblI / 2);  // alpha open shells a row det needs for equal counts
+          ok &= rows_valid;
+          if (!so) {
             uint32_t nk = 0u;
 #pragma unroll
             for (int k = 0; k <= FAST_MAXOPEN; ++k)
               if (k == need) nk = Nk[k];
-            ok &= (need <= nopI) ? nk : 0u;
+            ok &= (need >= 0 && need <= nopI) ? nk : 0u;
           }
-          ok &= (ndI >= 32) ? 0xffffffffu : ((1u << ndI) - 1u);
           const int t = odd ? b : (nopJ ? (b >> 1) : 0);
+          const int y = (!odd && nopJ) ? (b & 1) : 0;
           while (ok) {
             const int a = __ffs(ok) - 1;
             ok &= ok - 1;
-            M[odd ? a : (nopI ? (a >> 1) : 0)] |= 1u << t;
+            const int x = (!odd && nopI) ? (a & 1) : 0;
+            C[odd ? a : (nopI ? (a >> 1) : 0)] |= 1ull << (t + 16 * ((x << 1) | y));
           }
         }
       }
@@ -951,7 +1103,8 @@ __global__ void __launch_bounds__(WARPS_PER_CTA * 32) k_hbuild_fast(Params P) {
     // in chunks and advances through a chunk by the kept count of each row.
     const int64_t prbase = P.pr_off[I] + (k0 - P.nbroff[I]) * nsefI;
     for (int r = 0; r < nsefI; ++r) {
-      const uint32_t mr = (lane < n) ? M[r] : 0u;
+      const uint64_t cr = (lane < n) ? C[r] : 0ull;
+      const uint32_t mr = (uint32_t)((cr | (cr >> 16) | (cr >> 32) | (cr >> 48)) & 0xffffull);
       const int cm = __popc(mr);
       int inclm = cm;
 #pragma unroll
@@ -962,6 +1115,7 @@ __global__ void __launch_bounds__(WARPS_PER_CTA * 32) k_hbuild_fast(Params P) {
       const int T = __shfl_sync(0xffffffffu, inclm, 31);
       ws->pre[lane] = inclm - cm;
       ws->mrow[lane] = mr;
+      ws->cm[lane] = cr;
       ws->keep[lane] = 0u;
       if (cursor + T > chunk_end) {  // room for every marked element of the row
         const unsigned long long len = (unsigned long long)max(T, SLAB_CHUNK);
@@ -992,7 +1146,11 @@ __global__ void __launch_bounds__(WARPS_PER_CTA * 32) k_hbuild_fast(Params P) {
           // reference roles: the lower half of a diagonal block, block (J, I) for J > I
           const bool diag_blk = (pi.kind == K_DIAG);
           const bool flip = diag_blk ? (t > r) : (pi.swap != 0);
-          v = sef_elem<W>(P, pi, ws->K, flip ? t : r, flip ? r : t);
+          const uint64_t co = ws->cm[o] >> t;
+          unsigned conn = (unsigned)((co & 1ull) | ((co >> 15) & 2ull) | ((co >> 30) & 4ull) | ((co >> 45) & 8ull));
+          // a diagonal block is symmetric: the transposed element swaps the determinant roles
+          if (flip) conn = (conn & 9u) | ((conn & 2u) << 1) | ((conn & 4u) >> 1);
+          v = sef_elem<W>(P, pi, ws->K, flip ? t : r, flip ? r : t, conn);
           keep = (fabs(v) >= PSOCI_MIN_VALUE) || (diag_blk && t == r);
           if (keep) atomicOr(&ws->keep[o], 1u << t);
         }
@@ -1250,7 +1408,10 @@ psoci_status run_build(psoci_ctx *c, psoci_hmode mode, int64_t *nnz_out) {
   int *d_err = nullptr;
   unsigned long long *d_counter = nullptr;
   double *d_slabval = nullptr;
+  cudaEvent_t ev[6] = {};
   auto cleanup = [&]() {
+    for (auto &e : ev)
+      if (e) cudaEventDestroy(e);
     psoci_free(d_soff); psoci_free(d_tot); psoci_free(d_segslot); psoci_free(d_counter);
     psoci_free(d_candoff); psoci_free(d_cand);
     psoci_free(d_nlow); psoci_free(d_prrows); psoci_free(d_proff); psoci_free(d_mk); psoci_free(d_prm);
@@ -1281,10 +1442,34 @@ psoci_status run_build(psoci_ctx *c, psoci_hmode mode, int64_t *nnz_out) {
     if (c->verbose) cudaStreamSynchronize(st);
     return std::chrono::steady_clock::now();
   };
+  for (auto &e : ev) TRYC(cudaEventCreate(&e));
+  TRYC(cudaEventRecord(ev[0], st));
   auto t_a = tnow();
   // 1. screen
+  int64_t ncand = 0, npairs = 0;
+  int nsplit = 0;
+  if (c->join_ok) {
+    // by lookup, with the integral pruning fused
+    JoinTabs J = {c->join_s, c->join_G, c->join_L, c->d_jgid, c->d_jlid, c->d_jT, c->d_jlnoff, c->d_jln,
+                  c->d_jhdec, c->d_jlokey};
+    TRY(psoci_alloc(c, &d_cnt, n + 1));
+    TRY(psoci_alloc(c, &d_tot, n + 1));
+    TRY(psoci_alloc(c, &d_candoff, n + 1));
+    TRY(psoci_alloc(c, &d_nbroff, n + 1));
+    const int jblocks = (int)std::max<int64_t>(1, std::min<int64_t>(((int64_t)n * 32 + 255) / 256, 152 * 32));
+    psoci_note_launch();
+    k_join<W, 0><<<jblocks, 256, 0, st>>>(P, J, d_cnt, d_tot, nullptr);
+    TRYC(cudaGetLastError());
+    TRY(psoci_scan_i64(c, d_tot, d_candoff, n, &ncand));
+    TRY(psoci_scan_i64(c, d_cnt, d_nbroff, n, &npairs));
+    TRY(psoci_alloc(c, &d_nbr, npairs));
+    P.nbroff = d_nbroff; P.nbr = d_nbr;
+    psoci_note_launch();
+    k_join<W, 1><<<jblocks, 256, 0, st>>>(P, J, nullptr, nullptr, d_nbroff);
+    TRYC(cudaGetLastError());
+  } else {
   const int scr_rows = (n + SCR_THREADS * SCR_ROWS - 1) / (SCR_THREADS * SCR_ROWS);
-  int nsplit = (int)std::max<int64_t>(1, std::min<int64_t>(64, (152 * 8 + scr_rows - 1) / scr_rows));
+  nsplit = (int)std::max<int64_t>(1, std::min<int64_t>(64, (152 * 8 + scr_rows - 1) / scr_rows));
   int64_t chunk = ((int64_t)n + nsplit - 1) / nsplit;
   chunk = std::max<int64_t>(chunk, SCR_TILE);
   nsplit = (int)((n + chunk - 1) / chunk);
@@ -1300,7 +1485,6 @@ psoci_status run_build(psoci_ctx *c, psoci_hmode mode, int64_t *nnz_out) {
   psoci_note_launch();
   k_screen_offsets<<<(n + 255) / 256, 256, 0, st>>>(n, nsplit, d_cnt, d_soff, d_tot);
   TRYC(cudaGetLastError());
-  int64_t ncand = 0;
   TRY(psoci_scan_i64(c, d_tot, d_candoff, n, &ncand));
   TRY(psoci_alloc(c, &d_cand, ncand));
   psoci_note_launch();
@@ -1310,7 +1494,6 @@ psoci_status run_build(psoci_ctx *c, psoci_hmode mode, int64_t *nnz_out) {
   psoci_note_launch();
   k_prune<W, 0><<<prune_blocks, 256, 0, st>>>(P, d_candoff, d_cand, d_tot);
   TRYC(cudaGetLastError());
-  int64_t npairs = 0;
   TRY(psoci_scan_i64(c, d_tot, d_nbroff, n, &npairs));
   TRY(psoci_alloc(c, &d_nbr, npairs));
   P.nbroff = d_nbroff; P.nbr = d_nbr;
@@ -1318,8 +1501,10 @@ psoci_status run_build(psoci_ctx *c, psoci_hmode mode, int64_t *nnz_out) {
   k_prune<W, 1><<<prune_blocks, 256, 0, st>>>(P, d_candoff, d_cand, nullptr);
   TRYC(cudaGetLastError());
   psoci_free(d_cand);
+  }
   c->ncand = ncand;
   c->npairs = npairs;
+  TRYC(cudaEventRecord(ev[1], st));
   auto t_b = tnow();
 
   // fast path: only the lower pairs (J <= I) are evaluated; the rest are mirrored
@@ -1364,7 +1549,8 @@ psoci_status run_build(psoci_ctx *c, psoci_hmode mode, int64_t *nnz_out) {
   // 3. evaluate
   int hb_blocks = (int)std::max<int64_t>(1, std::min<int64_t>((nseg + WARPS_PER_CTA - 1) / WARPS_PER_CTA, 152 * 16));
   const int64_t N = c->nsef_total;
-  int64_t nnz = 0;
+  int64_t nnz = 0, slab_used = 0;
+  int evaluations = 0;
   auto t_c = tnow();
   auto t_d = t_c, t_e = t_c;
   if (fast) {
@@ -1376,19 +1562,28 @@ psoci_status run_build(psoci_ctx *c, psoci_hmode mode, int64_t *nnz_out) {
     size_t freeb = 0, totb = 0;
     TRYC(cudaMemGetInfo(&freeb, &totb));
     // slots hold the kept elements of the lower pairs plus the unused tails of the warps'
-    // chunks; first guess from the pair count (observed 2.5-5.5 kept elements per lower
-    // pair, about half the pairs lower); an overflow is detected by the kernel's counter
-    // and the evaluation repeats with the exact size
+    // chunks; first guess from the pair count (observed up to 7 kept elements per lower
+    // pair; (npairs + nconf) / 2 lower pairs) or from the previous build of the same space;
+    // an overflow is detected by the kernel's counter and the evaluation repeats with the
+    // exact size
     const int64_t tails = (int64_t)hb_blocks * WARPS_PER_CTA * SLAB_CHUNK;
-    int64_t cap = std::min<int64_t>((int64_t)(freeb * 0.35) / 8, 3 * npairs + tails);
+    int64_t cap = std::max<int64_t>(4 * npairs + 4 * (int64_t)n, c->slab_hint) + tails;
+    cap = std::min<int64_t>((int64_t)(freeb * 0.5) / 8, cap);
     int64_t nlower = 0;
     for (int attempt = 0; attempt < 2; ++attempt) {
+      auto t_al = std::chrono::steady_clock::now();
       TRY(psoci_alloc(c, &d_slabval, cap));
+      if (c->verbose)
+        fprintf(stderr, "psoci: H build slab allocation %.4f s (%lld slots)\n",
+                std::chrono::duration<double>(std::chrono::steady_clock::now() - t_al).count(), (long long)cap);
       TRYC(cudaMemsetAsync(d_counter, 0, sizeof(unsigned long long), st));
       P.seg_slot = d_segslot; P.slab_counter = d_counter; P.slab_cap = cap; P.slab_val = d_slabval;
+      TRYC(cudaEventRecord(ev[2], st));
       psoci_note_launch();
       k_hbuild_fast<W><<<hb_blocks, WARPS_PER_CTA * 32, smem, st>>>(P);
       TRYC(cudaGetLastError());
+      TRYC(cudaEventRecord(ev[3], st));
+      ++evaluations;
       unsigned long long used = 0;
       TRYC(cudaMemcpyAsync(&used, d_counter, sizeof(used), cudaMemcpyDeviceToHost, st));
       TRYC(cudaStreamSynchronize(st));
@@ -1415,6 +1610,9 @@ psoci_status run_build(psoci_ctx *c, psoci_hmode mode, int64_t *nnz_out) {
     TRY(psoci_alloc(c, &c->d_rowptr, N + 1));
     TRY(psoci_scan_i64(c, d_rownnz, c->d_rowptr, N, &nnz));
     if (herr) TRY(psoci_fail(c, PSOCI_ERR_CUDA, "H build: neighbour lists are not symmetric"));
+    TRYC(cudaEventRecord(ev[4], st));
+    slab_used = nlower;
+    c->slab_hint = nlower;
     if (nnz < N) TRY(psoci_fail(c, PSOCI_ERR_CUDA, "H build: rows without their diagonal element"));
     TRY(psoci_alloc(c, &c->d_col, nnz));
     TRY(psoci_alloc(c, &c->d_val, nnz));
@@ -1426,15 +1624,19 @@ psoci_status run_build(psoci_ctx *c, psoci_hmode mode, int64_t *nnz_out) {
     psoci_note_launch();
     k_assemble<<<cfg_blocks, 256, 0, st>>>(P, d_mk);
     TRYC(cudaGetLastError());
+    TRYC(cudaEventRecord(ev[5], st));
     TRYC(cudaStreamSynchronize(st));
   } else {
     const size_t smem = sizeof(WarpSmem) * WARPS_PER_CTA;
     TRYC(cudaFuncSetAttribute(k_hbuild<W, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     TRYC(cudaFuncSetAttribute(k_hbuild<W, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     // 3. count
+    TRYC(cudaEventRecord(ev[2], st));
     psoci_note_launch();
     k_hbuild<W, 0><<<hb_blocks, WARPS_PER_CTA * 32, smem, st>>>(P);
     TRYC(cudaGetLastError());
+    TRYC(cudaEventRecord(ev[3], st));
+    ++evaluations;
     t_d = tnow();
     // 4. offsets
     TRY(psoci_alloc(c, &d_rownnz, N + 1));
@@ -1443,6 +1645,7 @@ psoci_status run_build(psoci_ctx *c, psoci_hmode mode, int64_t *nnz_out) {
     TRYC(cudaGetLastError());
     TRY(psoci_alloc(c, &c->d_rowptr, N + 1));
     TRY(psoci_scan_i64(c, d_rownnz, c->d_rowptr, N, &nnz));
+    TRYC(cudaEventRecord(ev[4], st));
     TRY(psoci_alloc(c, &c->d_col, nnz));
     TRY(psoci_alloc(c, &c->d_val, nnz));
     if (mode == PSOCI_HMODE_CSR_BOTH) TRY(psoci_alloc(c, &c->d_val32, nnz));
@@ -1453,15 +1656,30 @@ psoci_status run_build(psoci_ctx *c, psoci_hmode mode, int64_t *nnz_out) {
     psoci_note_launch();
     k_hbuild<W, 1><<<hb_blocks, WARPS_PER_CTA * 32, smem, st>>>(P);
     TRYC(cudaGetLastError());
+    TRYC(cudaEventRecord(ev[5], st));
     TRYC(cudaStreamSynchronize(st));
   }
   auto t_f = std::chrono::steady_clock::now();
   if (c->verbose) {
     auto d = [](auto a, auto b) { return std::chrono::duration<double>(b - a).count(); };
     fprintf(stderr,
-            "psoci: H build phases (%s kernel, %d column ranges): screen %.4f s, segments %.4f s, evaluate %.4f s, "
+            "psoci: H build phases (%s kernel, %s screen): screen %.4f s, segments %.4f s, evaluate %.4f s, "
             "offsets %.4f s, fill/copy %.4f s\n",
-            fast ? "fast" : "generic", nsplit, d(t_a, t_b), d(t_b, t_c), d(t_c, t_d), d(t_d, t_e), d(t_e, t_f));
+            fast ? "fast" : "generic", nsplit ? "all-pairs" : "lookup", d(t_a, t_b), d(t_b, t_c), d(t_c, t_d),
+            d(t_d, t_e), d(t_e, t_f));
+  }
+  {
+    psoci_build_info &b = c->binfo;
+    b = psoci_build_info{};
+    b.candidates = ncand; b.pairs = npairs; b.segments = nseg; b.nnz = nnz; b.nnz_lower = (nnz + N) / 2;
+    b.slab_slots = slab_used; b.evaluations = evaluations; b.fast = fast ? 1 : 0;
+    b.lookup_screen = c->join_ok ? 1 : 0;
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, ev[0], ev[1]) == cudaSuccess) b.screen_ms = ms;
+    if (cudaEventElapsedTime(&ms, ev[2], ev[3]) == cudaSuccess) b.evaluate_ms = ms;
+    if (cudaEventElapsedTime(&ms, ev[3], ev[4]) == cudaSuccess) b.rows_ms = ms;
+    if (cudaEventElapsedTime(&ms, ev[4], ev[5]) == cudaSuccess) b.assemble_ms = ms;
+    if (cudaEventElapsedTime(&ms, ev[0], ev[5]) == cudaSuccess) b.total_ms = ms;
   }
   cleanup();
   c->nnz = nnz;
@@ -1473,6 +1691,135 @@ psoci_status run_build(psoci_ctx *c, psoci_hmode mode, int64_t *nnz_out) {
 
 }  // namespace
 
+void psoci_join_release(psoci_ctx *c) {
+  psoci_free(c->d_jgid);
+  psoci_free(c->d_jlid);
+  psoci_free(c->d_jT);
+  psoci_free(c->d_jlnoff);
+  psoci_free(c->d_jln);
+  psoci_free(c->d_jhdec);
+  psoci_free(c->d_jlokey);
+  c->join_ok = false;
+}
+
+// Tables of the lookup screen (see k_join).  The space qualifies when some split s <= 12
+// leaves every configuration at most two electrons in the orbitals >= s, the
+// configurations are numbered in ascending (hi pattern, lo pattern) order with lo patterns
+// numbered by first appearance, and the tables stay small; otherwise the all-pairs screen
+// is used.  Not qualifying is not an error.
+psoci_status psoci_join_prepare(psoci_ctx *c) {
+  psoci_join_release(c);
+  const int n = c->nconf, nbf = c->nbf;
+  const uint8_t *occ = c->h_occ.data();
+  // split: orbitals >= s hold at most two electrons in every configuration
+  int s = 0;
+  for (int i = 0; i < n; ++i) {
+    const uint8_t *o = occ + (size_t)i * nbf;
+    int e = 0, si = 0;
+    for (int q = nbf - 1; q >= 0; --q) {
+      e += o[q];
+      if (e >= 3) { si = q + 1; break; }
+    }
+    s = std::max(s, si);
+  }
+  const int nh = nbf - s;
+  if (s > 12 || nh < 1) return PSOCI_OK;
+  const int64_t G = 1 + nh + (int64_t)nh * (nh + 1) / 2;
+  std::vector<int32_t> gid(n), lid(n), keyid((size_t)1 << (2 * s), -1);
+  std::vector<uint32_t> lokey;
+  for (int i = 0; i < n; ++i) {
+    const uint8_t *o = occ + (size_t)i * nbf;
+    uint32_t key = 0;
+    for (int q = 0; q < s; ++q) {
+      if (o[q] >= 1) key |= 1u << q;
+      if (o[q] == 2) key |= 1u << (s + q);
+    }
+    int pa = -1, pb = -1, kind = 0;
+    for (int q = s; q < nbf; ++q) {
+      if (o[q] == 0) continue;
+      if (o[q] == 2) { kind = 3; pa = q - s; }
+      else if (pa < 0) { kind = 1; pa = q - s; }
+      else { kind = 2; pb = q - s; }
+    }
+    gid[i] = (kind == 0) ? 0 : (kind == 1) ? 1 + pa
+             : (int32_t)(1 + nh + (kind == 3 ? (int64_t)pa * (pa + 1) / 2 + pa : (int64_t)pb * (pb + 1) / 2 + pa));
+    if (keyid[key] < 0) { keyid[key] = (int32_t)lokey.size(); lokey.push_back(key); }
+    lid[i] = keyid[key];
+    if (i > 0 && gid[i] < gid[i - 1]) return PSOCI_OK;  // hi patterns must ascend
+  }
+  const int64_t L = (int64_t)lokey.size();
+  // Number the lo patterns so that they ascend inside every hi pattern: each group's order
+  // is a chain of constraints; a topological order of all of them (ties broken by first
+  // appearance) exists unless two groups order some patterns differently.
+  {
+    std::vector<std::vector<int32_t>> next((size_t)L);
+    std::vector<int32_t> indeg((size_t)L, 0);
+    for (int i = 1; i < n; ++i)
+      if (gid[i] == gid[i - 1]) {
+        if (lid[i] == lid[i - 1]) return PSOCI_OK;  // repeated configuration
+        next[lid[i - 1]].push_back(lid[i]);
+        ++indeg[lid[i]];
+      }
+    std::vector<int32_t> order;
+    order.reserve((size_t)L);
+    std::priority_queue<int32_t, std::vector<int32_t>, std::greater<int32_t>> ready;
+    for (int64_t l = 0; l < L; ++l)
+      if (indeg[l] == 0) ready.push((int32_t)l);
+    while (!ready.empty()) {
+      const int32_t l = ready.top();
+      ready.pop();
+      order.push_back(l);
+      for (int32_t m : next[l])
+        if (--indeg[m] == 0) ready.push(m);
+    }
+    if ((int64_t)order.size() != L) return PSOCI_OK;  // contradictory orders
+    std::vector<int32_t> rank((size_t)L);
+    std::vector<uint32_t> key2((size_t)L);
+    for (int64_t r = 0; r < L; ++r) { rank[order[r]] = (int32_t)r; key2[r] = lokey[order[r]]; }
+    for (int i = 0; i < n; ++i) lid[i] = rank[lid[i]];
+    lokey.swap(key2);
+    for (int i = 1; i < n; ++i)
+      if (gid[i] == gid[i - 1] && lid[i] <= lid[i - 1]) return PSOCI_OK;
+  }
+  if (G * L > ((int64_t)1 << 26)) return PSOCI_OK;
+  std::vector<int32_t> T((size_t)(G * L), -1), hdec((size_t)G);
+  for (int i = 0; i < n; ++i) T[(size_t)lid[i] * G + gid[i]] = i;  // [lo pattern][hi pattern]
+  hdec[0] = 0;
+  for (int a = 0; a < nh; ++a) hdec[1 + a] = 1 | (a << 8);
+  for (int b = 0; b < nh; ++b)
+    for (int a = 0; a <= b; ++a)
+      hdec[1 + nh + (size_t)b * (b + 1) / 2 + a] = (a == b) ? (3 | (a << 8)) : (2 | (a << 8) | (b << 20));
+  // lo patterns within tau = 1..4 of each lo pattern (itself included), ascending
+  std::vector<int32_t> lnoff(4 * (L + 1)), ln;
+  for (int tau = 1; tau <= 4; ++tau)
+    for (int64_t l = 0; l <= L; ++l) {
+      lnoff[(tau - 1) * (L + 1) + l] = (int32_t)ln.size();
+      if (l == L) break;
+      for (int64_t m = 0; m < L; ++m)
+        if (__builtin_popcount(lokey[l] ^ lokey[m]) <= tau) ln.push_back((int32_t)m);
+    }
+  psoci_status st;
+  if ((st = psoci_alloc(c, &c->d_jgid, n)) || (st = psoci_alloc(c, &c->d_jlid, n)) ||
+      (st = psoci_alloc(c, &c->d_jT, T.size())) || (st = psoci_alloc(c, &c->d_jlnoff, lnoff.size())) ||
+      (st = psoci_alloc(c, &c->d_jln, ln.size())) || (st = psoci_alloc(c, &c->d_jhdec, hdec.size())) ||
+      (st = psoci_alloc(c, &c->d_jlokey, lokey.size()))) {
+    psoci_join_release(c);
+    return st;
+  }
+  cudaStream_t q = c->stream;
+  PSOCI_CUDA(c, cudaMemcpyAsync(c->d_jgid, gid.data(), 4 * gid.size(), cudaMemcpyHostToDevice, q));
+  PSOCI_CUDA(c, cudaMemcpyAsync(c->d_jlid, lid.data(), 4 * lid.size(), cudaMemcpyHostToDevice, q));
+  PSOCI_CUDA(c, cudaMemcpyAsync(c->d_jT, T.data(), 4 * T.size(), cudaMemcpyHostToDevice, q));
+  PSOCI_CUDA(c, cudaMemcpyAsync(c->d_jlnoff, lnoff.data(), 4 * lnoff.size(), cudaMemcpyHostToDevice, q));
+  PSOCI_CUDA(c, cudaMemcpyAsync(c->d_jln, ln.data(), 4 * std::max<size_t>(ln.size(), 1), cudaMemcpyHostToDevice, q));
+  PSOCI_CUDA(c, cudaMemcpyAsync(c->d_jhdec, hdec.data(), 4 * hdec.size(), cudaMemcpyHostToDevice, q));
+  PSOCI_CUDA(c, cudaMemcpyAsync(c->d_jlokey, lokey.data(), 4 * lokey.size(), cudaMemcpyHostToDevice, q));
+  PSOCI_CUDA(c, cudaStreamSynchronize(q));
+  c->join_s = s; c->join_nh = nh; c->join_G = (int)G; c->join_L = (int)L;
+  c->join_ok = true;
+  return PSOCI_OK;
+}
+
 void psoci_h_release(psoci_ctx *c) {
   psoci_free(c->d_rowptr);
   psoci_free(c->d_col);
@@ -1481,6 +1828,7 @@ void psoci_h_release(psoci_ctx *c) {
   psoci_free(c->d_diag);
   c->have_h = false;
   c->nnz = 0;
+  c->binfo = psoci_build_info{};
 }
 
 psoci_status psoci_h_blocks(psoci_ctx *c, int npairs, const int32_t *A, const int32_t *B, double *out) {

@@ -210,6 +210,9 @@ psoci_status psoci_load_hamiltonian(psoci_ctx *c, const char *path) {
   PSOCI_CUDA(c, cudaMemcpy(c->d_diag, dg.data(), 8 * N, cudaMemcpyHostToDevice));
   if (has32) PSOCI_CUDA(c, cudaMemcpy(c->d_val32, v32.data(), 4 * nnz, cudaMemcpyHostToDevice));
   c->nnz = nnz;
+  c->binfo = psoci_build_info{};  // loaded, not built: counts only
+  c->binfo.nnz = nnz;
+  c->binfo.nnz_lower = (nnz + c->nsef_total) / 2;
   c->have_h = true;
   return PSOCI_OK;
 }

@@ -45,6 +45,18 @@ struct psoci_ctx {
   int32_t *d_jsym = nullptr;  // [nconf]
   int32_t *d_nopen = nullptr; // [nconf]
 
+  // neighbour screen by lookup ("split join"): usable when every configuration holds at
+  // most two electrons in the orbitals >= join_s (MRCI-type spaces); built by set_configs
+  bool join_ok = false;
+  int join_s = 0, join_nh = 0, join_G = 0, join_L = 0;
+  int32_t *d_jgid = nullptr;    // [nconf] pattern id of the orbitals >= s
+  int32_t *d_jlid = nullptr;    // [nconf] pattern id of the orbitals < s
+  int32_t *d_jT = nullptr;      // [L*G] configuration of (lo pattern, hi pattern), or -1
+  int32_t *d_jlnoff = nullptr;  // [4*(L+1)] per distance tau = 1..4: offsets into d_jln
+  int32_t *d_jln = nullptr;     // lo patterns within tau of each lo pattern, ascending
+  int32_t *d_jhdec = nullptr;   // [G] hi pattern: kind | a << 8 | b << 20
+  uint32_t *d_jlokey = nullptr; // [L] lo pattern: e1 bits | e2 bits << s
+
   // determinants
   bool have_dets = false;
   std::vector<int64_t> h_sefoff, h_detoff;  // nconf+1
@@ -70,6 +82,8 @@ struct psoci_ctx {
   float *d_val32 = nullptr;
   double *d_diag = nullptr;
   double build_seconds = 0.0;
+  psoci_build_info binfo{};
+  int64_t slab_hint = 0;  // value-slab slots the last build of this space used
 
   // initial guess for the next Davidson run (root-major, guess_k x nsef)
   std::vector<double> guess;
@@ -123,6 +137,8 @@ psoci_status psoci_sigma_launch(psoci_ctx *c, int k, const double *dX, int ldx, 
 psoci_status psoci_dets_build(psoci_ctx *c);
 psoci_status psoci_h_build(psoci_ctx *c, psoci_hmode mode, int64_t *nnz);
 psoci_status psoci_h_blocks(psoci_ctx *c, int npairs, const int32_t *A, const int32_t *B, double *out);
+psoci_status psoci_join_prepare(psoci_ctx *c);  // after h_occ is set
+void psoci_join_release(psoci_ctx *c);
 void psoci_h_release(psoci_ctx *c);
 void psoci_dets_release(psoci_ctx *c);
 

@@ -305,7 +305,8 @@ def named_workload(name: str, seed: int = 0, ksym: int = 1) -> Problem:
         "mrcis_6e8o_v40": ("mrcis", dict(nact=8, nelec=6, nvirt=40)),
         # MRCISD: CAS(4e,6o) reference + singles and doubles into 30 virtuals
         "mrcisd_4e6o_v30": ("mrcisd", dict(nact=6, nelec=4, nvirt=30)),
-        # the same space with 24 virtuals (568,204 SEFs): small enough for profiler captures
+        # the same space with 16 and 24 virtuals (263,004 / 568,204 SEFs): profiler captures
+        "mrcisd_6e8o_v16": ("mrcisd", dict(nact=8, nelec=6, nvirt=16)),
         "mrcisd_6e8o_v24": ("mrcisd", dict(nact=8, nelec=6, nvirt=24)),
         # scaled MRCISD: CAS(6e,8o) + singles and doubles into 64 virtuals (~3.8M SEFs)
         "mrcisd_6e8o_v64": ("mrcisd", dict(nact=8, nelec=6, nvirt=64)),

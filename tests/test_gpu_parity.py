@@ -91,6 +91,31 @@ def test_two_word_orbitals(oracle_mod):
     _check_h(c, O, p)
 
 
+@pytest.mark.parametrize("kind,kw,ksym", [
+    ("mrcisd", dict(nact=6, nelec=4, nvirt=8), 1),
+    ("mrcisd", dict(nact=6, nelec=4, nvirt=8), 2),
+    ("mrcisd", dict(nact=6, nelec=5, nvirt=6), 1),
+    ("mrcis", dict(nact=8, nelec=6, nvirt=6), 3),
+])
+def test_mrci_lookup_screen(oracle_mod, kind, kw, ksym):
+    """MRCI spaces take the lookup screen (at most two electrons above the active orbitals);
+    the Hamiltonian must be the reference's all the same."""
+    from psoci_gb300.inputs import make_problem
+
+    p = make_problem(kind, seed=11, ksym=ksym, **kw)
+    O = oracle_mod.Oracle(p)
+    c = _ctx(p)
+    _check_h(c, O, p)
+    assert c.build_stats()["lookup_screen"] == 1
+
+
+def test_fci_takes_all_pairs_screen(oracle_mod):
+    p = small_problem("fci_6e8o", 1)
+    c = _ctx(p)
+    c.build_hamiltonian(mixed=True)
+    assert c.build_stats()["lookup_screen"] == 0
+
+
 def test_sigma_fp64_and_mixed(oracle_mod):
     p = small_problem("fci_6e8o", 1)
     O = oracle_mod.Oracle(p)
