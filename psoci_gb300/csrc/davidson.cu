@@ -34,28 +34,71 @@ constexpr int TN_MAXOUT = 8;      // outputs per thread => m*k <= 2048
 constexpr int NN_THREADS = 256;
 constexpr int MAX_SUB = 96;       // Jacobi keeps two m x m FP64 matrices in shared memory
 
+// The tall-skinny products below run in float-float arithmetic on the FP32 pipe: on GB300
+// the FP64 pipe issues ~2 FMA/clk/SM against 128 FP32 lanes, and these products are
+// FP64-bound.  Each FP64 operand is split into hi + lo floats by bit manipulation (no FP64
+// instruction): hi keeps the sign, the exponent and the top 23 mantissa bits, lo the other
+// 29 bits rounded to 24 — about 47 significant bits, 2^-47 relative.  Products are formed
+// error-free (hi*hi with its FMA residual, plus the cross terms) and summed with TwoSum into
+// a float pair; block partials are combined in FP64.  Operands below 2^-126 in magnitude
+// are treated as zero and those below 2^-74 keep hi only (absolute error < 2^-97); the
+// vectors here are normalised or bounded by |H|.
+__device__ __forceinline__ float2 split_f64(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const unsigned sign = (unsigned)(b >> 32) & 0x80000000u;
+  const int e = (int)((b >> 52) & 0x7ff);
+  if (e == 0x7ff) return make_float2(__int_as_float((int)(sign | 0x7fc00000u)), 0.f);  // inf / nan -> nan
+  if (e < 1023 - 126) return make_float2(__int_as_float((int)sign), 0.f);
+  if (e > 1023 + 127) return make_float2(__int_as_float((int)(sign | 0x7f800000u)), 0.f);
+  const unsigned mh = (unsigned)(b >> 29) & 0x7fffffu;
+  const float hi = __int_as_float((int)(sign | ((unsigned)(e - 1023 + 127) << 23) | mh));
+  const int el = e - 1075 + 127;  // biased exponent of 2^(e - 1075), the weight of lo's unit
+  float lo = 0.f;
+  if (el > 0) lo = __uint2float_rn((unsigned)(b & 0x1fffffffull)) * __int_as_float(el << 23);
+  return make_float2(hi, sign ? -lo : lo);
+}
+
+// (sh, sl) += a * b, a and b float pairs
+__device__ __forceinline__ void ff_fma(float &sh, float &sl, float2 a, float2 b) {
+  const float ph = __fmul_rn(a.x, b.x);
+  float pl = __fmaf_rn(a.x, b.x, -ph);
+  pl = __fmaf_rn(a.x, b.y, pl);
+  pl = __fmaf_rn(a.y, b.x, pl);
+  const float t = __fadd_rn(sh, ph);
+  const float bp = __fsub_rn(t, sh);
+  const float err = __fadd_rn(__fsub_rn(sh, __fsub_rn(t, bp)), __fsub_rn(ph, bp));
+  sl = __fadd_rn(sl, __fadd_rn(err, pl));
+  sh = t;
+}
+
+__device__ __forceinline__ void ff_renorm(float &sh, float &sl) {
+  const float t = __fadd_rn(sh, sl);
+  sl = __fsub_rn(sl, __fsub_rn(t, sh));
+  sh = t;
+}
+
 // C_partial[blk][i*k + j] = sum over the block's rows of A[r, a0+i] * B[r, b0+j]
 __global__ void __launch_bounds__(TN_THREADS) k_tn(int64_t n, const double *__restrict__ A, int lda, int a0, int m,
                                                    const double *__restrict__ B, int ldb, int b0, int k,
                                                    double *__restrict__ partial, int64_t rows_per_blk) {
   extern __shared__ double sm[];
-  double *As = sm;                 // [TN_ROWS][m]
-  double *Bs = sm + TN_ROWS * m;   // [TN_ROWS][k]
+  float2 *As = reinterpret_cast<float2 *>(sm);   // [TN_ROWS][m]
+  float2 *Bs = As + TN_ROWS * m;                 // [TN_ROWS][k]
   const int nout = m * k;
-  double acc[TN_MAXOUT];
+  float sh[TN_MAXOUT], sl[TN_MAXOUT];
 #pragma unroll
-  for (int o = 0; o < TN_MAXOUT; ++o) acc[o] = 0.0;
+  for (int o = 0; o < TN_MAXOUT; ++o) { sh[o] = 0.f; sl[o] = 0.f; }
   int64_t r0 = (int64_t)blockIdx.x * rows_per_blk;
   int64_t r1 = min(n, r0 + rows_per_blk);
   for (int64_t rt = r0; rt < r1; rt += TN_ROWS) {
     int rows = (int)min((int64_t)TN_ROWS, r1 - rt);
     for (int e = threadIdx.x; e < TN_ROWS * m; e += blockDim.x) {
       int rr = e / m, i = e - rr * m;
-      As[e] = (rr < rows) ? A[(rt + rr) * lda + a0 + i] : 0.0;
+      As[e] = (rr < rows) ? split_f64(A[(rt + rr) * lda + a0 + i]) : make_float2(0.f, 0.f);
     }
     for (int e = threadIdx.x; e < TN_ROWS * k; e += blockDim.x) {
       int rr = e / k, j = e - rr * k;
-      Bs[e] = (rr < rows) ? B[(rt + rr) * ldb + b0 + j] : 0.0;
+      Bs[e] = (rr < rows) ? split_f64(B[(rt + rr) * ldb + b0 + j]) : make_float2(0.f, 0.f);
     }
     __syncthreads();
 #pragma unroll
@@ -63,9 +106,11 @@ __global__ void __launch_bounds__(TN_THREADS) k_tn(int64_t n, const double *__re
       int idx = threadIdx.x + o * TN_THREADS;
       if (idx < nout) {
         int i = idx / k, j = idx - i * k;
-        double s = acc[o];
-        for (int rr = 0; rr < rows; ++rr) s = fma(As[rr * m + i], Bs[rr * k + j], s);
-        acc[o] = s;
+        float h = sh[o], l = sl[o];
+        for (int rr = 0; rr < rows; ++rr) ff_fma(h, l, As[rr * m + i], Bs[rr * k + j]);
+        ff_renorm(h, l);
+        sh[o] = h;
+        sl[o] = l;
       }
     }
     __syncthreads();
@@ -73,7 +118,7 @@ __global__ void __launch_bounds__(TN_THREADS) k_tn(int64_t n, const double *__re
 #pragma unroll
   for (int o = 0; o < TN_MAXOUT; ++o) {
     int idx = threadIdx.x + o * TN_THREADS;
-    if (idx < nout) partial[(int64_t)blockIdx.x * nout + idx] = acc[o];
+    if (idx < nout) partial[(int64_t)blockIdx.x * nout + idx] = (double)sh[o] + (double)sl[o];
   }
 }
 
@@ -89,29 +134,31 @@ __global__ void k_reduce_partials(const double *__restrict__ partial, int nblk, 
 }
 
 // Out[r, o0+j] = beta*Out[r, o0+j] + alpha * sum_i A[r, a0+i] * Y[i*ldy + y0 + j]
+// (float-float sums as in k_tn; alpha, beta and the update of Out in FP64)
 __global__ void __launch_bounds__(NN_THREADS) k_nn(int64_t n, const double *__restrict__ A, int lda, int a0, int m,
                                                    const double *__restrict__ Y, int ldy, int y0, int k, double alpha,
                                                    double beta, double *Out, int ldo, int o0) {
   extern __shared__ double sm[];
-  double *Ys = sm;              // [m][k]
-  double *As = sm + m * k;      // [32][m]
+  float2 *Ys = reinterpret_cast<float2 *>(sm);  // [m][k]
+  float2 *As = Ys + m * k;                      // [32][m]
   for (int e = threadIdx.x; e < m * k; e += blockDim.x) {
     int i = e / k, j = e - i * k;
-    Ys[e] = Y[i * ldy + y0 + j];
+    Ys[e] = split_f64(Y[i * ldy + y0 + j]);
   }
   __syncthreads();
   for (int64_t rt = (int64_t)blockIdx.x * 32; rt < n; rt += (int64_t)gridDim.x * 32) {
     int rows = (int)min((int64_t)32, n - rt);
     for (int e = threadIdx.x; e < 32 * m; e += blockDim.x) {
       int rr = e / m, i = e - rr * m;
-      As[e] = (rr < rows) ? A[(rt + rr) * lda + a0 + i] : 0.0;
+      As[e] = (rr < rows) ? split_f64(A[(rt + rr) * lda + a0 + i]) : make_float2(0.f, 0.f);
     }
     __syncthreads();
     for (int e = threadIdx.x; e < 32 * k; e += blockDim.x) {
       int rr = e / k, j = e - rr * k;
       if (rr < rows) {
-        double s = 0.0;
-        for (int i = 0; i < m; ++i) s = fma(As[rr * m + i], Ys[i * k + j], s);
+        float h = 0.f, l = 0.f;
+        for (int i = 0; i < m; ++i) ff_fma(h, l, As[rr * m + i], Ys[i * k + j]);
+        const double s = (double)h + (double)l;
         double *o = Out + (rt + rr) * ldo + o0 + j;
         *o = (beta == 0.0) ? alpha * s : fma(beta, *o, alpha * s);
       }

@@ -131,7 +131,35 @@ __global__ void __launch_bounds__(SIG_THREADS) k_spmm_mixed(int64_t nrows, const
 #pragma unroll
     for (int q = 0; q < K; ++q) { s[q] = 0.f; cmp[q] = 0.f; }
     const int64_t e = rowptr[r + 1];
-    for (int64_t t = rowptr[r] + lane; t < e; t += 32) {
+    int64_t t = rowptr[r] + lane;
+    if (K == 8) {
+      // four elements per lane in flight: the gathers are latency-bound, not bandwidth-bound
+      for (; t + 96 < e; t += 128) {
+        int cc[4];
+        float vv[4], xx[4][8];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          cc[u] = ldg_stream(col + t + 32 * u);
+          vv[u] = ldg_stream(val + t + 32 * u);
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+          asm("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+              : "=f"(xx[u][0]), "=f"(xx[u][1]), "=f"(xx[u][2]), "=f"(xx[u][3]), "=f"(xx[u][4]), "=f"(xx[u][5]),
+                "=f"(xx[u][6]), "=f"(xx[u][7])
+              : "l"(x + (int64_t)cc[u] * ldx));
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+#pragma unroll
+          for (int q = 0; q < K; ++q) {
+            const float yv = __fsub_rn(__fmul_rn(vv[u], xx[u][q]), cmp[q]);
+            const float tt = __fadd_rn(s[q], yv);
+            cmp[q] = __fsub_rn(__fsub_rn(tt, s[q]), yv);
+            s[q] = tt;
+          }
+      }
+    }
+    for (; t < e; t += 32) {
       const int c = ldg_stream(col + t);
       const float v = ldg_stream(val + t);
       const float *xr = x + (int64_t)c * ldx;
