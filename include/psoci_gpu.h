@@ -51,7 +51,9 @@ typedef struct {
 /* Precision of the stored Hamiltonian used by sigma. */
 typedef enum {
   PSOCI_PREC_FP64 = 0,   /* FP64 elements, FP64 products and sums                        */
-  PSOCI_PREC_MIXED = 1   /* FP32 elements and FP32 products, FP64 accumulation            */
+  PSOCI_PREC_MIXED = 1,  /* FP32 elements and FP32 products, FP64 accumulation            */
+  PSOCI_PREC_FF = 2      /* FP64 elements and inputs as FP32 hi+lo pairs, float-float      */
+                         /* products and sums (about 47 bits) on the FP32 pipe             */
 } psoci_prec;
 
 typedef enum {
@@ -109,7 +111,9 @@ PSOCI_API psoci_status psoci_build_hamiltonian(psoci_ctx *ctx, psoci_hmode mode,
  * attempt only (an undersized value slab makes the build evaluate twice).  The reference
  * reports its build time through PsociTimer; there is no direct counterpart. */
 typedef struct {
-  int64_t candidates;    /* configuration pairs within two excitations (ordered)             */
+  int64_t candidates;    /* configuration pairs the screen tested one by one (ordered): all   */
+                         /* pairs within two excitations (all-pairs screen), or those left  */
+                         /* after the per-hi-pattern integral test (lookup screen)          */
   int64_t pairs;         /* of those, pairs whose block is not zero from the integrals alone */
   int64_t segments;      /* warp work items (<= 32 neighbours of one row configuration)      */
   int64_t nnz;           /* stored elements, both triangles                                  */
@@ -162,7 +166,8 @@ typedef struct {
   int max_iter;        /* iteration limit (reference: 1000 per tolerance)                */
   double rtol;         /* residual-norm tolerance for convergence                        */
   psoci_prec prec;     /* sigma precision during the iterations                          */
-  int refine;          /* 1: FP64 sigma refinement pass after a MIXED run                */
+  int refine;          /* after a MIXED run: 1 refine with PSOCI_PREC_FF sigma,          */
+                       /* 2 refine with PSOCI_PREC_FP64 sigma, 0 no refinement           */
   int block;           /* 1: block Davidson (all unconverged roots per iteration);
                           0: one new vector per iteration, as the reference does          */
   double precond_min;  /* |D_i - lambda| guard of the preconditioner (reference 1e-3)     */
@@ -172,7 +177,7 @@ typedef struct {
   int iterations;      /* Davidson iterations                                            */
   int sigma_calls;     /* H*v products (counted per vector)                              */
   int collapses;       /* subspace contractions                                          */
-  int refine_iters;    /* FP64 iterations after the mixed phase                          */
+  int refine_iters;    /* refinement iterations after the mixed phase                    */
   double seconds;      /* wall time of psoci_davidson                                    */
   double sigma_seconds;/* device time inside sigma kernels                               */
 } psoci_dav_stats;

@@ -20,7 +20,7 @@ STATUS = {
     0: "ok", 1: "invalid argument", 2: "unsupported", 3: "call order", 4: "cuda error", 5: "out of device memory",
     6: "device wait timed out", 7: "not converged", 8: "non-finite value", 9: "i/o error",
 }
-PREC_FP64, PREC_MIXED = 0, 1
+PREC_FP64, PREC_MIXED, PREC_FF = 0, 1, 2
 HMODE_CSR_FP64, HMODE_CSR_BOTH = 0, 1
 
 

@@ -254,8 +254,8 @@ psoci_status psoci_sigma_device(psoci_ctx *c, int k, const double *dX, int ldx, 
   if (!c || !dX || !dY) return PSOCI_ERR_INVALID_ARG;
   psoci_status s;
   if ((s = set_device(c))) return s;
-  if (prec == PSOCI_PREC_MIXED) {
-    size_t need = (size_t)c->nsef_total * 8;
+  if (prec == PSOCI_PREC_MIXED || prec == PSOCI_PREC_FF) {
+    size_t need = (size_t)c->nsef_total * (prec == PSOCI_PREC_FF ? 16 : 8);
     if (c->x32_cap < need) {
       if ((s = psoci_alloc(c, &c->d_x32, need))) return s;
       c->x32_cap = need;

@@ -24,6 +24,7 @@
 #include <numeric>
 #include <vector>
 
+#include "ffmath.cuh"
 #include "psoci_internal.cuh"
 
 namespace {
@@ -34,48 +35,9 @@ constexpr int TN_MAXOUT = 8;      // outputs per thread => m*k <= 2048
 constexpr int NN_THREADS = 256;
 constexpr int MAX_SUB = 96;       // Jacobi keeps two m x m FP64 matrices in shared memory
 
-// The tall-skinny products below run in float-float arithmetic on the FP32 pipe: on GB300
-// the FP64 pipe issues ~2 FMA/clk/SM against 128 FP32 lanes, and these products are
-// FP64-bound.  Each FP64 operand is split into hi + lo floats by bit manipulation (no FP64
-// instruction): hi keeps the sign, the exponent and the top 23 mantissa bits, lo the other
-// 29 bits rounded to 24 — about 47 significant bits, 2^-47 relative.  Products are formed
-// error-free (hi*hi with its FMA residual, plus the cross terms) and summed with TwoSum into
-// a float pair; block partials are combined in FP64.  Operands below 2^-126 in magnitude
-// are treated as zero and those below 2^-74 keep hi only (absolute error < 2^-97); the
-// vectors here are normalised or bounded by |H|.
-__device__ __forceinline__ float2 split_f64(double x) {
-  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
-  const unsigned sign = (unsigned)(b >> 32) & 0x80000000u;
-  const int e = (int)((b >> 52) & 0x7ff);
-  if (e == 0x7ff) return make_float2(__int_as_float((int)(sign | 0x7fc00000u)), 0.f);  // inf / nan -> nan
-  if (e < 1023 - 126) return make_float2(__int_as_float((int)sign), 0.f);
-  if (e > 1023 + 127) return make_float2(__int_as_float((int)(sign | 0x7f800000u)), 0.f);
-  const unsigned mh = (unsigned)(b >> 29) & 0x7fffffu;
-  const float hi = __int_as_float((int)(sign | ((unsigned)(e - 1023 + 127) << 23) | mh));
-  const int el = e - 1075 + 127;  // biased exponent of 2^(e - 1075), the weight of lo's unit
-  float lo = 0.f;
-  if (el > 0) lo = __uint2float_rn((unsigned)(b & 0x1fffffffull)) * __int_as_float(el << 23);
-  return make_float2(hi, sign ? -lo : lo);
-}
-
-// (sh, sl) += a * b, a and b float pairs
-__device__ __forceinline__ void ff_fma(float &sh, float &sl, float2 a, float2 b) {
-  const float ph = __fmul_rn(a.x, b.x);
-  float pl = __fmaf_rn(a.x, b.x, -ph);
-  pl = __fmaf_rn(a.x, b.y, pl);
-  pl = __fmaf_rn(a.y, b.x, pl);
-  const float t = __fadd_rn(sh, ph);
-  const float bp = __fsub_rn(t, sh);
-  const float err = __fadd_rn(__fsub_rn(sh, __fsub_rn(t, bp)), __fsub_rn(ph, bp));
-  sl = __fadd_rn(sl, __fadd_rn(err, pl));
-  sh = t;
-}
-
-__device__ __forceinline__ void ff_renorm(float &sh, float &sl) {
-  const float t = __fadd_rn(sh, sl);
-  sl = __fsub_rn(sl, __fsub_rn(t, sh));
-  sh = t;
-}
+// The tall-skinny products below run in float-float arithmetic on the FP32 pipe (see
+// ffmath.cuh): on GB300 the FP64 pipe issues ~2 FMA/clk/SM against 128 FP32 lanes, and
+// these products are FP64-bound.  Block partials are combined in FP64.
 
 // C_partial[blk][i*k + j] = sum over the block's rows of A[r, a0+i] * B[r, b0+j]
 __global__ void __launch_bounds__(TN_THREADS) k_tn(int64_t n, const double *__restrict__ A, int lda, int a0, int m,
@@ -522,6 +484,8 @@ psoci_status psoci_davidson_impl(psoci_ctx *c, const psoci_dav_opts *o, double *
   maxsub = std::max(maxsub, 3 * nr);
   maxsub = std::min<int64_t>(maxsub, std::min<int64_t>(MAX_SUB, N));
   if (maxsub < 2 * nr && N >= 2 * nr) return psoci_fail(c, PSOCI_ERR_INVALID_ARG, "davidson: subspace too small");
+  if (o->prec != PSOCI_PREC_FP64 && o->prec != PSOCI_PREC_MIXED && o->prec != PSOCI_PREC_FF)
+    return psoci_fail(c, PSOCI_ERR_INVALID_ARG, "davidson: unknown precision");
   if (o->prec == PSOCI_PREC_MIXED && !c->d_val32)
     return psoci_fail(c, PSOCI_ERR_STATE, "davidson: MIXED needs PSOCI_HMODE_CSR_BOTH");
   const double rtol = o->rtol > 0 ? o->rtol : 1e-6;
@@ -548,8 +512,8 @@ psoci_status psoci_davidson_impl(psoci_ctx *c, const psoci_dav_opts *o, double *
       (s = psoci_alloc(c, &w.norms, 16)) || (s = psoci_alloc(c, &w.sel, 16)) || (s = psoci_alloc(c, &w.ibuf, 4)) ||
       (s = psoci_alloc(c, &w.idx, 16)))
     return s;
-  if (o->prec == PSOCI_PREC_MIXED || o->refine)
-    if ((s = psoci_alloc(c, &w.x32, (size_t)N * 8))) return s;
+  if (o->prec == PSOCI_PREC_MIXED || o->prec == PSOCI_PREC_FF || o->refine)
+    if ((s = psoci_alloc(c, &w.x32, (size_t)N * 16))) return s;  // FF staging: 8 float pairs per row
   cudaStream_t st = c->stream;
   const size_t jac_smem = sizeof(double) * 2 * MAX_SUB * MAX_SUB;
   PSOCI_CUDA(c, cudaFuncSetAttribute(k_jacobi, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)jac_smem));
@@ -567,7 +531,7 @@ psoci_status psoci_davidson_impl(psoci_ctx *c, const psoci_dav_opts *o, double *
   std::partial_sort(order.begin(), order.begin() + nr, order.end(),
                     [&](int64_t a, int64_t b) { return hdiag[a] < hdiag[b] || (hdiag[a] == hdiag[b] && a < b); });
   psoci_prec prec = o->prec;
-  bool refine_phase = (prec == PSOCI_PREC_FP64);
+  bool refine_phase = (prec != PSOCI_PREC_MIXED);  // FP64 and FF iterate to rtol directly
   const double tol_mixed = std::max(rtol, 1e-5);
   int m = nr;
   if (c->guess_k > 0 && (int64_t)c->guess.size() == (int64_t)c->guess_k * N) {
@@ -640,7 +604,7 @@ psoci_status psoci_davidson_impl(psoci_ctx *c, const psoci_dav_opts *o, double *
       if (!refine_phase && o->refine) {
         // FP64 refinement: restart from the Ritz vectors with exact (FP64) H products
         refine_phase = true;
-        prec = PSOCI_PREC_FP64;
+        prec = (o->refine == 2) ? PSOCI_PREC_FP64 : PSOCI_PREC_FF;
         if ((s = nn(w, w.V, ld, 0, m, w.Y, ld, 0, nr, 1.0, 0.0, w.T, nr, 0))) return s;
         int bk = 0;
         if ((s = orthonormalize(w, 0, nr, &bk))) return s;

@@ -332,6 +332,8 @@ struct JoinTabs {
   int s, G, L;
   const int32_t *gid, *lid, *T, *lnoff, *ln, *hdec;
   const uint32_t *lokey;
+  const int64_t *goff;    // per hi pattern g: its list of hi patterns h to visit ...
+  const uint32_t *glist;  // ... h | d_hi(g, h) << 28, ascending h
 };
 
 template <int W>
@@ -353,32 +355,72 @@ __device__ __forceinline__ void hi_bits(int code, int s, uint64_t (&e1)[W], uint
   if (kind == 2) set_bit_w<W>(e1, s + b);
 }
 
+// Hi-pattern lists.  For d_hi(g, h) = 4 the lo patterns must be equal, so the pair is a
+// double excitation between the hi orbitals alone and whether its block survives the
+// integral test (double_block_kept) depends on (g, h) only — it is decided here once
+// instead of once per configuration pair.  The list of g keeps every h with d_hi < 4 and
+// the h with d_hi = 4 whose block survives.  One warp per g, lanes over h; MODE 0 counts,
+// MODE 1 writes (ascending h).
+template <int W, int MODE>
+__global__ void k_group_lists(JoinTabs J, const double *__restrict__ eri, int64_t *gcnt, uint32_t *glist) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t g = warp; g < J.G; g += nwarps) {
+    uint64_t g1[W], g2[W];
+    hi_bits<W>(J.hdec[g], J.s, g1, g2);
+    int64_t n = 0;
+    const int64_t out = (MODE == 1) ? J.goff[g] : 0;
+    for (int h0 = 0; h0 < J.G; h0 += 32) {
+      const int h = h0 + lane;
+      bool take = false;
+      int d = 0;
+      if (h < J.G) {
+        uint64_t b1[W], b2[W];
+        hi_bits<W>(J.hdec[h], J.s, b1, b2);
+#pragma unroll
+        for (int w = 0; w < W; ++w) d += __popcll(g1[w] ^ b1[w]) + __popcll(g2[w] ^ b2[w]);
+        take = true;
+        if (d == 4) {
+          int ex[2], jy[2];
+          const int ni = excitation<W>(g1, g2, b1, b2, ex, jy);
+          take = (ni == 2) && double_block_kept(__ldg(eri + canon4(ex[0], jy[0], ex[1], jy[1])),
+                                                __ldg(eri + canon4(ex[0], jy[1], ex[1], jy[0])));
+        }
+      }
+      const unsigned b = __ballot_sync(0xffffffffu, take);
+      if (MODE == 1 && take) glist[out + n + __popc(b & ((1u << lane) - 1u))] = (uint32_t)h | ((uint32_t)d << 28);
+      n += __popc(b);
+    }
+    if (MODE == 0 && lane == 0) gcnt[g] = n;
+  }
+}
+
 template <int W, int MODE>
 __global__ void __launch_bounds__(256) k_join(Params P, JoinTabs J, int64_t *cnt, int64_t *ncand, const int64_t *off) {
-  __shared__ int s_pre[8][33], s_q0[8][32], s_lp[8][32];
+  __shared__ int s_pre[8][33], s_q0[8][32], s_lp[8][32], s_h[8][32];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
   const uint32_t lomask = (1u << J.s) - 1u;
   for (int64_t i = warp; i < P.nconf; i += nwarps) {
-    uint64_t a1[W], a2[W], hi1[W], hi2[W];
+    uint64_t a1[W], a2[W];
 #pragma unroll
     for (int w = 0; w < W; ++w) { a1[w] = P.e1[i * W + w]; a2[w] = P.e2[i * W + w]; }
     const int li = J.lid[i], js_i = P.jsym[i];
-    hi_bits<W>(J.hdec[J.gid[i]], J.s, hi1, hi2);
     int64_t nk = 0, nc = 0;
     int64_t base = (MODE == 1) ? off[i] : 0;
-    for (int h0 = 0; h0 < J.G; h0 += 32) {
+    const int64_t gl0 = J.goff[J.gid[i]], gl1 = J.goff[J.gid[i] + 1];
+    for (int64_t h0 = gl0; h0 < gl1; h0 += 32) {
       // this lane's hi pattern h: the lo patterns l' with d_lo <= 4 - d_hi, as a range of
-      // the neighbour list of l_i (or l_i alone when the hi patterns are disjoint)
-      const int h = h0 + lane;
+      // the neighbour list of l_i (or l_i alone when the hi patterns are disjoint: those
+      // blocks passed the integral test when the list was built)
+      int h = 0;
       int len = 0, q0 = 0, lp0 = li;
-      if (h < J.G) {
-        uint64_t g1[W], g2[W];
-        hi_bits<W>(J.hdec[h], J.s, g1, g2);
-        int d = 0;
-#pragma unroll
-        for (int w = 0; w < W; ++w) d += __popcll(hi1[w] ^ g1[w]) + __popcll(hi2[w] ^ g2[w]);
+      if (h0 + lane < gl1) {
+        const uint32_t ent = J.glist[h0 + lane];
+        h = (int)(ent & 0x0fffffffu);
+        const int d = (int)(ent >> 28);
         const int tau = 4 - d;
         if (tau <= 0) { len = 1; q0 = -1; }
         else {
@@ -396,6 +438,7 @@ __global__ void __launch_bounds__(256) k_join(Params P, JoinTabs J, int64_t *cnt
       s_pre[wib][lane] = incl - len;
       s_q0[wib][lane] = q0;
       s_lp[wib][lane] = lp0;
+      s_h[wib][lane] = h;
       __syncwarp();
       // the chunk's lookups, spread evenly over the lanes in (h, l') order
       for (int e0 = 0; e0 < tot; e0 += 32) {
@@ -407,15 +450,15 @@ __global__ void __launch_bounds__(256) k_join(Params P, JoinTabs J, int64_t *cnt
 #pragma unroll
           for (int st = 16; st > 0; st >>= 1)
             if (s_pre[wib][o + st] <= e) o += st;
-          const int qo = s_q0[wib][o];
+          const int qo = s_q0[wib][o], ho = s_h[wib][o];
           const int lp = (qo < 0) ? s_lp[wib][o] : J.ln[qo + (e - s_pre[wib][o])];
-          j = J.T[(int64_t)lp * J.G + (h0 + o)];
+          j = J.T[(int64_t)lp * J.G + ho];
           if (j >= 0) {
             found = true;
             keep = true;
-            if (j != (int)i) {
+            if (j != (int)i && qo >= 0) {
               uint64_t b1[W], b2[W];
-              hi_bits<W>(J.hdec[h0 + o], J.s, b1, b2);
+              hi_bits<W>(J.hdec[ho], J.s, b1, b2);
               const uint32_t key = J.lokey[lp];
               b1[0] |= key & lomask;
               b2[0] |= key >> J.s;
@@ -686,27 +729,33 @@ __device__ void pair_setup(const Params &P, int I, int J, PairInfo &pi, double *
 // ------------------------------------------------------------------------------------
 // determinant element <det a of A | H | det b of B>
 // ------------------------------------------------------------------------------------
-// The determinant tables and integrals det_elem reads, passed by value so that the
-// out-of-line function takes them in registers.
-struct DetTabs {
-  const uint64_t *alpha, *beta;
-  const uint8_t *phase, *nalpha;
-  const double *eri;
+// One determinant: alpha and beta bit-strings, phase, alpha count.
+template <int W>
+struct DetBits {
+  uint64_t al[W], be[W];
+  int ph, na;
 };
 
-// Kept out of line: sef_elem calls it four times, and four inlined copies of this body
-// overflow the instruction cache of the evaluation kernels.
 template <int W>
-__device__ __noinline__ double det_elem(const DetTabs P, const PairInfo &pi, const double *Kd, int64_t da,
-                                        int64_t db) {
-  uint64_t aa[W], ba[W], ab[W], bb[W];
+__device__ __forceinline__ void load_det(DetBits<W> &d, const uint64_t *alpha, const uint64_t *beta,
+                                         const uint8_t *phase, const uint8_t *nalpha, int64_t i) {
 #pragma unroll
-  for (int w = 0; w < W; ++w) {
-    aa[w] = __ldg(P.alpha + da * W + w); ba[w] = __ldg(P.beta + da * W + w);
-    ab[w] = __ldg(P.alpha + db * W + w); bb[w] = __ldg(P.beta + db * W + w);
-  }
-  int pha = __ldg(P.phase + da), phb = __ldg(P.phase + db);
-  int naa = __ldg(P.nalpha + da), nab = __ldg(P.nalpha + db);
+  for (int w = 0; w < W; ++w) { d.al[w] = alpha[i * W + w]; d.be[w] = beta[i * W + w]; }
+  d.ph = phase[i];
+  d.na = nalpha[i];
+}
+
+// <det a of A | H | det b of B> from the loaded determinants.  sef_elem calls it from a
+// single site (a loop over the determinant pairs of an SEF element), so the kernels hold
+// one copy of this body: several inlined copies overflow their instruction cache.
+template <int W>
+__device__ __forceinline__ double det_elem(const double *eri, const PairInfo &pi, const double *Kd,
+                                           const DetBits<W> &A, const DetBits<W> &B) {
+  const uint64_t(&aa)[W] = A.al;
+  const uint64_t(&ba)[W] = A.be;
+  const uint64_t(&ab)[W] = B.al;
+  const uint64_t(&bb)[W] = B.be;
+  const int pha = A.ph, phb = B.ph, naa = A.na, nab = B.na;
   uint64_t ua[W], ub[W];
 #pragma unroll
   for (int w = 0; w < W; ++w) { ua[w] = ab[w] & ~aa[w]; ub[w] = bb[w] & ~ba[w]; }
@@ -793,7 +842,7 @@ __device__ __noinline__ double det_elem(const DetTabs P, const PairInfo &pi, con
     int ncount = pha + phb;
     if (abs(iex2 - iex3) > 1) ncount += popc_range<W>(aa, min(iex2, iex3) + 1, max(iex2, iex3) - 1);
     if (abs(jex2 - jex3) > 1) ncount += popc_range<W>(ba, min(jex2, jex3) + 1, max(jex2, jex3) - 1);
-    double v = __ldg(P.eri + canon4(jex2, jex3, iex2, iex3));
+    double v = __ldg(eri + canon4(jex2, jex3, iex2, iex3));
     return (ncount & 1) ? -v : v;
   }
   // same-spin double (nmarka == 2: alpha, nmarka == 0: beta)
@@ -809,40 +858,70 @@ __device__ __noinline__ double det_elem(const DetTabs P, const PairInfo &pi, con
   return (ncount & 1) ? -v : v;
 }
 
+// Where sef_elem finds the determinants of A: the global tables, or a copy of A's own
+// determinants in shared memory (rows indexed from A's first determinant).
+struct RowDets {
+  const uint64_t *al, *be;
+  const uint8_t *ph, *na;
+};
+
 // SEF element (a, b) of the reference block (A, B): ciout / transformCDCt.  conn bit
 // (x << 1 | y) says whether determinant x of SEF a and determinant y of SEF b can couple;
 // a determinant element that cannot is exactly zero and is not evaluated (adding the zero
-// it would return leaves every partial sum unchanged).
+// it would return leaves every partial sum unchanged).  The determinant elements are
+// added in the reference's order: t = d00 + mB d01, u = d10 + mB d11, r (r t) + mA r (r u).
 template <int W>
 __device__ double sef_elem(const Params &PP, const PairInfo &pi, const double *Kd, int a, int b,
-                           unsigned conn = 0xFu) {
+                           unsigned conn = 0xFu, const RowDets *rowA = nullptr) {
   if (pi.kind == K_NONE) return 0.0;
-  const DetTabs P = {PP.alpha, PP.beta, PP.phase, PP.nalpha, PP.eri};
-  if (PP.nelec & 1) return (conn & 1u) ? det_elem<W>(P, pi, Kd, pi.detA + a, pi.detB + b) : 0.0;
-  const double r = sqrt(0.5);
-  const bool oa = pi.nopenA != 0, ob = pi.nopenB != 0;
+  const bool odd = PP.nelec & 1;
+  const bool oa = !odd && pi.nopenA != 0, ob = !odd && pi.nopenB != 0;
+  const int64_t a0 = odd ? a : (oa ? 2 * a : 0), b0 = pi.detB + (odd ? b : (ob ? 2 * b : 0));
+  if (!ob) conn &= 0x5u;
+  if (!oa) conn &= 0x3u;
+  DetBits<W> A[2] = {}, B[2] = {};
+#pragma unroll
+  for (int x = 0; x < 2; ++x) {
+    if (x == 1 && !oa) break;
+    if (rowA) load_det<W>(A[x], rowA->al, rowA->be, rowA->ph, rowA->na, a0 + x);
+    else load_det<W>(A[x], PP.alpha, PP.beta, PP.phase, PP.nalpha, pi.detA + a0 + x);
+  }
+#pragma unroll
+  for (int y = 0; y < 2; ++y) {
+    if (y == 1 && !ob) break;
+    load_det<W>(B[y], PP.alpha, PP.beta, PP.phase, PP.nalpha, b0 + y);
+  }
   const double mA = (pi.jsA % 2 != PP.ksym % 2) ? -1.0 : 1.0;
   const double mB = (pi.jsB % 2 != PP.ksym % 2) ? -1.0 : 1.0;
-  int64_t a0 = pi.detA + (oa ? 2 * a : 0), a1 = a0 + 1;
-  int64_t b0 = pi.detB + (ob ? 2 * b : 0), b1 = b0 + 1;
-  double ds0, ds1 = 0.0;
-  if (ob) {
-    double t = (conn & 1u) ? det_elem<W>(P, pi, Kd, a0, b0) : 0.0;
-    t += mB * ((conn & 2u) ? det_elem<W>(P, pi, Kd, a0, b1) : 0.0);
-    ds0 = t * r;
-    if (oa) {
-      double u = (conn & 4u) ? det_elem<W>(P, pi, Kd, a1, b0) : 0.0;
-      u += mB * ((conn & 8u) ? det_elem<W>(P, pi, Kd, a1, b1) : 0.0);
-      ds1 = u * r;
+  double t = 0.0, u = 0.0;
+#pragma unroll 1
+  for (int q = 0; q < 4; ++q) {
+    if (!((conn >> q) & 1u)) continue;
+    const int x = q >> 1, y = q & 1;
+    DetBits<W> Ax, By;  // selected by value: the arrays stay in registers
+#pragma unroll
+    for (int w = 0; w < W; ++w) {
+      Ax.al[w] = x ? A[1].al[w] : A[0].al[w];
+      Ax.be[w] = x ? A[1].be[w] : A[0].be[w];
+      By.al[w] = y ? B[1].al[w] : B[0].al[w];
+      By.be[w] = y ? B[1].be[w] : B[0].be[w];
     }
-  } else {
-    ds0 = (conn & 1u) ? det_elem<W>(P, pi, Kd, a0, b0) : 0.0;
-    if (oa) ds1 = (conn & 4u) ? det_elem<W>(P, pi, Kd, a1, b0) : 0.0;
+    Ax.ph = x ? A[1].ph : A[0].ph;
+    Ax.na = x ? A[1].na : A[0].na;
+    By.ph = y ? B[1].ph : B[0].ph;
+    By.na = y ? B[1].na : B[0].na;
+    const double d = det_elem<W>(PP.eri, pi, Kd, Ax, By);
+    if (x == 0) t = (y == 0) ? d : t + mB * d;
+    else u = (y == 0) ? d : u + mB * d;
   }
+  if (odd) return t;
+  const double r = sqrt(0.5);
+  const double ds0 = ob ? t * r : t;
+  const double ds1 = ob ? u * r : u;
   if (oa) {
-    double t = r * ds0;
-    t += (mA * r) * ds1;
-    return t;
+    double v = r * ds0;
+    v += (mA * r) * ds1;
+    return v;
   }
   return ds0;
 }
@@ -944,7 +1023,7 @@ struct FastSmem {
   PairInfo pi[PSOCI_SEG];
   double K[MAXK];
   uint64_t ra[FAST_MAXDET * W], rb[FAST_MAXDET * W];
-  uint8_t rna[FAST_MAXDET];
+  uint8_t rna[FAST_MAXDET], rph[FAST_MAXDET];
   // phase 2, per row: marked columns of each neighbour, their exclusive prefix, kept columns
   uint32_t mrow[PSOCI_SEG];
   int pre[PSOCI_SEG];
@@ -988,6 +1067,7 @@ __global__ void __launch_bounds__(WARPS_PER_CTA * 32) k_hbuild_fast(Params P) {
         ws->rb[d * W + w] = P.beta[(d0I + d) * W + w];
       }
       ws->rna[d] = P.nalpha[d0I + d];
+      ws->rph[d] = P.phase[d0I + d];
     }
     __syncwarp();
     // phase 1: connectivity masks C[r] for this lane's neighbour, bit-parallel over the
@@ -1102,6 +1182,7 @@ __global__ void __launch_bounds__(WARPS_PER_CTA * 32) k_hbuild_fast(Params P) {
     // same order, so each row stays in ascending column order.  Each warp takes slab space
     // in chunks and advances through a chunk by the kept count of each row.
     const int64_t prbase = P.pr_off[I] + (k0 - P.nbroff[I]) * nsefI;
+    const RowDets rowA = {ws->ra, ws->rb, ws->rph, ws->rna};  // I's determinants (A = I)
     for (int r = 0; r < nsefI; ++r) {
       const uint64_t cr = (lane < n) ? C[r] : 0ull;
       const uint32_t mr = (uint32_t)((cr | (cr >> 16) | (cr >> 32) | (cr >> 48)) & 0xffffull);
@@ -1150,7 +1231,7 @@ __global__ void __launch_bounds__(WARPS_PER_CTA * 32) k_hbuild_fast(Params P) {
           unsigned conn = (unsigned)((co & 1ull) | ((co >> 15) & 2ull) | ((co >> 30) & 4ull) | ((co >> 45) & 8ull));
           // a diagonal block is symmetric: the transposed element swaps the determinant roles
           if (flip) conn = (conn & 9u) | ((conn & 2u) << 1) | ((conn & 4u) >> 1);
-          v = sef_elem<W>(P, pi, ws->K, flip ? t : r, flip ? r : t, conn);
+          v = sef_elem<W>(P, pi, ws->K, flip ? t : r, flip ? r : t, conn, &rowA);
           keep = (fabs(v) >= PSOCI_MIN_VALUE) || (diag_blk && t == r);
           if (keep) atomicOr(&ws->keep[o], 1u << t);
         }
@@ -1404,6 +1485,8 @@ psoci_status run_build(psoci_ctx *c, psoci_hmode mode, int64_t *nnz_out) {
   int64_t *d_soff = nullptr, *d_tot = nullptr, *d_segslot = nullptr, *d_candoff = nullptr;
   int64_t *d_nlow = nullptr, *d_prrows = nullptr, *d_proff = nullptr;
   int32_t *d_cand = nullptr, *d_mk = nullptr;
+  int64_t *d_gcnt = nullptr, *d_goff = nullptr;
+  uint32_t *d_glist = nullptr;
   uint32_t *d_prm = nullptr;
   int *d_err = nullptr;
   unsigned long long *d_counter = nullptr;
@@ -1416,6 +1499,7 @@ psoci_status run_build(psoci_ctx *c, psoci_hmode mode, int64_t *nnz_out) {
     psoci_free(d_candoff); psoci_free(d_cand);
     psoci_free(d_nlow); psoci_free(d_prrows); psoci_free(d_proff); psoci_free(d_mk); psoci_free(d_prm);
     psoci_free(d_err); psoci_free(d_slabval);
+    psoci_free(d_gcnt); psoci_free(d_goff); psoci_free(d_glist);
     psoci_free(d_cnt); psoci_free(d_nbroff); psoci_free(d_nseg); psoci_free(d_nrow); psoci_free(d_segoff);
     psoci_free(d_rowslot); psoci_free(d_segk0); psoci_free(d_segrow); psoci_free(d_segcnt); psoci_free(d_rownnz);
     psoci_free(d_nbr); psoci_free(d_segcfg); psoci_free(d_segn);
@@ -1451,7 +1535,23 @@ psoci_status run_build(psoci_ctx *c, psoci_hmode mode, int64_t *nnz_out) {
   if (c->join_ok) {
     // by lookup, with the integral pruning fused
     JoinTabs J = {c->join_s, c->join_G, c->join_L, c->d_jgid, c->d_jlid, c->d_jT, c->d_jlnoff, c->d_jln,
-                  c->d_jhdec, c->d_jlokey};
+                  c->d_jhdec, c->d_jlokey, nullptr, nullptr};
+    // hi-pattern lists (depend on the integrals, so built here)
+    const int G = c->join_G;
+    TRY(psoci_alloc(c, &d_gcnt, G + 1));
+    TRY(psoci_alloc(c, &d_goff, G + 1));
+    const int gblocks = (int)std::max<int64_t>(1, std::min<int64_t>(((int64_t)G * 32 + 255) / 256, 152 * 32));
+    psoci_note_launch();
+    k_group_lists<W, 0><<<gblocks, 256, 0, st>>>(J, c->d_eri, d_gcnt, nullptr);
+    TRYC(cudaGetLastError());
+    int64_t nglist = 0;
+    TRY(psoci_scan_i64(c, d_gcnt, d_goff, G, &nglist));
+    TRY(psoci_alloc(c, &d_glist, nglist));
+    J.goff = d_goff;
+    psoci_note_launch();
+    k_group_lists<W, 1><<<gblocks, 256, 0, st>>>(J, c->d_eri, nullptr, d_glist);
+    TRYC(cudaGetLastError());
+    J.glist = d_glist;
     TRY(psoci_alloc(c, &d_cnt, n + 1));
     TRY(psoci_alloc(c, &d_tot, n + 1));
     TRY(psoci_alloc(c, &d_candoff, n + 1));

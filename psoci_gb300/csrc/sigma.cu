@@ -9,10 +9,14 @@
 //
 //   FP64 : FP64 elements, FP64 products and sums.
 //   MIXED: FP32 elements and FP32 inputs, FP32 products, compensated FP32 (Kahan / float-
-//          float) accumulation, FP64 result.  On GB300 the FP64 pipe issues ~2 FMA/clk/SM,
+//          float) accumulation, FP64 result.
+//   FF   : FP64 elements and inputs split into FP32 hi + lo pairs (inputs once per call,
+//          elements as they stream), error-free float-float products and sums — about 47
+//          significant bits on the FP32 pipe instead of FP64 on the FP64 pipe.  On GB300 the FP64 pipe issues ~2 FMA/clk/SM,
 //          so a kernel that adds in FP64 per element is bound by that pipe, not by HBM.
 #include <algorithm>
 
+#include "ffmath.cuh"
 #include "psoci_internal.cuh"
 
 namespace {
@@ -113,6 +117,21 @@ __global__ void __launch_bounds__(SIG_THREADS) k_spmm_f64(int64_t nrows, const i
   }
 }
 
+// the 8 floats at p (32-byte aligned) in one 256-bit read-only load
+__device__ __forceinline__ void ldg_row8(float (&f)[8], const float *p) {
+  asm("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+      : "=f"(f[0]), "=f"(f[1]), "=f"(f[2]), "=f"(f[3]), "=f"(f[4]), "=f"(f[5]), "=f"(f[6]), "=f"(f[7])
+      : "l"(p));
+}
+
+// Kahan step: the rounding error of every addition is carried in c and fed back
+__device__ __forceinline__ void kahan_add(float &s, float &c, float prod) {
+  const float yv = __fsub_rn(prod, c);
+  const float tt = __fadd_rn(s, yv);
+  c = __fsub_rn(__fsub_rn(tt, s), yv);
+  s = tt;
+}
+
 // MIXED: FP32 element x FP32 input products.  Each lane keeps a compensated FP32 sum per
 // vector (Kahan: the rounding error of every addition is carried in c and fed back), so
 // no FP64 arithmetic runs in the streaming loop — on GB300 the FP64 pipe, not HBM, would
@@ -121,8 +140,10 @@ template <int K>
 __global__ void __launch_bounds__(SIG_THREADS) k_spmm_mixed(int64_t nrows, const int64_t *__restrict__ rowptr,
                                                             const int32_t *__restrict__ col,
                                                             const float *__restrict__ val,
-                                                            const float *__restrict__ x, int ldx,
-                                                            double *__restrict__ y, int ldy) {
+                                                            const float *__restrict__ x, double *__restrict__ y,
+                                                            int ldy) {
+  // x: FP32 inputs with a row stride of 8 floats (32 bytes, 32-byte aligned) whatever K is, so
+  // every gather is one 256-bit load (sm_100+) — one L1 wavefront per gathered row
   const int lane = threadIdx.x & 31;
   const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
@@ -132,56 +153,29 @@ __global__ void __launch_bounds__(SIG_THREADS) k_spmm_mixed(int64_t nrows, const
     for (int q = 0; q < K; ++q) { s[q] = 0.f; cmp[q] = 0.f; }
     const int64_t e = rowptr[r + 1];
     int64_t t = rowptr[r] + lane;
-    if (K == 8) {
-      // four elements per lane in flight: the gathers are latency-bound, not bandwidth-bound
-      for (; t + 96 < e; t += 128) {
-        int cc[4];
-        float vv[4], xx[4][8];
+    // four elements per lane in flight: the gathers are latency-bound, not bandwidth-bound
+    for (; t + 96 < e; t += 128) {
+      int cc[4];
+      float vv[4], xx[4][8];
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
-          cc[u] = ldg_stream(col + t + 32 * u);
-          vv[u] = ldg_stream(val + t + 32 * u);
-        }
-#pragma unroll
-        for (int u = 0; u < 4; ++u)
-          asm("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
-              : "=f"(xx[u][0]), "=f"(xx[u][1]), "=f"(xx[u][2]), "=f"(xx[u][3]), "=f"(xx[u][4]), "=f"(xx[u][5]),
-                "=f"(xx[u][6]), "=f"(xx[u][7])
-              : "l"(x + (int64_t)cc[u] * ldx));
-#pragma unroll
-        for (int u = 0; u < 4; ++u)
-#pragma unroll
-          for (int q = 0; q < K; ++q) {
-            const float yv = __fsub_rn(__fmul_rn(vv[u], xx[u][q]), cmp[q]);
-            const float tt = __fadd_rn(s[q], yv);
-            cmp[q] = __fsub_rn(__fsub_rn(tt, s[q]), yv);
-            s[q] = tt;
-          }
+      for (int u = 0; u < 4; ++u) {
+        cc[u] = ldg_stream(col + t + 32 * u);
+        vv[u] = ldg_stream(val + t + 32 * u);
       }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) ldg_row8(xx[u], x + (int64_t)cc[u] * 8);
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int q = 0; q < K; ++q) kahan_add(s[q], cmp[q], __fmul_rn(vv[u], xx[u][q]));
     }
     for (; t < e; t += 32) {
       const int c = ldg_stream(col + t);
       const float v = ldg_stream(val + t);
-      const float *xr = x + (int64_t)c * ldx;
-      float xv[K];
-      if (K == 8) {
-        // the 8 inputs of one row are 32 contiguous, 32-byte-aligned bytes: one 256-bit load
-        // (sm_100+), i.e. one L1 wavefront per gathered row instead of two
-        asm("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
-            : "=f"(xv[0]), "=f"(xv[1]), "=f"(xv[2]), "=f"(xv[3]), "=f"(xv[4]), "=f"(xv[5]), "=f"(xv[6]),
-              "=f"(xv[7])
-            : "l"(xr));
-      } else {
+      float xv[8];
+      ldg_row8(xv, x + (int64_t)c * 8);
 #pragma unroll
-        for (int q = 0; q < K; ++q) xv[q] = __ldg(xr + q);
-      }
-#pragma unroll
-      for (int q = 0; q < K; ++q) {
-        float yv = __fsub_rn(__fmul_rn(v, xv[q]), cmp[q]);
-        float tt = __fadd_rn(s[q], yv);
-        cmp[q] = __fsub_rn(__fsub_rn(tt, s[q]), yv);
-        s[q] = tt;
-      }
+      for (int q = 0; q < K; ++q) kahan_add(s[q], cmp[q], __fmul_rn(v, xv[q]));
     }
     // Kahan leaves sum = s - cmp; reduce (s, -cmp) as float-float pairs, FP64 only at the end
     ff2 v[8];
@@ -209,12 +203,100 @@ __global__ void __launch_bounds__(SIG_THREADS) k_spmm_mixed(int64_t nrows, const
   }
 }
 
-// X (FP64, leading dim ldx) -> X32 (FP32, leading dim k); one thread per row
+// warp reduce-scatter of K float-float lane sums; the lane holding value q writes it
+template <int K>
+__device__ __forceinline__ void store_reduced_ff(ff2 (&v)[8], int lane, double *yr) {
+  ff2 a[4], b[2], cc;
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const bool hi = lane & 16;
+    a[i] = ff_add(hi ? v[i + 4] : v[i], shfl_ff(hi ? v[i] : v[i + 4], 16));
+  }
+#pragma unroll
+  for (int i = 0; i < 2; ++i) {
+    const bool hi = lane & 8;
+    b[i] = ff_add(hi ? a[i + 2] : a[i], shfl_ff(hi ? a[i] : a[i + 2], 8));
+  }
+  {
+    const bool hi = lane & 4;
+    cc = ff_add(hi ? b[1] : b[0], shfl_ff(hi ? b[0] : b[1], 4));
+  }
+  cc = ff_add(cc, shfl_ff(cc, 2));
+  cc = ff_add(cc, shfl_ff(cc, 1));
+  const int qq = lane >> 2;
+  if ((lane & 3) == 0 && qq < K) yr[qq] = (double)cc.h + (double)cc.l;
+}
+
+// FF: FP64 elements split as they stream, inputs pre-split into float pairs (x2, K per row)
+template <int K>
+__global__ void __launch_bounds__(SIG_THREADS) k_spmm_ff(int64_t nrows, const int64_t *__restrict__ rowptr,
+                                                         const int32_t *__restrict__ col,
+                                                         const double *__restrict__ val,
+                                                         const float2 *__restrict__ x2, double *__restrict__ y,
+                                                         int ldy) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t r = warp; r < nrows; r += nwarps) {
+    float sh[K], sl[K];
+#pragma unroll
+    for (int q = 0; q < K; ++q) { sh[q] = 0.f; sl[q] = 0.f; }
+    const int64_t e = rowptr[r + 1];
+    for (int64_t t = rowptr[r] + lane; t < e; t += 32) {
+      const int c = ldg_stream(col + t);
+      const float2 v = split_f64(ldg_stream(val + t));
+      const float2 *xr = x2 + (int64_t)c * K;
+      float2 xv[K];
+      if (K == 8) {
+        // 8 pairs = 64 contiguous, 64-byte-aligned bytes: two 256-bit loads
+        float f[16];
+        asm("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+            : "=f"(f[0]), "=f"(f[1]), "=f"(f[2]), "=f"(f[3]), "=f"(f[4]), "=f"(f[5]), "=f"(f[6]), "=f"(f[7])
+            : "l"(xr));
+        asm("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+            : "=f"(f[8]), "=f"(f[9]), "=f"(f[10]), "=f"(f[11]), "=f"(f[12]), "=f"(f[13]), "=f"(f[14]), "=f"(f[15])
+            : "l"(xr + 4));
+#pragma unroll
+        for (int q = 0; q < K; ++q) xv[q] = make_float2(f[2 * q], f[2 * q + 1]);
+      } else {
+#pragma unroll
+        for (int q = 0; q < K; ++q) xv[q] = __ldg(xr + q);
+      }
+#pragma unroll
+      for (int q = 0; q < K; ++q) ff_fma(sh[q], sl[q], v, xv[q]);
+    }
+    ff2 vv[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      if (q < K) {
+        float h = sh[q], l = sl[q];
+        ff_renorm(h, l);
+        vv[q] = ff2{h, l};
+      } else {
+        vv[q] = ff2{0.f, 0.f};
+      }
+    }
+    store_reduced_ff<K>(vv, lane, y + r * ldy);
+  }
+}
+
+// X (FP64, leading dim ldx) -> X2 (float pairs, leading dim k); one thread per row
+__global__ void k_split_x(int64_t n, int k, const double *__restrict__ x, int ldx, float2 *__restrict__ x2) {
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+    for (int q = 0; q < k; ++q) x2[r * k + q] = split_f64(x[r * ldx + q]);
+  }
+}
+
+// X (FP64, leading dim ldx, k <= 8 columns) -> X32 (FP32, row stride 8); one thread per row
 __global__ void k_to_f32(int64_t n, int k, const double *__restrict__ x, int ldx, float *__restrict__ x32) {
   for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
     const double *src = x + r * ldx;
-    float *dst = x32 + r * k;
-    for (int q = 0; q < k; ++q) dst[q] = (float)src[q];
+    float4 *dst = reinterpret_cast<float4 *>(x32 + r * 8);  // row stride 8, zero padded
+    float f[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) f[q] = (q < k) ? (float)src[q] : 0.f;
+    dst[0] = make_float4(f[0], f[1], f[2], f[3]);
+    dst[1] = make_float4(f[4], f[5], f[6], f[7]);
   }
 }
 
@@ -228,15 +310,20 @@ void launch_k(psoci_ctx *c, int64_t n, const double *dX, int ldx, double *dY, in
   if (prec == PSOCI_PREC_FP64)
     k_spmm_f64<K><<<blocks, SIG_THREADS, 0, c->stream>>>(n, c->d_rowptr, c->d_col, c->d_val, dX, ldx, dY, ldy,
                                                          ((uintptr_t)dX % 16 == 0) && (ldx % 2 == 0));
+  else if (prec == PSOCI_PREC_FF)
+    k_spmm_ff<K><<<blocks, SIG_THREADS, 0, c->stream>>>(n, c->d_rowptr, c->d_col, c->d_val,
+                                                        reinterpret_cast<const float2 *>(x32), dY, ldy);
   else
-    k_spmm_mixed<K><<<blocks, SIG_THREADS, 0, c->stream>>>(n, c->d_rowptr, c->d_col, c->d_val32, x32, ld32, dY, ldy);
+    k_spmm_mixed<K><<<blocks, SIG_THREADS, 0, c->stream>>>(n, c->d_rowptr, c->d_col, c->d_val32, x32, dY, ldy);
 }
 
 }  // namespace
 
-// dX32: FP32 staging of at least N*k floats (MIXED only); may be null for FP64.
+// dX32: staging of at least N*8 floats (MIXED) or N*16 floats (FF); may be null for FP64.
 psoci_status psoci_sigma_launch(psoci_ctx *c, int k, const double *dX, int ldx, double *dY, int ldy,
                                 psoci_prec prec, float *dX32) {
+  if (prec != PSOCI_PREC_FP64 && prec != PSOCI_PREC_MIXED && prec != PSOCI_PREC_FF)
+    return psoci_fail(c, PSOCI_ERR_INVALID_ARG, "sigma: unknown precision");
   if (!c->have_h) return psoci_fail(c, PSOCI_ERR_STATE, "sigma: Hamiltonian not built");
   if (k < 1 || ldx < k || ldy < k) return psoci_fail(c, PSOCI_ERR_INVALID_ARG, "sigma: bad k / leading dimensions");
   if (prec == PSOCI_PREC_MIXED && !c->d_val32)
@@ -253,6 +340,12 @@ psoci_status psoci_sigma_launch(psoci_ctx *c, int k, const double *dX, int ldx, 
       int blocks = (int)std::min<int64_t>((n + 255) / 256, 152 * 16);
       psoci_note_launch();
       k_to_f32<<<std::max(blocks, 1), 256, 0, c->stream>>>(n, kk, xs, ldx, dX32);
+      x32 = dX32;
+    } else if (prec == PSOCI_PREC_FF) {
+      if (!dX32) return psoci_fail(c, PSOCI_ERR_INVALID_ARG, "sigma: FF without staging");
+      int blocks = (int)std::min<int64_t>((n + 255) / 256, 152 * 16);
+      psoci_note_launch();
+      k_split_x<<<std::max(blocks, 1), 256, 0, c->stream>>>(n, kk, xs, ldx, reinterpret_cast<float2 *>(dX32));
       x32 = dX32;
     }
     switch (kk) {

@@ -16,6 +16,7 @@ pytestmark = pytest.mark.gpu
 
 H_TOL = 1e-12
 SIGMA_RTOL = 1e-12
+FF_RTOL = 1e-11
 EIG_TOL_FP64 = 1e-10
 EIG_TOL_MIXED = 1e-7
 
@@ -131,6 +132,8 @@ def test_sigma_fp64_and_mixed(oracle_mod):
         assert np.abs(Y - Yref).max() <= SIGMA_RTOL * scale * 10
         Ym = c.sigma(X, prec=1)
         assert np.abs(Ym - Yref).max() <= 1e-5 * scale
+        Yf = c.sigma(X, prec=2)  # float-float: about 47 significant bits
+        assert np.abs(Yf - Yref).max() <= FF_RTOL * scale
 
 
 @pytest.mark.parametrize("name,ksym", [("fci_6e8o", 1), ("fci_5e6o", 2)])
@@ -145,8 +148,11 @@ def test_davidson_fp64_and_mixed(oracle_mod, name, ksym):
     c.build_hamiltonian(mixed=True)
     r64 = c.davidson(nroots, rtol=1e-8, mixed=False)
     assert np.abs(r64.evals - ref[:nroots]).max() <= EIG_TOL_FP64, (r64.evals, ref[:nroots])
-    rmx = c.davidson(nroots, rtol=1e-8, mixed=True, refine=True)
+    rmx = c.davidson(nroots, rtol=1e-8, mixed=True, refine=True)  # float-float refinement
     assert np.abs(rmx.evals - ref[:nroots]).max() <= EIG_TOL_MIXED
+    assert rmx.refine_iters >= 1
+    rm2 = c.davidson(nroots, rtol=1e-8, mixed=True, refine=2)  # FP64 refinement
+    assert np.abs(rm2.evals - ref[:nroots]).max() <= EIG_TOL_MIXED
     r1 = c.davidson(nroots, rtol=1e-8, mixed=False, block=False)
     assert np.abs(r1.evals - ref[:nroots]).max() <= EIG_TOL_FP64
 
