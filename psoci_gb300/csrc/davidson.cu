@@ -47,6 +47,9 @@ __global__ void __launch_bounds__(TN_THREADS) k_tn(int64_t n, const double *__re
   float2 *As = reinterpret_cast<float2 *>(sm);   // [TN_ROWS][m]
   float2 *Bs = As + TN_ROWS * m;                 // [TN_ROWS][k]
   const int nout = m * k;
+  // fewer outputs than threads: S threads share each output, splitting the tile's rows
+  const int S = (nout >= TN_THREADS) ? 1 : TN_THREADS / nout;
+  const int sub = (S > 1) ? (int)threadIdx.x / nout : 0;
   float sh[TN_MAXOUT], sl[TN_MAXOUT];
 #pragma unroll
   for (int o = 0; o < TN_MAXOUT; ++o) { sh[o] = 0.f; sl[o] = 0.f; }
@@ -63,24 +66,45 @@ __global__ void __launch_bounds__(TN_THREADS) k_tn(int64_t n, const double *__re
       Bs[e] = (rr < rows) ? split_f64(B[(rt + rr) * ldb + b0 + j]) : make_float2(0.f, 0.f);
     }
     __syncthreads();
+    if (S == 1) {
 #pragma unroll
-    for (int o = 0; o < TN_MAXOUT; ++o) {
-      int idx = threadIdx.x + o * TN_THREADS;
-      if (idx < nout) {
-        int i = idx / k, j = idx - i * k;
-        float h = sh[o], l = sl[o];
-        for (int rr = 0; rr < rows; ++rr) ff_fma(h, l, As[rr * m + i], Bs[rr * k + j]);
-        ff_renorm(h, l);
-        sh[o] = h;
-        sl[o] = l;
+      for (int o = 0; o < TN_MAXOUT; ++o) {
+        int idx = threadIdx.x + o * TN_THREADS;
+        if (idx < nout) {
+          int i = idx / k, j = idx - i * k;
+          float h = sh[o], l = sl[o];
+          for (int rr = 0; rr < rows; ++rr) ff_fma(h, l, As[rr * m + i], Bs[rr * k + j]);
+          ff_renorm(h, l);
+          sh[o] = h;
+          sl[o] = l;
+        }
       }
+    } else if (sub < S) {
+      const int idx = (int)threadIdx.x - sub * nout, i = idx / k, j = idx - i * k;
+      float h = sh[0], l = sl[0];
+      for (int rr = sub; rr < rows; rr += S) ff_fma(h, l, As[rr * m + i], Bs[rr * k + j]);
+      ff_renorm(h, l);
+      sh[0] = h;
+      sl[0] = l;
     }
     __syncthreads();
   }
+  if (S == 1) {
 #pragma unroll
-  for (int o = 0; o < TN_MAXOUT; ++o) {
-    int idx = threadIdx.x + o * TN_THREADS;
-    if (idx < nout) partial[(int64_t)blockIdx.x * nout + idx] = (double)sh[o] + (double)sl[o];
+    for (int o = 0; o < TN_MAXOUT; ++o) {
+      int idx = threadIdx.x + o * TN_THREADS;
+      if (idx < nout) partial[(int64_t)blockIdx.x * nout + idx] = (double)sh[o] + (double)sl[o];
+    }
+  } else {
+    // combine the S shares of each output in FP64, in a fixed order
+    double *red = sm;  // the tiles are no longer needed
+    red[threadIdx.x] = (sub < S) ? (double)sh[0] + (double)sl[0] : 0.0;
+    __syncthreads();
+    if ((int)threadIdx.x < nout) {
+      double t = 0.0;
+      for (int q = 0; q < S; ++q) t += red[threadIdx.x + q * nout];
+      partial[(int64_t)blockIdx.x * nout + threadIdx.x] = t;
+    }
   }
 }
 
@@ -399,7 +423,7 @@ psoci_status tn(Work &w, const double *A, int lda, int a0, int m, const double *
                 int ldc, int c0) {
   psoci_ctx *c = w.c;
   if (m * k > TN_THREADS * TN_MAXOUT) return psoci_fail(c, PSOCI_ERR_INVALID_ARG, "tn: block too large");
-  size_t smem = sizeof(double) * TN_ROWS * (m + k);
+  size_t smem = sizeof(double) * std::max(TN_ROWS * (m + k), TN_THREADS);
   psoci_note_launch();
   k_tn<<<w.nblk, TN_THREADS, smem, c->stream>>>(w.N, A, lda, a0, m, B, ldb, b0, k, w.partial, w.rows_per_blk);
   psoci_note_launch();
