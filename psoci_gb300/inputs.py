@@ -308,6 +308,8 @@ def named_workload(name: str, seed: int = 0, ksym: int = 1) -> Problem:
         # the same space with 16 and 24 virtuals (263,004 / 568,204 SEFs): profiler captures
         "mrcisd_6e8o_v16": ("mrcisd", dict(nact=8, nelec=6, nvirt=16)),
         "mrcisd_6e8o_v24": ("mrcisd", dict(nact=8, nelec=6, nvirt=24)),
+        # 66 orbitals (two-word bit-strings, like the 72-orbital benchmark space), 124,815 SEFs
+        "mrcisd_4e6o_v60": ("mrcisd", dict(nact=6, nelec=4, nvirt=60)),
         # scaled MRCISD: CAS(6e,8o) + singles and doubles into 64 virtuals (~3.8M SEFs)
         "mrcisd_6e8o_v64": ("mrcisd", dict(nact=8, nelec=6, nvirt=64)),
         # small cases for tests
