@@ -33,7 +33,7 @@ sys.path.insert(0, ROOT)
 # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) from ncu captures of
 # a smaller case of the same space, scaled to the full launch by the units processed; the
 # captures and the scaling are summarised under profiles/.
-TRAFFIC = {}
+TRAFFIC = {("k_hbuild_fast", "mrcisd_6e8o_v64"): 2.00e10, ("k_spmm_mixed", "mrcisd_6e8o_v64"): 1.91e10}
 
 NROOTS = 8
 RTOL = 1e-5          # residual norm; |dE| ~ r^2/gap, well inside 1e-7 Eh (checked below)
