@@ -1314,9 +1314,17 @@ __global__ void k_mirror_count(Params P, int64_t *row_nnz, int32_t *mk, int *err
 }
 
 // One warp per configuration: columns, values (and the FP32 copy and the diagonal) of its
-// rows; lane r carries the write position of row r.
-__global__ void k_assemble(Params P, const int32_t *mk) {
-  const int lane = threadIdx.x & 31;
+// rows; lane r carries the write position of row r.  Entries are spread over the lanes one
+// per lane (e = lane, lane + 32, ...), so consecutive lanes write consecutive positions:
+// the lane that owns entry e is found by binary search over the per-pair offsets.
+constexpr int ASM_THREADS = 256;
+__global__ void __launch_bounds__(ASM_THREADS) k_assemble(Params P, const int32_t *mk) {
+  __shared__ int s_off[ASM_THREADS / 32][33];     // per lane: first entry of the lane in the run
+  __shared__ uint32_t s_msk[ASM_THREADS / 32][32];  // per lane: columns t of the run, as bits
+  __shared__ int32_t s_J[ASM_THREADS / 32][32];
+  __shared__ int64_t s_col[ASM_THREADS / 32][32], s_rs[ASM_THREADS / 32][32];
+  __shared__ uint32_t s_mm[ASM_THREADS / 32][32][FAST_MAXSEF];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
   for (int64_t I = warp; I < P.nconf; I += nwarps) {
@@ -1324,34 +1332,42 @@ __global__ void k_assemble(Params P, const int32_t *mk) {
     const int nsefI = (int)(P.sefoff[I + 1] - row0);
     const int64_t b0 = P.nbroff[I], nl = P.nlow[I], nn = P.nbroff[I + 1] - b0;
     int64_t mypos = (lane < nsefI) ? P.rowptr[row0 + lane] : 0;
-    // lower pairs, segment by segment
+    // lower pairs, segment by segment: the run of (segment, row r) is contiguous in the slab
+    // and in row r, in the same order
     for (int64_t sg = P.segoff[I]; sg < P.segoff[I + 1]; ++sg) {
       const int64_t k0 = P.seg_k0[sg];
       const int ns = P.seg_n[sg];
-      int J = -1;
-      int64_t colJ = 0;
-      if (lane < ns) { J = P.nbr[k0 + lane]; colJ = P.sefoff[J]; }
+      if (lane < ns) {
+        const int J = P.nbr[k0 + lane];
+        s_J[wib][lane] = J;
+        s_col[wib][lane] = P.sefoff[J];
+      }
       const uint32_t *pm = P.prm + P.pr_off[I] + (k0 - b0 + lane) * nsefI;
       for (int r = 0; r < nsefI; ++r) {
         const int64_t slot = P.seg_rowoff[sg] + r;
+        const int cnt = (int)P.seg_cnt[slot];
+        const int64_t src0 = P.seg_slot[slot];
         const int64_t dst = __shfl_sync(0xffffffffu, mypos, r);
-        if (lane < ns) {
-          const uint32_t w = pm[r];
-          uint32_t m = w & 0xffffu;
-          const int64_t src = P.seg_slot[slot] + (w >> 16), d0 = dst + (w >> 16);
-          int j = 0;
-          while (m) {
-            const int t = __ffs(m) - 1;
-            m &= m - 1;
-            const double v = P.slab_val[src + j];
-            P.col[d0 + j] = (int32_t)(colJ + t);
-            P.val[d0 + j] = v;
-            if (P.val32) P.val32[d0 + j] = (float)v;
-            if (J == (int)I && t == r) P.diag[row0 + r] = v;
-            ++j;
-          }
+        const uint32_t w = (lane < ns) ? pm[r] : ((uint32_t)cnt << 16);
+        s_off[wib][lane] = (int)(w >> 16);
+        s_msk[wib][lane] = w & 0xffffu;
+        __syncwarp();
+        for (int e = lane; e < cnt; e += 32) {
+          int o = 0;
+#pragma unroll
+          for (int st = 16; st > 0; st >>= 1)
+            if (o + st < 32 && s_off[wib][o + st] <= e) o += st;
+          uint32_t m = s_msk[wib][o];
+          for (int q = e - s_off[wib][o]; q > 0; --q) m &= m - 1;
+          const int t = __ffs(m) - 1;
+          const double v = P.slab_val[src0 + e];
+          P.col[dst + e] = (int32_t)(s_col[wib][o] + t);
+          P.val[dst + e] = v;
+          if (P.val32) P.val32[dst + e] = (float)v;
+          if (s_J[wib][o] == (int)I && t == r) P.diag[row0 + r] = v;
         }
-        if (lane == r) mypos += P.seg_cnt[slot];
+        __syncwarp();
+        if (lane == r) mypos += cnt;
       }
     }
     // upper neighbours, 32 at a time: column r of their lower block (J, I)
@@ -1374,10 +1390,15 @@ __global__ void k_assemble(Params P, const int32_t *mk) {
             if (t < nsefJ) mm[t] = pm[t];
         }
       }
-      for (int r = 0; r < nsefI; ++r) {
-        int cnt = 0;
 #pragma unroll
-        for (int t = 0; t < FAST_MAXSEF; ++t) cnt += (int)((mm[t] >> r) & 1u);
+      for (int t = 0; t < FAST_MAXSEF; ++t) s_mm[wib][lane][t] = mm[t];
+      s_col[wib][lane] = colJ;
+      s_rs[wib][lane] = rowslotJ;
+      for (int r = 0; r < nsefI; ++r) {
+        uint32_t cm = 0u;  // columns t of this lane's block whose row t keeps column r
+#pragma unroll
+        for (int t = 0; t < FAST_MAXSEF; ++t) cm |= ((mm[t] >> r) & 1u) << t;
+        const int cnt = __popc(cm);
         int incl = cnt;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
@@ -1385,21 +1406,29 @@ __global__ void k_assemble(Params P, const int32_t *mk) {
           if (lane >= o) incl += v;
         }
         const int tot = __shfl_sync(0xffffffffu, incl, 31);
-        int64_t d = __shfl_sync(0xffffffffu, mypos, r) + (incl - cnt);
+        const int64_t dst = __shfl_sync(0xffffffffu, mypos, r);
+        s_off[wib][lane] = incl - cnt;
+        s_msk[wib][lane] = cm;
+        __syncwarp();
         const uint32_t below = (1u << r) - 1u;
+        for (int e = lane; e < tot; e += 32) {
+          int o = 0;
 #pragma unroll
-        for (int t = 0; t < FAST_MAXSEF; ++t) {
-          if ((mm[t] >> r) & 1u) {
-            const int64_t src = P.seg_slot[rowslotJ + t] + (mm[t] >> 16) + __popc(mm[t] & below);
-            const double v = P.slab_val[src];
-            P.col[d] = (int32_t)(colJ + t);
-            P.val[d] = v;
-            if (P.val32) P.val32[d] = (float)v;
-            ++d;
-          }
+          for (int st = 16; st > 0; st >>= 1)
+            if (o + st < 32 && s_off[wib][o + st] <= e) o += st;
+          uint32_t m = s_msk[wib][o];
+          for (int q = e - s_off[wib][o]; q > 0; --q) m &= m - 1;
+          const int t = __ffs(m) - 1;
+          const uint32_t wt = s_mm[wib][o][t];
+          const double v = P.slab_val[P.seg_slot[s_rs[wib][o] + t] + (wt >> 16) + __popc(wt & below)];
+          P.col[dst + e] = (int32_t)(s_col[wib][o] + t);
+          P.val[dst + e] = v;
+          if (P.val32) P.val32[dst + e] = (float)v;
         }
+        __syncwarp();
         if (lane == r) mypos += tot;
       }
+      __syncwarp();
     }
   }
 }
@@ -1722,7 +1751,7 @@ psoci_status run_build(psoci_ctx *c, psoci_hmode mode, int64_t *nnz_out) {
     t_e = tnow();
     // 5. ordered assembly
     psoci_note_launch();
-    k_assemble<<<cfg_blocks, 256, 0, st>>>(P, d_mk);
+    k_assemble<<<cfg_blocks, ASM_THREADS, 0, st>>>(P, d_mk);
     TRYC(cudaGetLastError());
     TRYC(cudaEventRecord(ev[5], st));
     TRYC(cudaStreamSynchronize(st));
