@@ -126,6 +126,21 @@ class Oracle(_Base):
         f = self._fn("build_rows", ctypes.c_long, [ctypes.c_void_p, ctypes.c_int, _c_int_p, ctypes.c_int])
         return f(self.ctx, nthreads, _p(r, _c_int_p), len(r))
 
+    def ciden_block(self, i, j):
+        ns = self.p.nsef()
+        out = np.zeros(int(ns[i] * ns[j]))
+        st = self._fn("ciden_block", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, _c_dbl_p])(
+            self.ctx, i, j, _p(out, _c_dbl_p))
+        return st, out.reshape(int(ns[i]), int(ns[j]))
+
+    def density1(self, vecs):
+        """Packed 1-particle densities (k x nbf(nbf+1)/2) of root-major vectors (k x N)."""
+        v = np.ascontiguousarray(np.atleast_2d(vecs), np.float64)
+        out = np.zeros((v.shape[0], self.p.nbf * (self.p.nbf + 1) // 2))
+        self._fn("density1", None, [ctypes.c_void_p, ctypes.c_int, _c_dbl_p, _c_dbl_p])(
+            self.ctx, v.shape[0], _p(v, _c_dbl_p), _p(out, _c_dbl_p))
+        return out
+
     def diag(self):
         d = np.zeros(self.num_sefs())
         self._fn("diag", None, [ctypes.c_void_p, _c_dbl_p])(self.ctx, _p(d, _c_dbl_p))
@@ -189,6 +204,19 @@ class Reference(_Base):
         out = np.zeros(int(ns[i] * ns[j]))
         st = self._fn("block", ctypes.c_int, [ctypes.c_int, ctypes.c_int, _c_dbl_p])(i, j, _p(out, _c_dbl_p))
         return st, out.reshape(int(ns[i]), int(ns[j]))
+
+    def ciden_block(self, i, j):
+        ns = self.p.nsef()
+        out = np.zeros(int(ns[i] * ns[j]))
+        st = self._fn("ciden_block", ctypes.c_int, [ctypes.c_int, ctypes.c_int, _c_dbl_p])(i, j, _p(out, _c_dbl_p))
+        return st, out.reshape(int(ns[i]), int(ns[j]))
+
+    def density1(self, vecs):
+        v = np.ascontiguousarray(np.atleast_2d(vecs), np.float64)
+        out = np.zeros((v.shape[0], self.p.nbf * (self.p.nbf + 1) // 2))
+        self._fn("density1", None, [_c_u8_p, ctypes.c_int, _c_dbl_p, _c_dbl_p])(
+            _p(self._occ, _c_u8_p), v.shape[0], _p(v, _c_dbl_p), _p(out, _c_dbl_p))
+        return out
 
     def build_lower(self, nthreads=0):
         nthreads = nthreads or os.cpu_count() or 1

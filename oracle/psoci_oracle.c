@@ -686,3 +686,126 @@ void orc_sigma_lower(long n, const long *rowptr, const int *cols, const double *
   }
   for (int t = 0; t < nthreads; ++t) pthread_join(th[t], NULL);
 }
+
+/* ---------------------------------------------------------------------------
+ * 1-particle density matrix: the reference's CI-density (CIDEN) path.
+ *   block               generateSOCIblocksForCIDEN (PsociHamiltonian.C:572-705) and
+ *                       generateSEFCIGCIDEN (:1123-1269), transformed by ciout (CDC^T)
+ *   contraction         transformSEFSEFtoMOGET (PsociGAhamiltonian.C:10027-10099)
+ *   pair loop           constructCIdensityAltOrbMapChunkJmap (:11570-11760): pairs j <= i
+ *                       with |nopen_i - nopen_j| <= 2 and at most one electron moved
+ *                       (compareOrbMapCIDEN, PsociGADeterminants.C:2219-2240)
+ *   packed index        twoDindex (PsociGAhamiltonian.C:10297-10302): lower triangle
+ * Output per root: nbf(nbf+1)/2 values.  The diagonal holds sum_I occ_p(I) c_I.c_I (times
+ * the transformed identity); an off-diagonal (p, q) holds sum over pairs j < i of the
+ * c_i S c_j contraction for the single excitation p <-> q, once per unordered pair, as the
+ * reference accumulates it.
+ * ------------------------------------------------------------------------- */
+static int ciden_block(const orc_ctx *c, int I, int J, double *out, double *dd, double *scratch, int *ie,
+                       int *je) {
+  const orc_cfg *gi = &c->cfg[I], *gj = &c->cfg[J];
+  int nsi = gi->nsef, nsj = gj->nsef;
+  memset(out, 0, sizeof(double) * nsi * nsj);
+  memset(dd, 0, sizeof(double) * gi->ndet * gj->ndet);
+  if (abs(gi->nopen - gj->nopen) > 2) return 0;
+  if (gi->jsym != gj->jsym) return 0;
+  int iex = -1, jex = -1;
+  if (I != J) {
+    const unsigned char *io = c->occ + (size_t)I * c->nbf, *jo = c->occ + (size_t)J * c->nbf;
+    int ni = 0, nj = 0;
+    for (int p = 0; p < c->nbf; ++p) {
+      int d = (int)io[p] - (int)jo[p];
+      if (d < 0) { if (nj - d > 1) return 0; nj -= d; jex = p; }
+      else if (d > 0) { if (ni + d > 1) return 0; ni += d; iex = p; }
+    }
+  }
+  *ie = iex; *je = jex;
+  int nbf = c->nbf;
+  unsigned char figa[256], figb[256];
+  for (int ii = 0; ii < gi->ndet; ++ii) {
+    const int *ri = REC(c, gi, ii);
+    const int *ai = AL(c, ri), *bi = BE(c, ri);
+    memset(figa, 0, nbf); memset(figb, 0, nbf);
+    for (int t = 0; t < NA(ri); ++t) figa[ai[t]] = 1;
+    for (int t = 0; t < NB(ri); ++t) figb[bi[t]] = 1;
+    for (int jj = 0; jj < gj->ndet; ++jj) {
+      const int *rj = REC(c, gj, jj);
+      if (MS(ri) != MS(rj)) continue;
+      const int *aj = AL(c, rj), *bj = BE(c, rj);
+      int nmarka = 0, nmarkb;
+      for (int t = 0; t < NA(rj); ++t) if (!figa[aj[t]]) { if (++nmarka > 1) break; }
+      nmarkb = nmarka;
+      for (int t = 0; t < NB(rj); ++t) if (!figb[bj[t]]) { if (++nmarkb > 1) break; }
+      double v;
+      if (nmarka > 1 || nmarkb > 1) v = 0.0;
+      else if (nmarkb == 0) v = 1.0;
+      else {
+        int ncount = PH(ri) + PH(rj);
+        if (abs(iex - jex) > 1) {
+          int kbs = (iex > jex ? iex : jex) - 1, ka = iex + jex - kbs;
+          const int *lst = (nmarka != 0) ? ai : bi;
+          int nl = (nmarka != 0) ? NA(ri) : NB(ri);
+          for (int t = 0; t < nl; ++t) { if (lst[t] > kbs) break; if (lst[t] >= ka) ++ncount; }
+        }
+        v = (ncount % 2 == 1) ? -1.0 : 1.0;
+      }
+      dd[(size_t)ii * gj->ndet + jj] = v;
+    }
+  }
+  cdct(c, gi, gj, dd, out, scratch);
+  return 1;
+}
+
+int orc_ciden_block(const orc_ctx *c, int i, int j, double *out) {
+  double *dd = (double *)malloc(sizeof(double) * ORC_MAXDET * ORC_MAXDET);
+  double *sc = (double *)malloc(sizeof(double) * ORC_MAXDET * ORC_MAXDET);
+  int ie, je;
+  int st = ciden_block(c, i, j, out, dd, sc, &ie, &je);
+  free(dd); free(sc);
+  return st;
+}
+
+void orc_density1(const orc_ctx *c, int k, const double *vecs, double *dens) {
+  const long N = c->sefoff[c->nconf];
+  const long ntri = (long)c->nbf * (c->nbf + 1) / 2;
+  memset(dens, 0, sizeof(double) * k * ntri);
+  double *dd = (double *)malloc(sizeof(double) * ORC_MAXDET * ORC_MAXDET);
+  double *sc = (double *)malloc(sizeof(double) * ORC_MAXDET * ORC_MAXDET);
+  double *ss = (double *)malloc(sizeof(double) * ORC_MAXDET * ORC_MAXDET);
+  for (int q = 0; q < k; ++q) {
+    const double *v = vecs + (size_t)q * N;
+    double *D = dens + (size_t)q * ntri;
+    for (int I = 0; I < c->nconf; ++I) {
+      const orc_cfg *gi = &c->cfg[I];
+      const unsigned char *io = c->occ + (size_t)I * c->nbf;
+      for (int J = 0; J <= I; ++J) {
+        const orc_cfg *gj = &c->cfg[J];
+        int ie, je;
+        if (!ciden_block(c, I, J, ss, dd, sc, &ie, &je)) continue;
+        const double *vi = v + c->sefoff[I], *vj = v + c->sefoff[J];
+        int nsi = gi->nsef, nsj = gj->nsef;
+        if (I == J) {
+          /* occupied orbitals: doubly occupied first, then singly occupied, ascending */
+          for (int pass = 2; pass >= 1; --pass)
+            for (int p = 0; p < c->nbf; ++p) {
+              if (io[p] != pass) continue;
+              double value = 0.0;
+              for (int a = 0; a < nsi; ++a) {
+                double temp = vj[a];
+                for (int b = 0; b < nsj; ++b) value += ss[(size_t)a * nsj + b] * temp * vj[b] * pass;
+              }
+              D[tri(p, p)] += value;
+            }
+        } else {
+          double value = 0.0;
+          for (int a = 0; a < nsi; ++a) {
+            double temp = vi[a];
+            for (int b = 0; b < nsj; ++b) value += ss[(size_t)a * nsj + b] * temp * vj[b];
+          }
+          D[tri(ie, je)] += value;
+        }
+      }
+    }
+  }
+  free(dd); free(sc); free(ss);
+}

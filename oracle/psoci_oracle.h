@@ -29,6 +29,10 @@ long orc_build_rows(orc_ctx *c, int nthreads, const int *rows, int nrows);
 void orc_diag(const orc_ctx *c, double *diag);
 void orc_sigma_lower(long n, const long *rowptr, const int *cols, const double *vals, int k,
                      const double *x, double *y, int nthreads);
+/* 1-particle density (CIDEN): block of pair (i, j) and the packed densities of k roots
+ * (vecs: k x N root-major; dens: k x nbf(nbf+1)/2). */
+int orc_ciden_block(const orc_ctx *c, int i, int j, double *out);
+void orc_density1(const orc_ctx *c, int k, const double *vecs, double *dens);
 
 #ifdef __cplusplus
 }

@@ -329,4 +329,76 @@ int ref_vec_read(const char *path, int binary, long nbasis, int maxroots, double
   return n;
 }
 
+/* CI-density block of configurations (i, j), 0-based, via the reference's own
+ * generateSOCIblocksForCIDEN (PsociHamiltonian.C:572-705).  Returns its status. */
+int ref_ciden_block(int i, int j, double *out) {
+  PsociHamiltonian H(s_nbf, s_nelec);
+  H.specifyIntegrals(s_ints);
+  H.setKsym(s_ksym);
+  H.setPerSpatialValues(s_maxdet, s_maxsef);
+  vector<double> sefsef;
+  int st = H.generateSOCIblocksForCIDEN(s_J[i], s_J[j], sefsef);
+  for (size_t t = 0; t < sefsef.size(); ++t) out[t] = sefsef[t];
+  return st;
+}
+
+/* Packed 1-particle densities of k roots (vecs: k x N root-major) from the reference's block
+ * function, with the contraction of transformSEFSEFtoMOGET (PsociGAhamiltonian.C:10027-10099)
+ * and the pair order j <= i of constructCIdensityAltOrbMapChunkJmap (:11570-11760) restated
+ * here (they need Global Arrays).  occ is the array given to ref_set_configs. */
+void ref_density1(const unsigned char *occ, int k, const double *vecs, double *dens) {
+  const int nconf = (int)s_J.size();
+  const long N = s_sefoff.back();
+  const long ntri = (long)s_nbf * (s_nbf + 1) / 2;
+  memset(dens, 0, sizeof(double) * k * ntri);
+  PsociHamiltonian H(s_nbf, s_nelec);
+  H.specifyIntegrals(s_ints);
+  H.setKsym(s_ksym);
+  H.setPerSpatialValues(s_maxdet, s_maxsef);
+  vector<double> sefsef;
+  auto two_d = [](int m, int n) { int a = max(m, n) + 1, b = min(m, n) + 1; return a * (a - 1) / 2 + b - 1; };
+  for (int q = 0; q < k; ++q) {
+    const double *v = vecs + (size_t)q * N;
+    double *D = dens + (size_t)q * ntri;
+    for (int i = 0; i < nconf; ++i) {
+      const unsigned char *oi = occ + (size_t)i * s_nbf;
+      for (int j = 0; j <= i; ++j) {
+        const unsigned char *oj = occ + (size_t)j * s_nbf;
+        /* compareOrbMapCIDEN + the open-shell difference test of the pair list */
+        int ni = 0, nj = 0, ie = -1, je = -1;
+        bool ok = abs(s_J[i].num_singly - s_J[j].num_singly) <= 2;
+        for (int p = 0; p < s_nbf && ok; ++p) {
+          int d = (int)oi[p] - (int)oj[p];
+          if (d < 0) { nj -= d; je = p; if (nj > 1) ok = false; }
+          else if (d > 0) { ni += d; ie = p; if (ni > 1) ok = false; }
+        }
+        if (!ok) continue;
+        if (!H.generateSOCIblocksForCIDEN(s_J[i], s_J[j], sefsef)) continue;
+        int nsi = s_J[i].nsefi, nsj = s_J[j].nsefi;
+        const double *vi = v + s_sefoff[i], *vj = v + s_sefoff[j];
+        if (i == j) {
+          vector<pair<int, int>> mo;
+          for (int t = 0; t < s_J[i].num_doubly; ++t) mo.push_back({s_J[i].doubly[t], 2});
+          for (int t = 0; t < s_J[i].num_singly; ++t) mo.push_back({s_J[i].singly[t], 1});
+          for (auto &po : mo) {
+            double value = 0.0;
+            for (int a = 0; a < nsi; ++a) {
+              double temp = vj[a];
+              for (int b = 0; b < nsj; ++b) value += sefsef[(size_t)a * nsj + b] * temp * vj[b] * po.second;
+            }
+            D[two_d(po.first, po.first)] += value;
+          }
+        } else {
+          double value = 0.0;
+          for (int a = 0; a < nsi; ++a) {
+            double temp = vi[a];
+            for (int b = 0; b < nsj; ++b) value += sefsef[(size_t)a * nsj + b] * temp * vj[b];
+          }
+          D[two_d(ie, je)] += value;
+        }
+      }
+    }
+  }
+}
+
 }  /* extern "C" */

@@ -8,7 +8,9 @@ shim) on small seeded synthetic problems and stores, per problem:
 * per-configuration ndet / nsef / nopen and the full determinant table
   (nalpha, nbeta, spin projection, phase, sums, sorted alpha / beta lists);
 * the lower-triangle Hamiltonian in CSR as packSefsef keeps it;
-* the lowest eigenvalues of the assembled symmetric matrix (dense LAPACK).
+* the lowest eigenvalues of the assembled symmetric matrix (dense LAPACK);
+* two seeded unit vectors and their packed 1-particle densities from the reference's
+  CIDEN element path (generateSOCIblocksForCIDEN + transformSEFSEFtoMOGET).
 
 Needs the reference tree (only in the build container).  Usage:
     python tests/golden/make_golden.py
@@ -51,15 +53,18 @@ def main():
             counts = R.config_counts()
             dets = np.concatenate([R.config_dets(i) for i in range(p.nconf)], 0)
             rp, ci, va = R.build_lower(4)
+            n = int(counts[:, 1].sum())
+            dvec = np.random.default_rng(7).standard_normal((2, n))
+            dvec /= np.linalg.norm(dvec, axis=1, keepdims=True)
+            dens = R.density1(dvec)
         finally:
             os.dup2(saved, 1)
-        n = int(counts[:, 1].sum())
         F = lower_to_full(rp, ci, va, n)
         nev = min(8, n)
         ev = sla.eigvalsh(F.toarray())[:nev]
         np.savez_compressed(os.path.join(HERE, f"{name}.npz"), nbf=p.nbf, nelec=p.nelec, ksym=p.ksym,
                             mx_open=p.mx_open, jsym=p.jsym, occ=p.occ, h=p.h, so=p.so, eri=p.eri, counts=counts,
-                            dets=dets.astype(np.int16), rowptr=rp, cols=ci, vals=va, evals=ev)
+                            dets=dets.astype(np.int16), rowptr=rp, cols=ci, vals=va, evals=ev, dvec=dvec, dens=dens)
         print(f"{name}: nconf={p.nconf} N={n} nnz_lower={len(ci)} ev0={ev[0]:.10f}")
 
 

@@ -53,3 +53,13 @@ def test_fixture_covers_all_template_classes():
         for no in np.unique(z["counts"][:, 2]):
             seen.add((int(z["nelec"]) % 2, int(no)))
     assert {(1, 11), (0, 10), (0, 6), (1, 5), (0, 0)} <= seen
+
+
+@pytest.mark.parametrize("path", GOLD, ids=[os.path.basename(g)[:-4] for g in GOLD])
+def test_density1_matches_golden(oracle_mod, path):
+    """The CIDEN 1-particle density of two seeded unit vectors, bit for bit."""
+    p, z = load(path)
+    d = oracle_mod.Oracle(p).density1(z["dvec"])
+    assert np.array_equal(d, z["dens"]), np.abs(d - z["dens"]).max()
+    tr = d[:, [k * (k + 1) // 2 + k for k in range(p.nbf)]].sum(1)
+    assert np.abs(tr - p.nelec).max() < 1e-12

@@ -88,3 +88,44 @@ def test_blocks_status(both):
         so, bo = O.block(i, j)
         assert sr == so
         assert np.array_equal(br, bo)
+
+
+@pytest.mark.parametrize("name,ksym", [("fci_4e6o", 2), ("fci_5e6o", 1), ("fci_6e8o", 3)])
+def test_ciden_blocks_bit_exact(both, name, ksym):
+    """generateSOCIblocksForCIDEN: status and +-1/0 SEF blocks for every pair within one move."""
+    p = small_problem(name, ksym, seed=6)
+    with _Quiet():
+        R = both.Reference(p)
+    O = both.Oracle(p)
+    occ = p.occ.astype(int)
+    connected = 0
+    for i in range(p.nconf):
+        moved = np.abs(occ[:i + 1] - occ[i]).sum(1)
+        for j in np.nonzero(moved <= 2)[0]:
+            sr, br = R.ciden_block(i, int(j))
+            so, bo = O.ciden_block(i, int(j))
+            assert sr == so, (i, j)
+            assert np.array_equal(br, bo), (i, j)
+            connected += sr != 0
+    assert connected > p.nconf
+
+
+def test_density1_bit_exact(both):
+    """Packed spin-free 1-particle densities, FCI and MRCISD, even and odd electron counts."""
+    from psoci_gb300.inputs import make_problem
+
+    probs = [small_problem("fci_6e8o", 1, seed=2), small_problem("fci_5e6o", 2, seed=2),
+             make_problem("mrcisd", seed=11, ksym=1, nact=6, nelec=4, nvirt=8),
+             high_open_problem(nbf=12, seed=3, nelec=9, ksym=1, per=2)]
+    rng = np.random.default_rng(5)
+    for p in probs:
+        with _Quiet():
+            R = both.Reference(p)
+        O = both.Oracle(p)
+        v = rng.standard_normal((3, O.num_sefs()))
+        v /= np.linalg.norm(v, axis=1, keepdims=True)
+        dr = R.density1(v)
+        do = O.density1(v)
+        assert np.array_equal(dr, do)
+        tr = do[:, [k * (k + 1) // 2 + k for k in range(p.nbf)]].sum(1)
+        assert np.abs(tr - p.nelec).max() < 1e-12
