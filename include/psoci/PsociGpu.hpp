@@ -8,6 +8,7 @@
 // unavoidable change is that Global Arrays handles become a psoci::Device (one GPU, one
 // stream) owning the device arrays.  Errors throw psoci::Error carrying the C status.
 #pragma once
+#include <algorithm>
 #include <cstdint>
 #include <cstdio>
 #include <fstream>
@@ -202,6 +203,17 @@ class PsociGAhamiltonian {
     return nnz_;
   }
   int64_t numberNonzeroElements() const { return nnz_; }
+  // constructCIdensityAltOrbMapChunkJmap (PsociGAhamiltonian.C:11570-11760): density[root] is
+  // the packed nbf(nbf+1)/2 spin-free 1-particle density of root-major vectors vecs (k x N)
+  int64_t constructCIdensityAltOrbMapChunkJmap(int numRoots, const std::vector<double> &vecs, int nbf,
+                                               std::vector<std::vector<double> > &density) {
+    const size_t ntri = (size_t)nbf * (nbf + 1) / 2;
+    std::vector<double> flat((size_t)numRoots * ntri);
+    check(dev_.get(), psoci_density1(dev_.get(), numRoots, vecs.data(), flat.data()), "psoci_density1");
+    density.assign(numRoots, std::vector<double>());
+    for (int r = 0; r < numRoots; ++r) density[r].assign(flat.begin() + r * ntri, flat.begin() + (r + 1) * ntri);
+    return (int64_t)numRoots * (int64_t)ntri;
+  }
   // fetchDIAG_SEF (PsociGAhamiltonian.C:9014)
   void fetchDIAG_SEF(std::vector<double> &diag, int64_t nsef) {
     diag.resize(nsef);
@@ -260,6 +272,38 @@ class PsociGAsubspace {
 
  private:
   Device &dev_;
+};
+
+// PsociNOpopulations (PsociNOpopulations.hpp): natural orbitals of the CI densities in the MO
+// basis.  The AO transformation, Mulliken analysis and NO files need the MO coefficient file
+// and stay with the caller.
+class PsociNOpopulations {
+ public:
+  struct Root {
+    std::vector<double> occupations;  // per block, largest first; blocks in ascending label order
+    std::vector<double> vectors;      // per block n_b x n_b, natural orbital i contiguous
+    std::vector<int32_t> orbitals;    // the orbitals of the blocks, in output order
+  };
+  // constructNaturalOrbitals (PsociNOpopulations.C:569-669), MO-basis part, one root
+  static Root constructNaturalOrbitals(int nbf, const std::vector<double> &density, const std::vector<int32_t> &orbSym) {
+    Root r;
+    r.occupations.resize(nbf);
+    r.orbitals.resize(nbf);
+    size_t nvec = 0;
+    std::vector<int32_t> labels(orbSym);
+    std::sort(labels.begin(), labels.end());
+    for (size_t i = 0; i < labels.size();) {
+      size_t j = i;
+      while (j < labels.size() && labels[j] == labels[i]) ++j;
+      nvec += (j - i) * (j - i);
+      i = j;
+    }
+    r.vectors.resize(nvec);
+    check(nullptr, psoci_natural_orbitals(nbf, density.data(), orbSym.data(), r.occupations.data(), r.vectors.data(),
+                                          r.orbitals.data()),
+          "psoci_natural_orbitals");
+    return r;
+  }
 };
 
 // PsociVector (PsociVector.hpp): CI vector files in the reference's scalable layout.

@@ -198,6 +198,29 @@ PSOCI_API psoci_status psoci_davidson(psoci_ctx *ctx, const psoci_dav_opts *opts
  * k = 0 clears the guess. */
 PSOCI_API psoci_status psoci_set_guess(psoci_ctx *ctx, int k, const double *vecs);
 
+/* Spin-free 1-particle density of k CI vectors (the reference's CI-density path,
+ * PsociGAhamiltonian::constructCIdensityAltOrbMapChunkJmap, PsociGAhamiltonian.C:11570-11760,
+ * with blocks from PsociHamiltonian::generateSOCIblocksForCIDEN, PsociHamiltonian.C:572-705,
+ * contracted as transformSEFSEFtoMOGET, PsociGAhamiltonian.C:10027-10099).  vecs: k vectors
+ * of length N, root-major (as psoci_davidson returns them).  dens: k x nbf(nbf+1)/2 doubles,
+ * root-major, packed lower triangle D[p(p+1)/2 + q], p >= q (twoDindex).  The diagonal holds
+ * the orbital occupations; an off-diagonal element holds the sum over unordered configuration
+ * pairs one electron apart (same jsym) of c_I S_IJ c_J, once per pair, as the reference
+ * accumulates it.  Needs psoci_build_determinants; the Hamiltonian is not used. */
+PSOCI_API psoci_status psoci_density1(psoci_ctx *ctx, int k, const double *vecs, double *dens);
+
+/* Natural orbitals and occupations of one packed 1-particle density (the MO-basis part of
+ * PsociNOpopulations::constructNaturalOrbitals, PsociNOpopulations.C:569-669: per symmetry
+ * block diagonalizeNOinMObasis :456-497 with a unit metric, then sortNOinMObasis :269-344,
+ * largest occupation first).  orb_sym[nbf]: a symmetry label per orbital; a block holds the
+ * orbitals of one label in ascending order, blocks in ascending label order (the reference's
+ * nstart/nsize split when MOs are ordered by symmetry).  Outputs, blocks concatenated:
+ * occ[nbf] occupations; vecs[sum of n_b^2] per block n_b x n_b, natural orbital i's
+ * coefficients over the block's orbitals contiguous; orb_order[nbf] (may be NULL) the
+ * orbitals of the blocks in output order.  Host computation; needs no context or device. */
+PSOCI_API psoci_status psoci_natural_orbitals(int nbf, const double *dens, const int32_t *orb_sym, double *occ,
+                                              double *vecs, int32_t *orb_order);
+
 /* CI vector files in the reference's PsociVector "scalable" layout (PsociVector.C:530-706,
  * written by PsociGAvectors::dumpVectorScalable, PsociGAvectors.C:207-326).  binary = 0:
  * ASCII (header "nbasis nroots" / "width prec", per root its 1-based number then nbasis

@@ -1,11 +1,13 @@
 """Solve one double-group symmetry block of a named synthetic workload on one GPU.
 
   python -m psoci_gb300 --workload mrcisd_6e8o_v24 [--roots 8] [--rtol 1e-5] [--fp64]
-                        [--no-davidson] [--sigma K] [--verbose 1]
+                        [--no-davidson] [--sigma K] [--density] [--verbose 1]
 
 Determinants -> Hamiltonian (CSR) -> block Davidson; prints the sizes and the total
 energies in the layout of the reference driver's "Eigenvalue" lines.  ``--sigma K`` also
-applies H to K random vectors once (the Davidson's inner product, on its own).
+applies H to K random vectors once (the Davidson's inner product, on its own);
+``--density`` forms the 1-particle densities of the converged roots and prints the
+natural-orbital occupations of the first root (diagonal blocks of one orbital label).
 """
 from __future__ import annotations
 
@@ -28,6 +30,7 @@ def main(argv=None):
     ap.add_argument("--fp64", action="store_true", help="FP64 elements in sigma (default: FP32 copy)")
     ap.add_argument("--no-davidson", action="store_true")
     ap.add_argument("--sigma", type=int, default=0, help="apply H to this many random vectors once")
+    ap.add_argument("--density", action="store_true", help="1-particle densities of the roots")
     ap.add_argument("--max-subspace", type=int, default=48)
     ap.add_argument("--device", type=int, default=0)
     ap.add_argument("--verbose", type=int, default=0)
@@ -51,11 +54,23 @@ def main(argv=None):
             Y = c.sigma(X, prec=api.PREC_MIXED if mixed else api.PREC_FP64)
             print(f"sigma on {a.sigma} vectors: |HX|_max {np.abs(Y).max():.6e}")
         if not a.no_davidson:
-            r = c.davidson(a.roots, rtol=a.rtol, mixed=mixed, refine=True, max_subspace=a.max_subspace)
+            r = c.davidson(a.roots, rtol=a.rtol, mixed=mixed, refine=True, max_subspace=a.max_subspace,
+                           want_vectors=a.density)
             ecore = c.core_energy()
             for i, e in enumerate(r.evals):
                 print(f"Eigenvalue {i + 1:4d} Total energy (au) {e + ecore:20.12f} Electronic (au) {e:20.12f}")
             print(f"iterations {r.iterations}, sigma vectors {r.sigma_calls}, {r.seconds:.3f} s")
+            if a.density:
+                for rep in range(2):  # the first call also forms the configuration groups
+                    t0 = time.perf_counter()
+                    d = c.density1(r.evecs)
+                    td = time.perf_counter() - t0
+                    print(f"density1 of {len(r.evals)} roots ({'with' if rep == 0 else 'groups kept'}): "
+                          f"{td * 1e3:.2f} ms")
+                occ, _ = api.natural_orbitals(d[0], p.irreps)
+                tr = d[:, [q * (q + 1) // 2 + q for q in range(p.nbf)]].sum(1)
+                print(f"traces {np.array2string(tr, precision=10)}; largest NO occupations, root 1: "
+                      + " ".join(f"{x:.6f}" for x in np.sort(occ)[::-1][:8]))
 
 
 if __name__ == "__main__":

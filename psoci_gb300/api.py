@@ -91,6 +91,8 @@ SIGNATURES = {
     "psoci_sigma_mixed_noalloc": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
                                                  ctypes.c_int]),
     "psoci_set_guess": (ctypes.c_int, [_P, ctypes.c_int, _DP]),
+    "psoci_density1": (ctypes.c_int, [_P, ctypes.c_int, _DP, _DP]),
+    "psoci_natural_orbitals": (ctypes.c_int, [ctypes.c_int, _DP, _I32P, _DP, _DP, _I32P]),
     "psoci_write_vectors": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int, ctypes.c_int64, ctypes.c_int, _DP,
                                            ctypes.c_char_p]),
     "psoci_read_vectors": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int, ctypes.c_int64, ctypes.c_int, _DP, _IP]),
@@ -149,6 +151,7 @@ class Context:
             raise PsociError(st, "psoci_create failed (no CUDA device?)")
         self.nsef = 0
         self.nnz = 0
+        self.nbf = 0
 
     def close(self):
         if getattr(self, "ctx", None):
@@ -184,6 +187,7 @@ class Context:
         oc = np.ascontiguousarray(occ, np.uint8)
         self._check(self.lib.psoci_set_configs(self.ctx, nbf, nelec, ksym, mx_open, len(js), _ptr(js, _I32P),
                                                _ptr(oc, _U8P)), "set_configs")
+        self.nbf = nbf
 
     def load_problem(self, p):
         """Integrals and configurations of an inputs.Problem."""
@@ -279,6 +283,16 @@ class Context:
         return DavidsonResult(ev, vec, rn, stats.iterations, stats.sigma_calls, stats.collapses, stats.refine_iters,
                               stats.seconds, stats.sigma_seconds)
 
+    def density1(self, vecs) -> np.ndarray:
+        """Spin-free 1-particle densities of CI vectors [k, N] (root-major): array
+        [k, nbf(nbf+1)/2], packed lower triangle (index p(p+1)/2 + q, p >= q)."""
+        v = np.ascontiguousarray(np.atleast_2d(vecs), np.float64)
+        if v.shape[1] != self.nsef:
+            raise ValueError(f"density1: vectors of length {v.shape[1]}, expected {self.nsef}")
+        out = np.zeros((v.shape[0], self.nbf * (self.nbf + 1) // 2))
+        self._check(self.lib.psoci_density1(self.ctx, v.shape[0], _ptr(v, _DP), _ptr(out, _DP)), "density1")
+        return out
+
     def core_energy(self) -> float:
         return self.lib.psoci_core_energy(self.ctx)
 
@@ -315,6 +329,37 @@ class Context:
     def launch_count(self) -> int:
         """Kernels the library has launched in this process so far (all contexts)."""
         return int(self.lib.psoci_launch_count())
+
+
+def natural_orbitals(dens_packed, orb_sym):
+    """Natural orbitals of one packed density [nbf(nbf+1)/2] per symmetry block.
+
+    Returns (occupations [nbf], blocks): blocks is a list, in ascending label order, of
+    dicts {"sym", "orbitals", "occupations", "vectors"}; vectors[i] holds natural orbital i
+    over the block's orbitals, occupations largest first."""
+    lib = load_library()
+    d = np.ascontiguousarray(dens_packed, np.float64).ravel()
+    sym = np.ascontiguousarray(orb_sym, np.int32).ravel()
+    nbf = len(sym)
+    if len(d) != nbf * (nbf + 1) // 2:
+        raise ValueError(f"natural_orbitals: density of length {len(d)} for {nbf} orbitals")
+    _, counts = np.unique(sym, return_counts=True)
+    occ = np.zeros(nbf)
+    vecs = np.zeros(int((counts.astype(np.int64) ** 2).sum()))
+    order = np.zeros(nbf, np.int32)
+    st = lib.psoci_natural_orbitals(nbf, _ptr(d, _DP), _ptr(sym, _I32P), _ptr(occ, _DP), _ptr(vecs, _DP),
+                                    _ptr(order, _I32P))
+    if st != PSOCI_OK:
+        raise PsociError(st, "natural_orbitals")
+    blocks, e, v = [], 0, 0
+    for n in counts:
+        n = int(n)
+        orbs = order[e:e + n].copy()
+        blocks.append(dict(sym=int(sym[orbs[0]]), orbitals=orbs, occupations=occ[e:e + n].copy(),
+                           vectors=vecs[v:v + n * n].reshape(n, n).copy()))
+        e += n
+        v += n * n
+    return occ, blocks
 
 
 def write_vectors(path: str, vecs: np.ndarray, binary: bool = False, title: str = ""):

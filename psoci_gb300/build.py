@@ -17,7 +17,8 @@ CSRC = os.path.join(HERE, "csrc")
 LIBDIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(LIBDIR, "libpsoci_gpu.so")
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
-SOURCES = ["util.cu", "dets.cu", "hbuild.cu", "sigma.cu", "davidson.cu", "capi.cu", "io.cu", "noalloc.cu"]
+SOURCES = ["util.cu", "dets.cu", "hbuild.cu", "sigma.cu", "davidson.cu", "capi.cu", "io.cu", "noalloc.cu", "density.cu",
+           "natorb.cpp"]
 PER_FILE = {"hbuild.cu": ["--fmad=false"]}
 
 
@@ -29,7 +30,7 @@ def nvcc() -> str:
 
 
 def _compile(src: str, extra: list[str]) -> str:
-    obj = os.path.join(LIBDIR, src.replace(".cu", ".o"))
+    obj = os.path.join(LIBDIR, os.path.splitext(src)[0] + ".o")
     cmd = [nvcc(), ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden",
            "-I" + CSRC, "-c", os.path.join(CSRC, src), "-o", obj] + PER_FILE.get(src, []) + extra
     r = subprocess.run(cmd, capture_output=True, text=True)

@@ -17,6 +17,7 @@ void release_all(psoci_ctx *c) {
   psoci_h_release(c);
   psoci_dets_release(c);
   psoci_join_release(c);
+  psoci_density_release(c);
   psoci_free(c->d_one);
   psoci_free(c->d_eri);
   psoci_free(c->d_e1);
@@ -153,6 +154,7 @@ psoci_status psoci_set_configs(psoci_ctx *c, int nbf, int nelec, int ksym, int m
   if ((s = set_device(c))) return s;
   psoci_h_release(c);
   psoci_dets_release(c);
+  psoci_density_release(c);
   if ((s = psoci_alloc(c, &c->d_e1, e1.size())) || (s = psoci_alloc(c, &c->d_e2, e2.size())) ||
       (s = psoci_alloc(c, &c->d_jsym, nconf)) || (s = psoci_alloc(c, &c->d_nopen, nconf)))
     return s;

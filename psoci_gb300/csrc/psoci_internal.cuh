@@ -85,6 +85,14 @@ struct psoci_ctx {
   psoci_build_info binfo{};
   int64_t slab_hint = 0;  // value-slab slots the last build of this space used
 
+  // 1-particle density: configuration groups sharing a hole key (density.cu)
+  bool den_ready = false;
+  int64_t den_ng = 0, den_npairs = 0;
+  int64_t *den_geoff = nullptr;  // [ng+1] first member of each group
+  int64_t *den_gpoff = nullptr;  // [ng+1] first candidate pair of each group
+  int32_t *den_gcfg = nullptr;   // members: configuration
+  uint8_t *den_gorb = nullptr;   // members: orbital the key removed
+
   // initial guess for the next Davidson run (root-major, guess_k x nsef)
   std::vector<double> guess;
   int guess_k = 0;
@@ -141,6 +149,8 @@ psoci_status psoci_join_prepare(psoci_ctx *c);  // after h_occ is set
 void psoci_join_release(psoci_ctx *c);
 void psoci_h_release(psoci_ctx *c);
 void psoci_dets_release(psoci_ctx *c);
+void psoci_density_release(psoci_ctx *c);
+psoci_status psoci_density1_device(psoci_ctx *c, int k, const double *dV, int64_t ldv, double *dD);
 
 // ------------------------------------------------------------------------------------
 // device helpers

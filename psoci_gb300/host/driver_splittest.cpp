@@ -13,6 +13,9 @@
 //   -p 0|1  sigma precision (0 FP64, 1 mixed FP32/FP64 with FP64 refinement; default 1)
 //   -b 0|1  block Davidson (default 1) or one vector per iteration as the reference
 //   -d N    CUDA device
+//   -N      natural-orbital occupations of each root from its 1-particle density (the
+//           reference's PsociNOpopulations step, driver.PSOCI.splittest.C:1420-1450; the
+//           integral file carries no orbital symmetries, so all orbitals form one block)
 // Output lines keep the reference's format (driver.PSOCI.splittest.C:1373):
 //   "Eigenvalue i Total energy (au) E+core Electronic (au) E rnorm r"
 #include <getopt.h>
@@ -31,9 +34,9 @@ int main(int argc, char **argv) {
   std::string cfg = "configs", moints = "moints", vecfile = "psoci_vectors.txt", hfile = "psoci_hamiltonian.bin";
   int nroots = 1, maxmult = 4, maxiter = 1000, prec = 1, block = 1, device = 0, verbose = 0;
   double rtol = 1e-6;
-  bool restart = false, hread = false, hwrite = false;
+  bool restart = false, hread = false, hwrite = false, natorb = false;
   int c;
-  while ((c = getopt(argc, argv, "c:m:n:F:x:I:v:rHWk:p:b:d:V")) != -1) {
+  while ((c = getopt(argc, argv, "c:m:n:F:x:I:v:rHWk:p:b:d:VN")) != -1) {
     switch (c) {
       case 'c': cfg = optarg; break;
       case 'm': moints = optarg; break;
@@ -50,6 +53,7 @@ int main(int argc, char **argv) {
       case 'b': block = atoi(optarg); break;
       case 'd': device = atoi(optarg); break;
       case 'V': verbose = 1; break;
+      case 'N': natorb = true; break;
       default:
         std::cerr << "usage: psoci_driver -c configs -m ints [-n roots] [-F rtol] [-p 0|1] ..." << std::endl;
         return 2;
@@ -107,6 +111,18 @@ int main(int argc, char **argv) {
       std::cout << "Eigenvalue " << i << " Total energy (au) " << std::setprecision(6) << r.evals[i] + fcore
                 << " Electronic (au) " << std::setprecision(15) << r.evals[i] << " rnorm " << std::setprecision(10)
                 << r.rnorms[i] << std::endl;
+    if (natorb) {
+      const int nbf = ints.nbf();
+      std::vector<std::vector<double> > density;
+      ham.constructCIdensityAltOrbMapChunkJmap(nroots, r.evecs, nbf, density);
+      std::vector<int32_t> oneBlock(nbf, 1);
+      for (int i = 0; i < nroots; ++i) {
+        psoci::PsociNOpopulations::Root no = psoci::PsociNOpopulations::constructNaturalOrbitals(nbf, density[i], oneBlock);
+        std::cout << "NO occupations root " << i << std::setprecision(8);
+        for (int k = 0; k < nbf && k < 10; ++k) std::cout << " " << no.occupations[k];
+        std::cout << std::endl;
+      }
+    }
     std::cout << "Total time (s) " << total << std::endl;
   } catch (const psoci::Error &e) {
     std::cerr << "psoci_driver: " << e.what() << std::endl;

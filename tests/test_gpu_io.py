@@ -40,6 +40,15 @@ def test_cpp_driver(tmp_path, oracle_mod):
     assert out2.returncode == 0, out2.stderr
     iters = int(re.search(r"Number of total iterations is (\d+)", out2.stdout).group(1))
     assert iters <= 3
+    # -N: natural-orbital occupations of each root, from its density through the C++ mirror
+    out3 = subprocess.run([build.DRIVER, "-c", cfg, "-m", ints, "-n", "2", "-F", "1e-8", "-p", "0", "-v", vec, "-N"],
+                          capture_output=True, text=True, timeout=300)
+    assert out3.returncode == 0, out3.stderr
+    rows = re.findall(r"NO occupations root (\d+) (.*)", out3.stdout)
+    assert [int(r[0]) for r in rows] == [0, 1]
+    for _, vals in rows:
+        occ = np.array([float(x) for x in vals.split()])
+        assert occ.max() <= 2.0 + 1e-9 and occ.min() >= -1e-9 and (np.diff(occ) <= 1e-12).all()
 
 
 def test_hamiltonian_checkpoint(tmp_path):
