@@ -208,6 +208,10 @@ PSOCI_API psoci_status psoci_set_guess(psoci_ctx *ctx, int k, const double *vecs
  * pairs one electron apart (same jsym) of c_I S_IJ c_J, once per pair, as the reference
  * accumulates it.  Needs psoci_build_determinants; the Hamiltonian is not used. */
 PSOCI_API psoci_status psoci_density1(psoci_ctx *ctx, int k, const double *vecs, double *dens);
+/* psoci_density1 on device memory: dV k vectors with stride ldv (root-major), dD k x
+ * nbf(nbf+1)/2 (overwritten); runs on the context's stream and returns without waiting.
+ * The first call after new configurations also forms the configuration groups. */
+PSOCI_API psoci_status psoci_density1_device(psoci_ctx *ctx, int k, const double *dV, int64_t ldv, double *dD);
 
 /* Natural orbitals and occupations of one packed 1-particle density (the MO-basis part of
  * PsociNOpopulations::constructNaturalOrbitals, PsociNOpopulations.C:569-669: per symmetry

@@ -92,6 +92,7 @@ SIGNATURES = {
                                                  ctypes.c_int]),
     "psoci_set_guess": (ctypes.c_int, [_P, ctypes.c_int, _DP]),
     "psoci_density1": (ctypes.c_int, [_P, ctypes.c_int, _DP, _DP]),
+    "psoci_density1_device": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p]),
     "psoci_natural_orbitals": (ctypes.c_int, [ctypes.c_int, _DP, _I32P, _DP, _DP, _I32P]),
     "psoci_write_vectors": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int, ctypes.c_int64, ctypes.c_int, _DP,
                                            ctypes.c_char_p]),
@@ -292,6 +293,12 @@ class Context:
         out = np.zeros((v.shape[0], self.nbf * (self.nbf + 1) // 2))
         self._check(self.lib.psoci_density1(self.ctx, v.shape[0], _ptr(v, _DP), _ptr(out, _DP)), "density1")
         return out
+
+    def density1_device(self, dV_ptr: int, ldv: int, dD_ptr: int, k: int):
+        """density1 on device pointers (root-major vectors, stride ldv); asynchronous on
+        the context's stream."""
+        self._check(self.lib.psoci_density1_device(self.ctx, k, ctypes.c_void_p(dV_ptr), ldv,
+                                                   ctypes.c_void_p(dD_ptr)), "density1_device")
 
     def core_energy(self) -> float:
         return self.lib.psoci_core_energy(self.ctx)

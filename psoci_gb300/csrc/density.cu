@@ -30,6 +30,7 @@
 // with the reference's sequential sums to rounding.
 #include <cstdio>
 
+#include "ffmath.cuh"
 #include "psoci_internal.cuh"
 
 namespace {
@@ -140,11 +141,17 @@ __global__ void k_group_compact(int64_t T, const int32_t *__restrict__ gcnt, con
   }
 }
 
-// group members in slot order: (configuration, orbital the key removed)
-__global__ void k_hole_scatter(int nconf, int W, const uint64_t *__restrict__ e1g, const int64_t *__restrict__ hoff,
-                               const int32_t *__restrict__ ent_slot, const int32_t *__restrict__ ent_rank,
-                               const int32_t *__restrict__ slot2g, const int64_t *__restrict__ geoff, int32_t *gcfg,
-                               uint8_t *gorb) {
+// group members in slot order: (configuration, orbital the key removed) and, where the
+// determinant and SEF totals fit 31 bits, a packed copy with the configuration's offsets,
+// {cfg, first determinant, first SEF, orbital | nopen << 8 | ndet << 16 | phase << 30},
+// and its open shells
+__global__ void k_hole_scatter(int nconf, int W, const uint64_t *__restrict__ e1g, const uint64_t *__restrict__ e2g,
+                               const int64_t *__restrict__ hoff, const int32_t *__restrict__ ent_slot,
+                               const int32_t *__restrict__ ent_rank, const int32_t *__restrict__ slot2g,
+                               const int64_t *__restrict__ geoff, int32_t *gcfg, uint8_t *gorb,
+                               const int64_t *__restrict__ detoff, const int64_t *__restrict__ sefoff,
+                               const int32_t *__restrict__ nopen, const uint8_t *__restrict__ phase, int4 *gmem,
+                               uint64_t *gopen) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nconf; i += (int64_t)gridDim.x * blockDim.x) {
     int64_t e = hoff[i];
     for (int w = 0; w < W; ++w) {
@@ -158,10 +165,40 @@ __global__ void k_hole_scatter(int nconf, int W, const uint64_t *__restrict__ e1
           const int64_t pos = geoff[g] + ent_rank[e];
           gcfg[pos] = (int32_t)i;
           gorb[pos] = (uint8_t)p;
+          if (gmem) {
+            gmem[pos] = make_int4((int)i, (int)detoff[i], (int)sefoff[i],
+                                  p | (nopen[i] << 8) | (int)((detoff[i + 1] - detoff[i]) << 16) |
+                                      ((int)(phase[detoff[i]] & 1) << 30));
+            for (int v = 0; v < W; ++v) gopen[pos * W + v] = e1g[i * W + v] & ~e2g[i * W + v];
+          }
         }
         ++e;
       }
     }
+  }
+}
+
+// 1 for a group whose members do not all share one exact key (a 64-bit hash collision):
+// its pairs are checked one by one
+template <int W>
+__global__ void k_group_verify(int64_t ng, const int64_t *__restrict__ geoff, const int32_t *__restrict__ gcfg,
+                               const uint8_t *__restrict__ gorb, const uint64_t *__restrict__ e1g,
+                               const uint64_t *__restrict__ e2g, const int32_t *__restrict__ jsym, uint8_t *gflag) {
+  for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < ng; g += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t e0 = geoff[g], e1 = geoff[g + 1];
+    const int c0 = gcfg[e0];
+    uint64_t k1[W], k2[W];
+    remove_one<W>(e1g + (int64_t)c0 * W, e2g + (int64_t)c0 * W, gorb[e0], k1, k2);
+    bool mixed = false;
+    for (int64_t e = e0 + 1; e < e1; ++e) {
+      const int ci = gcfg[e];
+      uint64_t a1[W], a2[W];
+      remove_one<W>(e1g + (int64_t)ci * W, e2g + (int64_t)ci * W, gorb[e], a1, a2);
+#pragma unroll
+      for (int w = 0; w < W; ++w) mixed = mixed || a1[w] != k1[w] || a2[w] != k2[w];
+      mixed = mixed || jsym[ci] != jsym[c0] || ci == c0;
+    }
+    gflag[g] = mixed;
   }
 }
 
@@ -179,6 +216,12 @@ struct DenParams {
   const int64_t *geoff, *gpoff;
   const int32_t *gcfg;
   const uint8_t *gorb;
+  const int4 *gmem;        // packed members (warp path)
+  const uint64_t *gopen;   // members: open shells of the configuration [W]
+  const uint8_t *gflag;    // per group: members' keys differ, check each pair
+  const float2 *vs;        // float-float roots of this pass, KBW per SEF (warp path)
+  const uint32_t *tmpl;    // determinant templates (amask | bmask << 12)
+  const int32_t *tmpl_off; // start of each (class, nopen) run
   double *dens;  // [kb][ntri] of this batch
 };
 
@@ -317,6 +360,233 @@ __global__ void __launch_bounds__(DEN_T) k_density_pairs(DenParams P) {
     if (acc[t] != 0.0) atomicAdd(P.dens + t, acc[t]);
 }
 
+constexpr int KBW = 4;        // roots per pass of the warp-per-pair kernel
+constexpr int INV_NOPEN = 7;  // warp path: at most 6 open shells (32 determinants)
+
+// float-float sum a + b (TwoSum on the high parts, low parts added)
+__device__ __forceinline__ float2 ff_add(float2 a, float2 b) {
+  const float s = __fadd_rn(a.x, b.x);
+  const float bb = __fsub_rn(s, a.x);
+  const float e = __fadd_rn(__fsub_rn(a.x, __fsub_rn(s, bb)), __fsub_rn(b.x, bb));
+  return make_float2(s, __fadd_rn(__fadd_rn(a.y, b.y), e));
+}
+__device__ __forceinline__ float2 shfl_xor_ff(float2 v, int m) {
+  return make_float2(__shfl_xor_sync(0xffffffffu, v.x, m), __shfl_xor_sync(0xffffffffu, v.y, m));
+}
+
+// Float-float sum of v[0..3] over the warp, scattered: afterwards lane l with (l & 7) == 0
+// holds the total of root (l >> 3) & 3.  Two halving exchanges (2 + 1 values) then three
+// butterfly steps.
+__device__ __forceinline__ float2 reduce_scatter4(const float2 (&v)[4], int lane) {
+  float2 w[2];
+  const bool b4 = lane & 16, b3 = lane & 8;
+#pragma unroll
+  for (int i = 0; i < 2; ++i) {
+    const float2 send = b4 ? v[i] : v[i + 2];
+    const float2 keep = b4 ? v[i + 2] : v[i];
+    w[i] = ff_add(keep, shfl_xor_ff(send, 16));
+  }
+  float2 z = ff_add(b3 ? w[1] : w[0], shfl_xor_ff(b3 ? w[0] : w[1], 8));
+  z = ff_add(z, shfl_xor_ff(z, 4));
+  z = ff_add(z, shfl_xor_ff(z, 2));
+  z = ff_add(z, shfl_xor_ff(z, 1));
+  return z;
+}
+
+// Inverse template table in shared memory: (class, nopen <= 6, alpha pattern over the open
+// shells in ascending order) -> index of that determinant in the configuration, or -1.
+// Within one template run the alpha pattern fixes the determinant (beta holds the other
+// open shells).
+__device__ __forceinline__ void build_inverse(const uint32_t *__restrict__ tmpl, const int32_t *__restrict__ tmpl_off,
+                                              int8_t *inv) {
+  for (int t = threadIdx.x; t < PSOCI_NCLS * INV_NOPEN * 64; t += blockDim.x) inv[t] = -1;
+  __syncthreads();
+  for (int t = threadIdx.x; t < PSOCI_NCLS * INV_NOPEN * 32; t += blockDim.x) {
+    const int cls = t / (INV_NOPEN * 32), no = (t / 32) % INV_NOPEN, d = t % 32;
+    const int r0 = tmpl_off[cls * PSOCI_NOPEN_SLOTS + no], r1 = tmpl_off[cls * PSOCI_NOPEN_SLOTS + no + 1];
+    if (d < r1 - r0) inv[(cls * INV_NOPEN + no) * 64 + (tmpl[r0 + d] & 63u)] = (int8_t)d;
+  }
+  __syncthreads();
+}
+
+// SEF of determinant d (ciout: odd electron counts one SEF per determinant; even, open
+// shells: SEF s = r2 (det 2s + m det 2s+1); closed shell: one of each)
+__device__ __forceinline__ int sef_of_det(int d, bool odd, int nopen) { return odd ? d : (nopen ? d >> 1 : 0); }
+
+// exact check of a pair from a group whose members' keys differ
+template <int W>
+__device__ __forceinline__ bool pair_exact(const DenParams &P, int I, int p, int J, int q) {
+  if (P.jsym[I] != P.jsym[J] || I == J) return false;
+  uint64_t a1[W], a2[W], b1[W], b2[W];
+  remove_one<W>(P.e1 + (int64_t)I * W, P.e2 + (int64_t)I * W, p, a1, a2);
+  remove_one<W>(P.e1 + (int64_t)J * W, P.e2 + (int64_t)J * W, q, b1, b2);
+  bool same = true;
+#pragma unroll
+  for (int w = 0; w < W; ++w) same = same && a1[w] == b1[w] && a2[w] == b2[w];
+  return same;
+}
+
+// One block per SM holding the [kb][ntri] accumulator once for 24 warps.
+constexpr int DEN_WT = 768;
+
+// Warp per configuration pair (both sides <= 32 determinants).  Lane d holds determinant d
+// of I; its partner in J under the move p <-> q is looked up in the inverse template table
+// from the moved string's alpha pattern over J's open shells.  Products and lane sums are
+// float-float on the FP32 pipe (GB300's FP64 pipe is ~64x narrower); each pair's total is
+// converted to FP64 once, scaled by the SEF normalisation and added to the accumulator.
+template <int W>
+__global__ void __launch_bounds__(DEN_WT, 1) k_density_pairs_warp(DenParams P) {
+  extern __shared__ double acc[];  // [kb][ntri], then the inverse table
+  int8_t *inv = reinterpret_cast<int8_t *>(acc + (size_t)P.kb * P.ntri);
+  for (int t = threadIdx.x; t < P.kb * P.ntri; t += blockDim.x) acc[t] = 0.0;
+  build_inverse(P.tmpl, P.tmpl_off, inv);
+  const int lane = threadIdx.x & 31;
+  const bool odd = P.nelec & 1;
+  const double r2 = sqrt(0.5);
+  const int64_t nwarps = (int64_t)gridDim.x * (blockDim.x >> 5);
+  const int64_t wid = blockIdx.x * (int64_t)(blockDim.x >> 5) + (threadIdx.x >> 5);
+  // each warp walks one contiguous range of the pair list: one search for its start
+  const int64_t t0 = P.npairs * wid / nwarps, tend = P.npairs * (wid + 1) / nwarps;
+  if (t0 < tend) {
+    int64_t lo = 0, hi = P.ng - 1;
+    while (lo < hi) {
+      const int64_t mid = (lo + hi + 1) >> 1;
+      if (P.gpoff[mid] <= t0) lo = mid;
+      else hi = mid - 1;
+    }
+    int64_t g = lo;
+    int64_t e0 = P.geoff[g];
+    int m = (int)(P.geoff[g + 1] - e0);
+    bool mixed = P.gflag[g];
+    int64_t u = t0 - P.gpoff[g];
+    int a = 0;
+    while (u >= m - 1 - a) { u -= m - 1 - a; ++a; }
+    int b = a + 1 + (int)u;
+    int64_t cachedA = -1;
+    // row configuration I, cached over the pairs of one group member
+    int4 mA = make_int4(0, 0, 0, 0);
+    int clsI = 0, negI = 0, oI = 0;
+    uint64_t al[W], be[W];
+    float2 cI[KBW];
+    for (int64_t t = t0; t < tend; ++t) {
+      const int64_t ea = e0 + a, eb = e0 + b;
+      if (ea != cachedA) {
+        mA = P.gmem[ea];
+        const int js = P.jsym[mA.x];
+        clsI = psoci_det_class(P.nelec & 1, js, P.ksym);
+        negI = (js % 2 != P.ksym % 2);  // m = -1: the second determinant of an SEF enters negated
+        oI = (mA.w >> 8) & 0xff;
+        const int nI = (mA.w >> 16) & 0x3fff;
+        const bool has = lane < nI;
+        const int64_t d = (int64_t)mA.y + lane;
+#pragma unroll
+        for (int w = 0; w < W; ++w) {
+          al[w] = has ? P.alpha[d * W + w] : 0ull;
+          be[w] = has ? P.beta[d * W + w] : 0ull;
+        }
+        const float4 *src = reinterpret_cast<const float4 *>(P.vs + ((int64_t)mA.z + sef_of_det(lane, odd, oI)) * KBW);
+        const float4 c01 = has ? src[0] : make_float4(0.f, 0.f, 0.f, 0.f);
+        const float4 c23 = has ? src[1] : make_float4(0.f, 0.f, 0.f, 0.f);
+        const bool flip = has && !odd && oI && (lane & 1) && negI;
+        const float sg = flip ? -1.f : 1.f;
+        cI[0] = make_float2(sg * c01.x, sg * c01.y);
+        cI[1] = make_float2(sg * c01.z, sg * c01.w);
+        cI[2] = make_float2(sg * c23.x, sg * c23.y);
+        cI[3] = make_float2(sg * c23.z, sg * c23.w);
+        cachedA = ea;
+      }
+      const int4 mB = P.gmem[eb];
+      const int p = mA.w & 0xff, q = mB.w & 0xff;
+      if (!mixed || pair_exact<W>(P, mA.x, p, mB.x, q)) {
+        const int oJ = (mB.w >> 8) & 0xff;
+        const int phs = ((mA.w >> 30) ^ (mB.w >> 30)) & 1;  // configuration phases
+        uint64_t openJ[W];
+#pragma unroll
+        for (int w = 0; w < W; ++w) openJ[w] = P.gopen[eb * W + w];
+        const int8_t *invJ = inv + (clsI * INV_NOPEN + oJ) * 64;
+        const int plo = min(p, q), phi = max(p, q);
+        const int wp = p >> 6, wq = q >> 6;
+        const uint64_t bp = 1ull << (p & 63), bq = 1ull << (q & 63);
+        float2 s[KBW];
+#pragma unroll
+        for (int r = 0; r < KBW; ++r) s[r] = make_float2(0.f, 0.f);
+#pragma unroll
+        for (int spin = 0; spin < 2; ++spin) {
+          bool ok = true;
+          uint64_t ta[W];  // alpha string of the target determinant
+          int nb = 0;
+#pragma unroll
+          for (int w = 0; w < W; ++w) {
+            const uint64_t x = spin ? be[w] : al[w];
+            if (w == wp) ok = ok && (x & bp);
+            if (w == wq) ok = ok && !(x & bq);
+            const int b0 = w * 64;
+            const int lo1 = max(plo + 1 - b0, 0), hi1 = min(phi - b0, 64);
+            if (lo1 < hi1) nb += __popcll(x & ((hi1 == 64 ? ~0ull : ((1ull << hi1) - 1)) & ~((1ull << lo1) - 1)));
+            uint64_t tw = al[w];
+            if (!spin) {
+              if (w == wp) tw ^= bp;
+              if (w == wq) tw ^= bq;
+            }
+            ta[w] = tw;
+          }
+          // alpha pattern of the target over J's open shells (ascending)
+          int pat = 0, k = 0;
+#pragma unroll
+          for (int w = 0; w < W; ++w) {
+            uint64_t om = openJ[w];
+            while (om) {
+              const uint64_t lowbit = om & (~om + 1);
+              if (ta[w] & lowbit) pat |= 1 << k;
+              ++k;
+              om ^= lowbit;
+            }
+          }
+          const int jj = ok ? invJ[pat & 63] : -1;
+          if (jj >= 0) {
+            const float4 *src = reinterpret_cast<const float4 *>(P.vs + ((int64_t)mB.z + sef_of_det(jj, odd, oJ)) * KBW);
+            const float4 c01 = src[0], c23 = src[1];
+            const bool flipJ = !odd && oJ && (jj & 1) && negI;
+            const float sg = ((phs + nb + (int)flipJ) & 1) ? -1.f : 1.f;
+            const float2 cj[4] = {make_float2(sg * c01.x, sg * c01.y), make_float2(sg * c01.z, sg * c01.w),
+                                  make_float2(sg * c23.x, sg * c23.y), make_float2(sg * c23.z, sg * c23.w)};
+#pragma unroll
+            for (int r = 0; r < KBW; ++r) ff_fma(s[r].x, s[r].y, cI[r], cj[r]);
+          }
+        }
+        const float2 z = reduce_scatter4(s, lane);
+        const int r = (lane >> 3) & 3;
+        if ((lane & 7) == 0 && r < P.kb) {
+          const double f = (odd ? 1.0 : (oI ? r2 : 1.0) * (oJ ? r2 : 1.0));
+          const double v = ((double)z.x + (double)z.y) * f;
+          if (v != 0.0) atomicAdd(acc + (int64_t)r * P.ntri + phi * (phi + 1) / 2 + plo, v);
+        }
+      }
+      if (++b == m) {
+        if (++a == m - 1) {
+          if (++g >= P.ng) break;
+          e0 = P.geoff[g];
+          m = (int)(P.geoff[g + 1] - e0);
+          mixed = P.gflag[g];
+          a = 0;
+        }
+        b = a + 1;
+      }
+    }
+  }
+  __syncthreads();
+  for (int t = threadIdx.x; t < P.kb * P.ntri; t += blockDim.x)
+    if (acc[t] != 0.0) atomicAdd(P.dens + t, acc[t]);
+}
+
+// roots r0 .. r0+kb-1 of V as float-float pairs, KBW per SEF (missing roots zero)
+__global__ void k_split_roots(int64_t n, int kb, const double *__restrict__ v, int64_t ldv, float2 *__restrict__ vs) {
+  for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < n; s += (int64_t)gridDim.x * blockDim.x) {
+#pragma unroll
+    for (int r = 0; r < KBW; ++r) vs[s * KBW + r] = r < kb ? split_f64(v[(int64_t)r * ldv + s]) : make_float2(0.f, 0.f);
+  }
+}
+
 // diagonal: D[tri(p,p)] += occ_p(I) c_I^T (C C^T) c_I, one warp-reduction per orbital
 template <int W>
 __global__ void __launch_bounds__(DEN_T) k_density_diag(DenParams P) {
@@ -391,6 +661,11 @@ void psoci_density_release(psoci_ctx *c) {
   psoci_free(c->den_gpoff);
   psoci_free(c->den_gcfg);
   psoci_free(c->den_gorb);
+  psoci_free(c->den_gmem);
+  psoci_free(c->den_gopen);
+  psoci_free(c->den_vs);
+  c->den_vs_cap = 0;
+  psoci_free(c->den_gflag);
   c->den_ng = 0;
   c->den_npairs = 0;
   c->den_ready = false;
@@ -479,9 +754,26 @@ static psoci_status density_groups(psoci_ctx *c) {
   DEN_TRY(psoci_scan_i64(c, gm_p, c->den_gpoff, ng, &P));
   DEN_TRY(psoci_alloc(c, &c->den_gcfg, E2));
   DEN_TRY(psoci_alloc(c, &c->den_gorb, E2));
+  DEN_TRY(psoci_alloc(c, &c->den_gflag, ng));
+  const bool packed = c->ndet_total < (1ll << 31) && c->nsef_total < (1ll << 31);
+  if (packed) {
+    DEN_TRY(psoci_alloc(c, &c->den_gmem, E2));
+    DEN_TRY(psoci_alloc(c, &c->den_gopen, (size_t)E2 * W));
+  }
   psoci_note_launch();
-  k_hole_scatter<<<grid, DEN_T, 0, st>>>(nconf, W, c->d_e1, hoff, ent_slot, ent_rank, slot2g, c->den_geoff,
-                                         c->den_gcfg, c->den_gorb);
+  k_hole_scatter<<<grid, DEN_T, 0, st>>>(nconf, W, c->d_e1, c->d_e2, hoff, ent_slot, ent_rank, slot2g, c->den_geoff,
+                                         c->den_gcfg, c->den_gorb, c->d_detoff, c->d_sefoff, c->d_nopen,
+                                         c->d_phase, packed ? c->den_gmem : nullptr,
+                                         packed ? c->den_gopen : nullptr);
+  if (ng > 0) {
+    psoci_note_launch();
+    if (W == 1)
+      k_group_verify<1><<<grid, DEN_T, 0, st>>>(ng, c->den_geoff, c->den_gcfg, c->den_gorb, c->d_e1, c->d_e2,
+                                                c->d_jsym, c->den_gflag);
+    else
+      k_group_verify<2><<<grid, DEN_T, 0, st>>>(ng, c->den_geoff, c->den_gcfg, c->den_gorb, c->d_e1, c->d_e2,
+                                                c->d_jsym, c->den_gflag);
+  }
   DEN_CU(cudaStreamSynchronize(st));
   DEN_CU(cudaGetLastError());
   cleanup();
@@ -494,19 +786,31 @@ static psoci_status density_groups(psoci_ctx *c) {
 }
 
 // device vectors (root-major, stride ldv), device output [k][nbf(nbf+1)/2] (overwritten)
-psoci_status psoci_density1_device(psoci_ctx *c, int k, const double *dV, int64_t ldv, double *dD) {
+extern "C" psoci_status psoci_density1_device(psoci_ctx *c, int k, const double *dV, int64_t ldv, double *dD) {
+  if (!c || k < 1 || !dV || !dD) return PSOCI_ERR_INVALID_ARG;
   if (!c->have_dets) return psoci_fail(c, PSOCI_ERR_STATE, "density1: build the determinants first");
+  if (ldv < c->nsef_total) return psoci_fail(c, PSOCI_ERR_INVALID_ARG, "density1: ldv < N");
+  PSOCI_CUDA(c, cudaSetDevice(c->device));
   psoci_status s;
   if ((s = density_groups(c))) return s;
   cudaStream_t st = c->stream;
   const int ntri = c->nbf * (c->nbf + 1) / 2;
   PSOCI_CUDA(c, cudaMemsetAsync(dD, 0, sizeof(double) * (size_t)k * ntri, st));
-  // roots per pass: the block accumulator stays within 96 KB (two blocks per SM)
-  int kb = (int)((96 * 1024) / (sizeof(double) * ntri));
-  if (kb < 1) kb = 1;
-  if (kb > KB_MAX) kb = KB_MAX;
+  // roots per pass (spread evenly over the passes), bounded by the block accumulator
+  // one warp per configuration pair when every configuration has at most 32 determinants
+  const bool warp_path = c->max_ndet <= 32 && c->den_gmem != nullptr;
+  // accumulator budget: one block per SM on the warp path, two on the thread path
+  int kbmax = (int)(((warp_path ? 200 : 100) * 1024) / (sizeof(double) * ntri));
+  if (kbmax < 1) kbmax = 1;
+  if (kbmax > (warp_path ? KBW : KB_MAX)) kbmax = warp_path ? KBW : KB_MAX;
+  const int npass = (k + kbmax - 1) / kbmax;
+  const int kb = (k + npass - 1) / npass;
   int dev = c->device, nsm = 0;
   PSOCI_CUDA(c, cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  if (warp_path && c->den_vs_cap < (size_t)c->nsef_total * KBW) {
+    if ((s = psoci_alloc(c, &c->den_vs, (size_t)c->nsef_total * KBW))) return s;
+    c->den_vs_cap = (size_t)c->nsef_total * KBW;
+  }
   for (int r0 = 0; r0 < k; r0 += kb) {
     DenParams P{};
     P.nconf = c->nconf;
@@ -533,21 +837,34 @@ psoci_status psoci_density1_device(psoci_ctx *c, int k, const double *dV, int64_
     P.gpoff = c->den_gpoff;
     P.gcfg = c->den_gcfg;
     P.gorb = c->den_gorb;
+    P.gmem = c->den_gmem;
+    P.gopen = c->den_gopen;
+    P.gflag = c->den_gflag;
+    P.vs = c->den_vs;
+    P.tmpl = c->d_tmpl;
+    P.tmpl_off = c->d_tmpl_off;
     P.dens = dD + (int64_t)r0 * ntri;
     const size_t sm_diag = sizeof(double) * P.kb * c->nbf;
-    const size_t sm_pair = sizeof(double) * (size_t)P.kb * ntri;
+    const size_t sm_pair = sizeof(double) * (size_t)P.kb * ntri + (warp_path ? PSOCI_NCLS * INV_NOPEN * 64 : 0);
+    if (warp_path && P.npairs > 0) {
+      psoci_note_launch();
+      k_split_roots<<<4 * nsm, 256, 0, st>>>(c->nsef_total, P.kb, P.v, ldv, c->den_vs);
+      PSOCI_CUDA(c, cudaGetLastError());
+    }
     auto kd = (c->words == 1) ? k_density_diag<1> : k_density_diag<2>;
-    auto kp = (c->words == 1) ? k_density_pairs<1> : k_density_pairs<2>;
+    auto kp = warp_path ? ((c->words == 1) ? k_density_pairs_warp<1> : k_density_pairs_warp<2>)
+                        : ((c->words == 1) ? k_density_pairs<1> : k_density_pairs<2>);
+    const int nthr = warp_path ? DEN_WT : DEN_T;
     PSOCI_CUDA(c, cudaFuncSetAttribute(kp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_pair));
     psoci_note_launch();
     kd<<<2 * nsm, DEN_T, sm_diag, st>>>(P);
     PSOCI_CUDA(c, cudaGetLastError());
     if (P.npairs > 0) {
       int per = 0;
-      PSOCI_CUDA(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kp, DEN_T, sm_pair));
+      PSOCI_CUDA(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kp, nthr, sm_pair));
       if (per < 1) per = 1;
       psoci_note_launch();
-      kp<<<per * nsm, DEN_T, sm_pair, st>>>(P);
+      kp<<<per * nsm, nthr, sm_pair, st>>>(P);
       PSOCI_CUDA(c, cudaGetLastError());
     }
   }

@@ -31,8 +31,8 @@
 
 namespace {
 
-enum { CLS_EVEN = 0, CLS_ODD = 1, CLS_FRAC_P = 2, CLS_FRAC_M = 3, NCLS = 4 };
-constexpr int NOPEN_SLOTS = PSOCI_MAX_OPEN + 1;
+constexpr int NCLS = PSOCI_NCLS;
+constexpr int NOPEN_SLOTS = PSOCI_NOPEN_SLOTS;
 
 struct TmplEntry {
   uint32_t amask, bmask;
@@ -86,11 +86,6 @@ void template_run(int cls, int n, std::vector<TmplEntry> &run) {
   }
 }
 
-__device__ __forceinline__ int det_class(int parity, int jsym, int ksym) {
-  if (parity == 1) return ((((jsym + 1) / 2) % 2) == 0) ? CLS_FRAC_M : CLS_FRAC_P;
-  return ((jsym + 1) / 2 == (ksym + 1) / 2) ? CLS_EVEN : CLS_ODD;
-}
-
 // one warp per configuration; lanes stride over its determinants
 template <int W>
 __global__ void k_build_dets(int nconf, int nelec, int ksym, int msbas, const uint64_t *__restrict__ e1,
@@ -134,7 +129,7 @@ __global__ void k_build_dets(int nconf, int nelec, int ksym, int msbas, const ui
         inv += __popcll(D[w] & m);
       }
     }
-    int cls = det_class(nelec & 1, jsym[i], ksym);
+    int cls = psoci_det_class(nelec & 1, jsym[i], ksym);
     int run0 = tmpl_off[cls * NOPEN_SLOTS + no];
     int nd = 1 << (no > 1 ? no - 1 : 0);
     int64_t d0 = detoff[i];

@@ -92,6 +92,11 @@ struct psoci_ctx {
   int64_t *den_gpoff = nullptr;  // [ng+1] first candidate pair of each group
   int32_t *den_gcfg = nullptr;   // members: configuration
   uint8_t *den_gorb = nullptr;   // members: orbital the key removed
+  int4 *den_gmem = nullptr;      // members packed with their configuration's offsets
+  uint8_t *den_gflag = nullptr;  // [ng] 1: members' exact keys differ (hash collision)
+  uint64_t *den_gopen = nullptr; // members: open shells of the configuration [words]
+  float2 *den_vs = nullptr;      // float-float copy of the roots of one pass
+  size_t den_vs_cap = 0;
 
   // initial guess for the next Davidson run (root-major, guess_k x nsef)
   std::vector<double> guess;
@@ -150,11 +155,18 @@ void psoci_join_release(psoci_ctx *c);
 void psoci_h_release(psoci_ctx *c);
 void psoci_dets_release(psoci_ctx *c);
 void psoci_density_release(psoci_ctx *c);
-psoci_status psoci_density1_device(psoci_ctx *c, int k, const double *dV, int64_t ldv, double *dD);
 
 // ------------------------------------------------------------------------------------
 // device helpers
 // ------------------------------------------------------------------------------------
+// determinant template classes (generateDeterminants, PsociDeterminants.C:1467-1505)
+enum { CLS_EVEN = 0, CLS_ODD = 1, CLS_FRAC_P = 2, CLS_FRAC_M = 3, PSOCI_NCLS = 4 };
+#define PSOCI_NOPEN_SLOTS (PSOCI_MAX_OPEN + 1)
+__host__ __device__ __forceinline__ int psoci_det_class(int parity, int jsym, int ksym) {
+  if (parity == 1) return ((((jsym + 1) / 2) % 2) == 0) ? CLS_FRAC_M : CLS_FRAC_P;
+  return ((jsym + 1) / 2 == (ksym + 1) / 2) ? CLS_EVEN : CLS_ODD;
+}
+
 __device__ __forceinline__ int64_t tri64(int64_t i, int64_t j) {
   int64_t a = i > j ? i : j, b = i > j ? j : i;
   return a * (a + 1) / 2 + b;
