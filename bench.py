@@ -218,6 +218,34 @@ def run_ours(args):
             torch.cuda.synchronize(dev)
             ts.append(a.elapsed_time(b) * 1e-3)
         sig[name] = float(np.mean(ts))
+    # 1-particle density (the reference's CIDEN path) of 8 unit vectors: outside the
+    # headline step; the first call also forms the configuration groups
+    ntri = p.nbf * (p.nbf + 1) // 2
+    V = torch.randn(NROOTS, N, dtype=torch.float64, device=dev)
+    V /= V.norm(dim=1, keepdim=True)
+    Dd = torch.empty(NROOTS, ntri, dtype=torch.float64, device=dev)
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize(dev)
+    a.record(stream)
+    ctx.density1_device(V.data_ptr(), N, Dd.data_ptr(), NROOTS)
+    b.record(stream)
+    torch.cuda.synchronize(dev)
+    den_first = a.elapsed_time(b) * 1e-3
+    ts = []
+    for _ in range(5):
+        flush_l2(torch, dev)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize(dev)
+        a.record(stream)
+        ctx.density1_device(V.data_ptr(), N, Dd.data_ptr(), NROOTS)
+        b.record(stream)
+        torch.cuda.synchronize(dev)
+        ts.append(a.elapsed_time(b) * 1e-3)
+    den_s = float(np.mean(ts))
+    diag = [q * (q + 1) // 2 + q for q in range(p.nbf)]
+    den_trace_err = float((Dd[:, diag].sum(1) - p.nelec).abs().max())
+    del V, Dd
+
     hbm, peak_kind = peaks()
     # dominant kernel: the element evaluation of the H build (k_hbuild_fast), timed by the
     # library's CUDA events on its stream in every timed mixed step.  Algorithmic bytes: the
@@ -254,9 +282,11 @@ def run_ours(args):
     e2e_s = barrier_max(float(np.mean(e2e_times)), ws)
 
     cpu = None
+    cpu_den = None
     if rank == 0 and not args.no_cpu:
         cpu = cpu_estimate(p, args.cpu_rows, args.cpu_sample, r_fp64.sigma_calls)
         cpu["nnz_full_measured"] = int(nnz)
+        cpu_den = cpu_density_estimate(p, args.cpu_density_rows)
 
     if rank == 0:
         clocks = clk.summary()
@@ -301,6 +331,10 @@ def run_ours(args):
                                                          "total_ms")},
             "h_build_counts": {k: int(bs[k]) for k in ("candidates", "pairs", "segments", "nnz", "nnz_lower",
                                                         "slab_slots", "evaluations")},
+            "density1": {"s": round(den_s, 6), "first_call_s": round(den_first, 6), "roots": NROOTS,
+                         "trace_err": den_trace_err, "cpu_estimate": cpu_den,
+                         "note": "CIDEN 1-particle density of 8 unit vectors, device pointers, mean of 5 "
+                                 "(L2 flushed); first call includes the configuration groups"},
             "e2e": {"value": round(e2e_s, 6), "unit": "s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": d2h},
             "gpu_launches": int(l_mixed),
             "gpu_launches_detail": {"mixed_steps": int(l_mixed), "per_mixed_step": round(l_mixed / max(args.steps, 1), 1),
@@ -366,6 +400,25 @@ def cpu_estimate(p, rows_sample, sigma_sample, sigma_vectors, seed=0):
             "sample_seconds": round(t_rows, 3)}
 
 
+def cpu_density_estimate(p, rows_sample, seed=0):
+    """Seconds the oracle's restatement of the reference's CIDEN loop (every pair j <= i
+    screened, one thread) needs for the densities of NROOTS vectors, from ``rows_sample``
+    random rows scaled by nconf / rows_sample."""
+    import oracle
+
+    oracle.build(ref=False)
+    O = oracle.Oracle(p)
+    rng = np.random.default_rng(seed)
+    ns = min(rows_sample, p.nconf)
+    rows = rng.choice(p.nconf, ns, replace=False).astype(np.int32)
+    v = rng.standard_normal((NROOTS, O.num_sefs()))
+    t0 = time.perf_counter()
+    O.density1_rows(v, rows)
+    dt = time.perf_counter() - t0
+    return {"value": round(dt * p.nconf / ns, 2), "unit": "s", "cores": 1, "kind": "port",
+            "sample": f"{ns} random rows of {p.nconf} ({dt:.2f} s), scaled x{p.nconf / ns:.0f}"}
+
+
 def sample_problem(p, nconf):
     import dataclasses
 
@@ -417,6 +470,7 @@ def main():
     ap.add_argument("--max-subspace", type=int, default=48)
     ap.add_argument("--cpu-sample", type=int, default=20000, help="configurations in the CPU sigma sample")
     ap.add_argument("--cpu-rows", type=int, default=8000, help="random row configurations in the CPU build sample")
+    ap.add_argument("--cpu-density-rows", type=int, default=48, help="random rows in the CPU density sample")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--verbose", type=int, default=0)
     args = ap.parse_args()

@@ -141,6 +141,15 @@ class Oracle(_Base):
             self.ctx, v.shape[0], _p(v, _c_dbl_p), _p(out, _c_dbl_p))
         return out
 
+    def density1_rows(self, vecs, rows):
+        """The reference's pair loop restricted to rows I (pairs J <= I), for timing samples."""
+        v = np.ascontiguousarray(np.atleast_2d(vecs), np.float64)
+        r = np.ascontiguousarray(rows, np.int32)
+        out = np.zeros((v.shape[0], self.p.nbf * (self.p.nbf + 1) // 2))
+        self._fn("density1_rows", None, [ctypes.c_void_p, ctypes.c_int, _c_dbl_p, ctypes.c_int, _c_int_p, _c_dbl_p])(
+            self.ctx, v.shape[0], _p(v, _c_dbl_p), len(r), _p(r, _c_int_p), _p(out, _c_dbl_p))
+        return out
+
     def diag(self):
         d = np.zeros(self.num_sefs())
         self._fn("diag", None, [ctypes.c_void_p, _c_dbl_p])(self.ctx, _p(d, _c_dbl_p))

@@ -765,7 +765,8 @@ int orc_ciden_block(const orc_ctx *c, int i, int j, double *out) {
   return st;
 }
 
-void orc_density1(const orc_ctx *c, int k, const double *vecs, double *dens) {
+/* rows: the configurations I whose pairs (I, J <= I) are accumulated (NULL: all, in order) */
+static void density1_rows(const orc_ctx *c, int k, const double *vecs, int nrows, const int *rows, double *dens) {
   const long N = c->sefoff[c->nconf];
   const long ntri = (long)c->nbf * (c->nbf + 1) / 2;
   memset(dens, 0, sizeof(double) * k * ntri);
@@ -775,7 +776,8 @@ void orc_density1(const orc_ctx *c, int k, const double *vecs, double *dens) {
   for (int q = 0; q < k; ++q) {
     const double *v = vecs + (size_t)q * N;
     double *D = dens + (size_t)q * ntri;
-    for (int I = 0; I < c->nconf; ++I) {
+    for (int t = 0; t < nrows; ++t) {
+      const int I = rows ? rows[t] : t;
       const orc_cfg *gi = &c->cfg[I];
       const unsigned char *io = c->occ + (size_t)I * c->nbf;
       for (int J = 0; J <= I; ++J) {
@@ -808,4 +810,13 @@ void orc_density1(const orc_ctx *c, int k, const double *vecs, double *dens) {
     }
   }
   free(dd); free(sc); free(ss);
+}
+
+void orc_density1(const orc_ctx *c, int k, const double *vecs, double *dens) {
+  density1_rows(c, k, vecs, c->nconf, NULL, dens);
+}
+
+/* the pairs of the listed rows only (a sample of the reference loop, for timing) */
+void orc_density1_rows(const orc_ctx *c, int k, const double *vecs, int nrows, const int *rows, double *dens) {
+  density1_rows(c, k, vecs, nrows, rows, dens);
 }

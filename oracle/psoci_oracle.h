@@ -33,6 +33,7 @@ void orc_sigma_lower(long n, const long *rowptr, const int *cols, const double *
  * (vecs: k x N root-major; dens: k x nbf(nbf+1)/2). */
 int orc_ciden_block(const orc_ctx *c, int i, int j, double *out);
 void orc_density1(const orc_ctx *c, int k, const double *vecs, double *dens);
+void orc_density1_rows(const orc_ctx *c, int k, const double *vecs, int nrows, const int *rows, double *dens);
 
 #ifdef __cplusplus
 }
