@@ -172,6 +172,7 @@ psoci_status psoci_set_configs(psoci_ctx *c, int nbf, int nelec, int ksym, int m
   c->h_jsym.assign(jsym, jsym + nconf);
   c->h_occ.assign(occ, occ + (size_t)nconf * nbf);
   c->slab_hint = 0;
+  c->join_hint = 0;
   c->have_cfgs = true;
   return psoci_join_prepare(c);
 }

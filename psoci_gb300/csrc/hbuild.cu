@@ -396,13 +396,27 @@ __global__ void k_group_lists(JoinTabs J, const double *__restrict__ eri, int64_
   }
 }
 
+// Slab of the single-pass join (MODE 2): each warp appends the neighbour lists of its
+// configurations to chunks it takes from a shared counter; a configuration's list stays
+// contiguous (a list outgrowing its chunk moves to a fresh one).  Positions at or beyond
+// cap are not touched; the host sees the counter and falls back to count + write passes.
+struct JoinSlab {
+  int32_t *list;
+  unsigned long long *counter;
+  int64_t cap;
+  int64_t *start;  // [nconf] slab position of each configuration's list
+};
+constexpr int JOIN_CHUNK = 4096;
+
 template <int W, int MODE>
-__global__ void __launch_bounds__(256) k_join(Params P, JoinTabs J, int64_t *cnt, int64_t *ncand, const int64_t *off) {
+__global__ void __launch_bounds__(256) k_join(Params P, JoinTabs J, int64_t *cnt, int64_t *ncand, const int64_t *off,
+                                              JoinSlab S) {
   __shared__ int s_pre[8][33], s_q0[8][32], s_lp[8][32], s_h[8][32];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
   const uint32_t lomask = (1u << J.s) - 1u;
+  unsigned long long cursor = 0, chunk_end = 0;  // MODE 2: this warp's slab chunk
   for (int64_t i = warp; i < P.nconf; i += nwarps) {
     uint64_t a1[W], a2[W];
 #pragma unroll
@@ -410,6 +424,7 @@ __global__ void __launch_bounds__(256) k_join(Params P, JoinTabs J, int64_t *cnt
     const int li = J.lid[i], js_i = P.jsym[i];
     int64_t nk = 0, nc = 0;
     int64_t base = (MODE == 1) ? off[i] : 0;
+    unsigned long long lstart = cursor;  // MODE 2: where this configuration's list begins
     const int64_t gl0 = J.goff[J.gid[i]], gl1 = J.goff[J.gid[i] + 1];
     for (int64_t h0 = gl0; h0 < gl1; h0 += 32) {
       // this lane's hi pattern h: the lo patterns l' with d_lo <= 4 - d_hi, as a range of
@@ -477,14 +492,48 @@ __global__ void __launch_bounds__(256) k_join(Params P, JoinTabs J, int64_t *cnt
         if (MODE == 0) {
           nc += __popc(__ballot_sync(0xffffffffu, found));
           nk += __popc(kb);
-        } else {
+        } else if (MODE == 1) {
           if (keep) P.nbr[base + __popc(kb & ((1u << lane) - 1u))] = j;
           base += __popc(kb);
+        } else {
+          nc += __popc(__ballot_sync(0xffffffffu, found));
+          if (cursor + 32 > chunk_end) {
+            // a fresh chunk; the list written so far moves along
+            const unsigned long long len = (unsigned long long)max((int64_t)JOIN_CHUNK, 2 * (nk + 32));
+            unsigned long long b = 0;
+            if (lane == 0) b = atomicAdd(S.counter, len);
+            b = __shfl_sync(0xffffffffu, b, 0);
+            __syncwarp();  // the list's earlier entries were written by other lanes
+            for (int64_t t = lane; t < nk; t += 32) {
+              const unsigned long long from = lstart + t, to = b + t;
+              if ((int64_t)from < S.cap && (int64_t)to < S.cap) S.list[to] = S.list[from];
+            }
+            lstart = b;
+            cursor = b + nk;
+            chunk_end = b + len;
+          }
+          const unsigned long long pos = cursor + __popc(kb & ((1u << lane) - 1u));
+          if (keep && (int64_t)pos < S.cap) S.list[pos] = j;
+          cursor += __popc(kb);
+          nk += __popc(kb);
         }
       }
       __syncwarp();
     }
-    if (MODE == 0 && lane == 0) { cnt[i] = nk; ncand[i] = nc; }
+    if (MODE != 1 && lane == 0) { cnt[i] = nk; ncand[i] = nc; }
+    if (MODE == 2 && lane == 0) S.start[i] = (int64_t)lstart;
+  }
+}
+
+// neighbour lists from the join slab to their final, contiguous places
+__global__ void k_join_compact(int nconf, const int32_t *__restrict__ slab, const int64_t *__restrict__ start,
+                               const int64_t *__restrict__ nbroff, int32_t *__restrict__ nbr) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t i = warp; i < nconf; i += nwarps) {
+    const int64_t o = nbroff[i], len = nbroff[i + 1] - o, st = start[i];
+    for (int64_t t = lane; t < len; t += 32) nbr[o + t] = slab[st + t];
   }
 }
 
@@ -1520,6 +1569,8 @@ psoci_status run_build(psoci_ctx *c, psoci_hmode mode, int64_t *nnz_out) {
   int *d_err = nullptr;
   unsigned long long *d_counter = nullptr;
   double *d_slabval = nullptr;
+  int32_t *d_jslab = nullptr;
+  int64_t *d_jstart = nullptr;
   cudaEvent_t ev[6] = {};
   auto cleanup = [&]() {
     for (auto &e : ev)
@@ -1527,7 +1578,7 @@ psoci_status run_build(psoci_ctx *c, psoci_hmode mode, int64_t *nnz_out) {
     psoci_free(d_soff); psoci_free(d_tot); psoci_free(d_segslot); psoci_free(d_counter);
     psoci_free(d_candoff); psoci_free(d_cand);
     psoci_free(d_nlow); psoci_free(d_prrows); psoci_free(d_proff); psoci_free(d_mk); psoci_free(d_prm);
-    psoci_free(d_err); psoci_free(d_slabval);
+    psoci_free(d_err); psoci_free(d_slabval); psoci_free(d_jslab); psoci_free(d_jstart);
     psoci_free(d_gcnt); psoci_free(d_goff); psoci_free(d_glist);
     psoci_free(d_cnt); psoci_free(d_nbroff); psoci_free(d_nseg); psoci_free(d_nrow); psoci_free(d_segoff);
     psoci_free(d_rowslot); psoci_free(d_segk0); psoci_free(d_segrow); psoci_free(d_segcnt); psoci_free(d_rownnz);
@@ -1586,16 +1637,58 @@ psoci_status run_build(psoci_ctx *c, psoci_hmode mode, int64_t *nnz_out) {
     TRY(psoci_alloc(c, &d_candoff, n + 1));
     TRY(psoci_alloc(c, &d_nbroff, n + 1));
     const int jblocks = (int)std::max<int64_t>(1, std::min<int64_t>(((int64_t)n * 32 + 255) / 256, 152 * 32));
-    psoci_note_launch();
-    k_join<W, 0><<<jblocks, 256, 0, st>>>(P, J, d_cnt, d_tot, nullptr);
-    TRYC(cudaGetLastError());
-    TRY(psoci_scan_i64(c, d_tot, d_candoff, n, &ncand));
-    TRY(psoci_scan_i64(c, d_cnt, d_nbroff, n, &npairs));
-    TRY(psoci_alloc(c, &d_nbr, npairs));
+    // single pass into a slab sized from the last build of this space (or 1024 neighbours
+    // a configuration plus the warps' chunk tails), then a compaction copy; the count and
+    // write passes remain for a slab that turns out too small
+    JoinSlab S = {};
+    bool single = false;
+    {
+      size_t freeb = 0, totb = 0;
+      TRYC(cudaMemGetInfo(&freeb, &totb));
+      const int64_t tails = (int64_t)jblocks * 8 * 2 * JOIN_CHUNK;
+      int64_t cap = std::max<int64_t>(c->join_hint + c->join_hint / 8, 1024 * (int64_t)n) + tails;
+      cap = std::min<int64_t>(cap, (int64_t)(freeb * 0.4) / 4);
+      if (psoci_alloc(c, &d_jslab, cap) == PSOCI_OK && psoci_alloc(c, &d_jstart, n + 1) == PSOCI_OK &&
+          psoci_alloc(c, &d_counter, 1) == PSOCI_OK) {
+        TRYC(cudaMemsetAsync(d_counter, 0, sizeof(unsigned long long), st));
+        S = {d_jslab, d_counter, cap, d_jstart};
+        psoci_note_launch();
+        k_join<W, 2><<<jblocks, 256, 0, st>>>(P, J, d_cnt, d_tot, nullptr, S);
+        TRYC(cudaGetLastError());
+        unsigned long long used = 0;
+        TRYC(cudaMemcpyAsync(&used, d_counter, sizeof(used), cudaMemcpyDeviceToHost, st));
+        TRYC(cudaStreamSynchronize(st));
+        if ((int64_t)used <= cap) {
+          TRY(psoci_scan_i64(c, d_tot, d_candoff, n, &ncand));
+          TRY(psoci_scan_i64(c, d_cnt, d_nbroff, n, &npairs));
+          TRY(psoci_alloc(c, &d_nbr, npairs));
+          psoci_note_launch();
+          k_join_compact<<<jblocks, 256, 0, st>>>(n, d_jslab, d_jstart, d_nbroff, d_nbr);
+          TRYC(cudaGetLastError());
+          single = true;
+        }
+        c->join_hint = (int64_t)used;
+      } else {
+        cudaGetLastError();  // no room for the slab: the two passes below
+      }
+      TRYC(cudaStreamSynchronize(st));
+      psoci_free(d_jslab);
+      psoci_free(d_jstart);
+      psoci_free(d_counter);
+    }
+    if (!single) {
+      psoci_note_launch();
+      k_join<W, 0><<<jblocks, 256, 0, st>>>(P, J, d_cnt, d_tot, nullptr, S);
+      TRYC(cudaGetLastError());
+      TRY(psoci_scan_i64(c, d_tot, d_candoff, n, &ncand));
+      TRY(psoci_scan_i64(c, d_cnt, d_nbroff, n, &npairs));
+      TRY(psoci_alloc(c, &d_nbr, npairs));
+      P.nbroff = d_nbroff; P.nbr = d_nbr;
+      psoci_note_launch();
+      k_join<W, 1><<<jblocks, 256, 0, st>>>(P, J, nullptr, nullptr, d_nbroff, S);
+      TRYC(cudaGetLastError());
+    }
     P.nbroff = d_nbroff; P.nbr = d_nbr;
-    psoci_note_launch();
-    k_join<W, 1><<<jblocks, 256, 0, st>>>(P, J, nullptr, nullptr, d_nbroff);
-    TRYC(cudaGetLastError());
   } else {
   const int scr_rows = (n + SCR_THREADS * SCR_ROWS - 1) / (SCR_THREADS * SCR_ROWS);
   nsplit = (int)std::max<int64_t>(1, std::min<int64_t>(64, (152 * 8 + scr_rows - 1) / scr_rows));

@@ -84,6 +84,7 @@ struct psoci_ctx {
   double build_seconds = 0.0;
   psoci_build_info binfo{};
   int64_t slab_hint = 0;  // value-slab slots the last build of this space used
+  int64_t join_hint = 0;  // join-slab slots the last build of this space used
 
   // 1-particle density: configuration groups sharing a hole key (density.cu)
   bool den_ready = false;
