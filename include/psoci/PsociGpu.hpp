@@ -202,6 +202,11 @@ class PsociGAhamiltonian {
           "psoci_build_hamiltonian");
     return nnz_;
   }
+  // the reference's DIRECTMATRIXPRODUCTS build (PsociGAhamiltonian.C:7549-7826): nothing
+  // stored, every matrixVectorProducts call evaluates the elements again
+  void constructGlobalHamiltonianDirect() {
+    check(dev_.get(), psoci_build_hamiltonian(dev_.get(), PSOCI_HMODE_DIRECT, &nnz_), "psoci_build_hamiltonian");
+  }
   int64_t numberNonzeroElements() const { return nnz_; }
   // constructCIdensityAltOrbMapChunkJmap (PsociGAhamiltonian.C:11570-11760): density[root] is
   // the packed nbf(nbf+1)/2 spin-free 1-particle density of root-major vectors vecs (k x N)

@@ -58,7 +58,9 @@ typedef enum {
 
 typedef enum {
   PSOCI_HMODE_CSR_FP64 = 0,   /* stored FP64 CSR only                                   */
-  PSOCI_HMODE_CSR_BOTH = 1    /* stored FP64 CSR plus an FP32 copy of the elements      */
+  PSOCI_HMODE_CSR_BOTH = 1,   /* stored FP64 CSR plus an FP32 copy of the elements      */
+  PSOCI_HMODE_DIRECT = 2      /* nothing stored: neighbour lists and the diagonal only;  */
+                              /* every sigma evaluates the elements again (FP64)         */
 } psoci_hmode;
 
 /* Replaces GA::Initialize + the PsociGAhamiltonian constructor
@@ -104,7 +106,14 @@ PSOCI_API psoci_status psoci_get_determinants(const psoci_ctx *ctx, uint64_t *al
 /* Replaces PsociGAhamiltonian::constructGlobalHamiltonianAltOrbMapDirectChunkJmap
  * (PsociGAhamiltonian.C:2530-2857) with packSefsef (:4077-4136): the full symmetric H in CSR
  * (both triangles; each off-diagonal element is the reference's lower-triangle value), elements
- * with |x| >= 1e-8 or on the diagonal.  *nnz receives the stored count. */
+ * with |x| >= 1e-8 or on the diagonal.  *nnz receives the stored count.
+ * PSOCI_HMODE_DIRECT stands in for the reference's direct products
+ * (matrixVectorProductsSplitChunkMultipleJchunksLowLevelAccumulateDirectFetch,
+ * PsociGAhamiltonian.C:7549-7826, built with DIRECTMATRIXPRODUCTS): only the screened
+ * neighbour lists and the diagonal are kept (*nnz = 0); psoci_sigma / psoci_sigma_device /
+ * psoci_davidson then evaluate every element again on each call, in FP64 whatever the
+ * precision asked for, applying the same |x| >= 1e-8 rule.  psoci_get_hamiltonian,
+ * psoci_save_hamiltonian and psoci_sigma_mixed_noalloc answer PSOCI_ERR_STATE. */
 PSOCI_API psoci_status psoci_build_hamiltonian(psoci_ctx *ctx, psoci_hmode mode, int64_t *nnz);
 /* Counters and phase times of the last psoci_build_hamiltonian.  Times are CUDA-event
  * intervals on the library stream, in milliseconds; the evaluation time covers the final

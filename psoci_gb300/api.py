@@ -21,7 +21,7 @@ STATUS = {
     6: "device wait timed out", 7: "not converged", 8: "non-finite value", 9: "i/o error",
 }
 PREC_FP64, PREC_MIXED, PREC_FF = 0, 1, 2
-HMODE_CSR_FP64, HMODE_CSR_BOTH = 0, 1
+HMODE_CSR_FP64, HMODE_CSR_BOTH, HMODE_DIRECT = 0, 1, 2
 
 
 class PsociError(RuntimeError):
@@ -219,10 +219,12 @@ class Context:
         return dict(alpha=a.reshape(-1, words), beta=b.reshape(-1, words), phase=ph, ms=ms, detoff=do, sefoff=so)
 
     # -- Hamiltonian ---------------------------------------------------------------------
-    def build_hamiltonian(self, mixed: bool = True) -> int:
+    def build_hamiltonian(self, mixed: bool = True, direct: bool = False) -> int:
+        """Stored CSR (FP64, plus an FP32 copy when mixed), or with direct=True no stored
+        elements: every sigma evaluates them again (returns 0)."""
         nnz = ctypes.c_int64()
-        self._check(self.lib.psoci_build_hamiltonian(self.ctx, HMODE_CSR_BOTH if mixed else HMODE_CSR_FP64,
-                                                     ctypes.byref(nnz)), "build_hamiltonian")
+        mode = HMODE_DIRECT if direct else (HMODE_CSR_BOTH if mixed else HMODE_CSR_FP64)
+        self._check(self.lib.psoci_build_hamiltonian(self.ctx, mode, ctypes.byref(nnz)), "build_hamiltonian")
         self.nnz = nnz.value
         return self.nnz
 

@@ -213,7 +213,7 @@ psoci_status psoci_get_determinants(const psoci_ctx *cc, uint64_t *alpha, uint64
 
 psoci_status psoci_build_hamiltonian(psoci_ctx *c, psoci_hmode mode, int64_t *nnz) {
   if (!c) return PSOCI_ERR_INVALID_ARG;
-  if (mode != PSOCI_HMODE_CSR_FP64 && mode != PSOCI_HMODE_CSR_BOTH)
+  if (mode != PSOCI_HMODE_CSR_FP64 && mode != PSOCI_HMODE_CSR_BOTH && mode != PSOCI_HMODE_DIRECT)
     return psoci_fail(c, PSOCI_ERR_INVALID_ARG, "build_hamiltonian: unknown mode");
   psoci_status s;
   if ((s = set_device(c))) return s;
@@ -234,6 +234,7 @@ psoci_status psoci_get_hamiltonian(const psoci_ctx *cc, int64_t *rowptr, int32_t
   psoci_ctx *c = const_cast<psoci_ctx *>(cc);
   if (!c) return PSOCI_ERR_INVALID_ARG;
   if (!c->have_h) return psoci_fail(c, PSOCI_ERR_STATE, "get_hamiltonian: not built");
+  if (c->direct) return psoci_fail(c, PSOCI_ERR_STATE, "get_hamiltonian: direct mode stores no matrix");
   psoci_status s;
   if ((s = set_device(c))) return s;
   if (rowptr)

@@ -510,7 +510,7 @@ psoci_status psoci_davidson_impl(psoci_ctx *c, const psoci_dav_opts *o, double *
   if (maxsub < 2 * nr && N >= 2 * nr) return psoci_fail(c, PSOCI_ERR_INVALID_ARG, "davidson: subspace too small");
   if (o->prec != PSOCI_PREC_FP64 && o->prec != PSOCI_PREC_MIXED && o->prec != PSOCI_PREC_FF)
     return psoci_fail(c, PSOCI_ERR_INVALID_ARG, "davidson: unknown precision");
-  if (o->prec == PSOCI_PREC_MIXED && !c->d_val32)
+  if (o->prec == PSOCI_PREC_MIXED && !c->d_val32 && !c->direct)
     return psoci_fail(c, PSOCI_ERR_STATE, "davidson: MIXED needs PSOCI_HMODE_CSR_BOTH");
   const double rtol = o->rtol > 0 ? o->rtol : 1e-6;
   const double dmin = o->precond_min > 0 ? o->precond_min : 1e-3;

@@ -102,6 +102,10 @@ struct Params {
   double *val;
   float *val32;
   double *diag;
+  // direct sigma (PASS 2): Y[:, 0:kvec] += H X[:, 0:kvec]
+  const double *dx;
+  double *dy;
+  int ldx, ldy, kvec;
 };
 
 // ------------------------------------------------------------------------------------
@@ -975,8 +979,30 @@ __device__ double sef_elem(const Params &PP, const PairInfo &pi, const double *K
   return ds0;
 }
 
+// FP64 sum over the warp of v[0..7], scattered: lanes 4q..4q+3 end with the total of q
+__device__ __forceinline__ double reduce_scatter8_f64(const double (&v)[8], int lane) {
+  double a[4], b[2];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const bool hi = lane & 16;
+    a[i] = (hi ? v[i + 4] : v[i]) + __shfl_xor_sync(0xffffffffu, hi ? v[i] : v[i + 4], 16);
+  }
+#pragma unroll
+  for (int i = 0; i < 2; ++i) {
+    const bool hi = lane & 8;
+    b[i] = (hi ? a[i + 2] : a[i]) + __shfl_xor_sync(0xffffffffu, hi ? a[i] : a[i + 2], 8);
+  }
+  const bool hi = lane & 4;
+  double c = (hi ? b[1] : b[0]) + __shfl_xor_sync(0xffffffffu, hi ? b[0] : b[1], 4);
+  c += __shfl_xor_sync(0xffffffffu, c, 2);
+  c += __shfl_xor_sync(0xffffffffu, c, 1);
+  return c;
+}
+
 // ------------------------------------------------------------------------------------
-// segment kernel: PASS 0 counts kept elements per row, PASS 1 writes them
+// segment kernel over full neighbour lists: PASS 0 counts kept elements per row, PASS 1
+// writes them; direct mode: PASS 2 adds H X into Y (atomically: a configuration's rows
+// may span several segments), PASS 3 writes the diagonal only
 // ------------------------------------------------------------------------------------
 template <int W, int PASS>
 __global__ void __launch_bounds__(WARPS_PER_CTA * 32) k_hbuild(Params P) {
@@ -1007,7 +1033,13 @@ __global__ void __launch_bounds__(WARPS_PER_CTA * 32) k_hbuild(Params P) {
     if (lane == 0) ws->itemoff[0] = 0;
     __syncwarp();
     const int T = ws->itemoff[n];
-    for (int r = 0; r < nsefI; ++r) {
+    // PASS 3: the diagonal block (J = I) is in exactly one segment of I
+    if (PASS == 3 && lane < n && ws->pi[lane].kind == K_DIAG)
+      for (int r = 0; r < nsefI; ++r) P.diag[P.sefoff[I] + r] = sef_elem<W>(P, ws->pi[lane], ws->K, r, r);
+    for (int r = 0; r < (PASS == 3 ? 0 : nsefI); ++r) {
+      double acc[8];
+#pragma unroll
+      for (int q = 0; q < 8; ++q) acc[q] = 0.0;
       int64_t base = 0;
       if (PASS == 1) base = P.rowptr[P.sefoff[I] + r] + P.seg_cnt[P.seg_rowoff[s] + r];
       int64_t cnt = 0;
@@ -1033,6 +1065,12 @@ __global__ void __launch_bounds__(WARPS_PER_CTA * 32) k_hbuild(Params P) {
           v = sef_elem<W>(P, pi, ws->K, flip ? t : r, flip ? r : t);
           keep = (fabs(v) >= PSOCI_MIN_VALUE) || (diag_blk && t == r);
         }
+        if (PASS == 2 && keep) {
+          const double *xr = P.dx + (int64_t)(ws->pi[k].colbase + t) * P.ldx;
+#pragma unroll
+          for (int q = 0; q < 8; ++q)
+            if (q < P.kvec) acc[q] = fma(v, xr[q], acc[q]);
+        }
         unsigned b = __ballot_sync(0xffffffffu, keep);
         if (PASS == 1 && keep) {
           int64_t pos = base + cnt + __popc(b & ((1u << lane) - 1u));
@@ -1045,6 +1083,11 @@ __global__ void __launch_bounds__(WARPS_PER_CTA * 32) k_hbuild(Params P) {
         cnt += __popc(b);
       }
       if (PASS == 0 && lane == 0) P.seg_cnt[P.seg_rowoff[s] + r] = cnt;
+      if (PASS == 2) {
+        const double tot = reduce_scatter8_f64(acc, lane);
+        const int q = lane >> 2;
+        if ((lane & 3) == 0 && q < P.kvec && tot != 0.0) atomicAdd(P.dy + (P.sefoff[I] + r) * P.ldy + q, tot);
+      }
     }
     __syncwarp();
   }
@@ -1730,7 +1773,8 @@ psoci_status run_build(psoci_ctx *c, psoci_hmode mode, int64_t *nnz_out) {
   auto t_b = tnow();
 
   // fast path: only the lower pairs (J <= I) are evaluated; the rest are mirrored
-  const bool fast = c->max_ndet <= FAST_MAXDET;
+  const bool direct = (mode == PSOCI_HMODE_DIRECT);
+  const bool fast = !direct && c->max_ndet <= FAST_MAXDET;
   int64_t nprm = 0;
   if (fast) {
     TRY(psoci_alloc(c, &d_nlow, n + 1));
@@ -1775,7 +1819,28 @@ psoci_status run_build(psoci_ctx *c, psoci_hmode mode, int64_t *nnz_out) {
   int evaluations = 0;
   auto t_c = tnow();
   auto t_d = t_c, t_e = t_c;
-  if (fast) {
+  if (direct) {
+    // direct mode: the diagonal now, the other elements in every sigma; the neighbour lists
+    // and segments move to the context
+    TRY(psoci_alloc(c, &c->d_diag, N));
+    P.diag = c->d_diag;
+    const size_t smem = sizeof(WarpSmem) * WARPS_PER_CTA;
+    TRYC(cudaFuncSetAttribute(k_hbuild<W, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    TRYC(cudaEventRecord(ev[2], st));
+    psoci_note_launch();
+    k_hbuild<W, 3><<<hb_blocks, WARPS_PER_CTA * 32, smem, st>>>(P);
+    TRYC(cudaGetLastError());
+    TRYC(cudaEventRecord(ev[3], st));
+    TRYC(cudaEventRecord(ev[4], st));
+    TRYC(cudaEventRecord(ev[5], st));
+    TRYC(cudaStreamSynchronize(st));
+    c->dir_nbroff = d_nbroff; d_nbroff = nullptr;
+    c->dir_nbr = d_nbr; d_nbr = nullptr;
+    c->dir_segcfg = d_segcfg; d_segcfg = nullptr;
+    c->dir_segk0 = d_segk0; d_segk0 = nullptr;
+    c->dir_segn = d_segn; d_segn = nullptr;
+    c->direct = true;
+  } else if (fast) {
     // 3. evaluate the lower pairs once: kept values go to slab slots, masks to prm
     const size_t smem = sizeof(FastSmem<W>) * WARPS_PER_CTA;
     TRYC(cudaFuncSetAttribute(k_hbuild_fast<W>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -1893,7 +1958,7 @@ psoci_status run_build(psoci_ctx *c, psoci_hmode mode, int64_t *nnz_out) {
   {
     psoci_build_info &b = c->binfo;
     b = psoci_build_info{};
-    b.candidates = ncand; b.pairs = npairs; b.segments = nseg; b.nnz = nnz; b.nnz_lower = (nnz + N) / 2;
+    b.candidates = ncand; b.pairs = npairs; b.segments = nseg; b.nnz = nnz; b.nnz_lower = direct ? 0 : (nnz + N) / 2;
     b.slab_slots = slab_used; b.evaluations = evaluations; b.fast = fast ? 1 : 0;
     b.lookup_screen = c->join_ok ? 1 : 0;
     float ms = 0.f;
@@ -1911,7 +1976,38 @@ psoci_status run_build(psoci_ctx *c, psoci_hmode mode, int64_t *nnz_out) {
 #undef TRYC
 }
 
+template <int W>
+psoci_status run_direct_sigma(psoci_ctx *c, int k, const double *dX, int ldx, double *dY, int ldy) {
+  cudaStream_t st = c->stream;
+  Params P = {};
+  P.nconf = c->nconf; P.nbf = c->nbf; P.nelec = c->nelec; P.ksym = c->ksym;
+  P.e1 = c->d_e1; P.e2 = c->d_e2; P.jsym = c->d_jsym; P.nopen = c->d_nopen;
+  P.sefoff = c->d_sefoff; P.detoff = c->d_detoff;
+  P.alpha = c->d_alpha; P.beta = c->d_beta; P.phase = c->d_phase; P.nalpha = c->d_nalpha;
+  P.one = c->d_one; P.eri = c->d_eri;
+  P.nbroff = c->dir_nbroff; P.nbr = c->dir_nbr;
+  P.nseg = c->nseg; P.seg_cfg = c->dir_segcfg; P.seg_k0 = c->dir_segk0; P.seg_n = c->dir_segn;
+  const int64_t N = c->nsef_total;
+  PSOCI_CUDA(c, cudaMemset2DAsync(dY, sizeof(double) * ldy, 0, sizeof(double) * k, N, st));
+  if (P.nseg == 0) return PSOCI_OK;
+  const size_t smem = sizeof(WarpSmem) * WARPS_PER_CTA;
+  PSOCI_CUDA(c, cudaFuncSetAttribute(k_hbuild<W, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>((P.nseg + WARPS_PER_CTA - 1) / WARPS_PER_CTA, 152 * 16));
+  for (int q0 = 0; q0 < k; q0 += 8) {
+    P.dx = dX + q0; P.dy = dY + q0; P.ldx = ldx; P.ldy = ldy; P.kvec = std::min(8, k - q0);
+    psoci_note_launch();
+    k_hbuild<W, 2><<<blocks, WARPS_PER_CTA * 32, smem, st>>>(P);
+    PSOCI_CUDA(c, cudaGetLastError());
+  }
+  return PSOCI_OK;
+}
+
 }  // namespace
+
+psoci_status psoci_direct_sigma(psoci_ctx *c, int k, const double *dX, int ldx, double *dY, int ldy) {
+  if (!c->direct) return psoci_fail(c, PSOCI_ERR_STATE, "direct sigma: no direct-mode build");
+  return (c->words == 1) ? run_direct_sigma<1>(c, k, dX, ldx, dY, ldy) : run_direct_sigma<2>(c, k, dX, ldx, dY, ldy);
+}
 
 void psoci_join_release(psoci_ctx *c) {
   psoci_free(c->d_jgid);
@@ -2043,6 +2139,12 @@ psoci_status psoci_join_prepare(psoci_ctx *c) {
 }
 
 void psoci_h_release(psoci_ctx *c) {
+  psoci_free(c->dir_nbroff);
+  psoci_free(c->dir_nbr);
+  psoci_free(c->dir_segcfg);
+  psoci_free(c->dir_segk0);
+  psoci_free(c->dir_segn);
+  c->direct = false;
   psoci_free(c->d_rowptr);
   psoci_free(c->d_col);
   psoci_free(c->d_val);

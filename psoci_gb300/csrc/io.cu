@@ -130,6 +130,7 @@ psoci_status psoci_save_hamiltonian(const psoci_ctx *cc, const char *path) {
   psoci_ctx *c = const_cast<psoci_ctx *>(cc);
   if (!c || !path) return PSOCI_ERR_INVALID_ARG;
   if (!c->have_h) return psoci_fail(c, PSOCI_ERR_STATE, "save_hamiltonian: not built");
+  if (c->direct) return psoci_fail(c, PSOCI_ERR_STATE, "save_hamiltonian: direct mode stores no matrix");
   PSOCI_CUDA(c, cudaSetDevice(c->device));
   const int64_t N = c->nsef_total, nnz = c->nnz;
   std::vector<int64_t> rp(N + 1);

@@ -58,6 +58,7 @@ extern "C" psoci_status psoci_sigma_mixed_noalloc(psoci_ctx *c, int k, const dou
                                                   int ldy) {
   if (!c || !dX || !dY) return PSOCI_ERR_INVALID_ARG;
   if (!c->have_h) return psoci_fail(c, PSOCI_ERR_STATE, "sigma_mixed_noalloc: Hamiltonian not built");
+  if (c->direct) return psoci_fail(c, PSOCI_ERR_STATE, "sigma_mixed_noalloc: direct mode stores no matrix");
   if (!c->d_val32)
     return psoci_fail(c, PSOCI_ERR_STATE, "sigma_mixed_noalloc: needs the FP32 copy (PSOCI_HMODE_CSR_BOTH)");
   if (k < 1 || ldx < k || ldy < k) return psoci_fail(c, PSOCI_ERR_INVALID_ARG, "sigma_mixed_noalloc: bad k / ld");

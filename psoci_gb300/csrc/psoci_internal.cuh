@@ -83,6 +83,12 @@ struct psoci_ctx {
   double *d_diag = nullptr;
   double build_seconds = 0.0;
   psoci_build_info binfo{};
+  // direct mode (no stored elements): the screened neighbour lists and their segments
+  bool direct = false;
+  int64_t *dir_nbroff = nullptr;  // [nconf+1]
+  int32_t *dir_nbr = nullptr;     // [npairs]
+  int32_t *dir_segcfg = nullptr, *dir_segn = nullptr;
+  int64_t *dir_segk0 = nullptr;
   int64_t slab_hint = 0;  // value-slab slots the last build of this space used
   int64_t join_hint = 0;  // join-slab slots the last build of this space used
 
@@ -151,6 +157,8 @@ psoci_status psoci_sigma_launch(psoci_ctx *c, int k, const double *dX, int ldx, 
 psoci_status psoci_dets_build(psoci_ctx *c);
 psoci_status psoci_h_build(psoci_ctx *c, psoci_hmode mode, int64_t *nnz);
 psoci_status psoci_h_blocks(psoci_ctx *c, int npairs, const int32_t *A, const int32_t *B, double *out);
+// sigma of a direct-mode build: every element evaluated again (hbuild.cu)
+psoci_status psoci_direct_sigma(psoci_ctx *c, int k, const double *dX, int ldx, double *dY, int ldy);
 psoci_status psoci_join_prepare(psoci_ctx *c);  // after h_occ is set
 void psoci_join_release(psoci_ctx *c);
 void psoci_h_release(psoci_ctx *c);

@@ -326,6 +326,7 @@ psoci_status psoci_sigma_launch(psoci_ctx *c, int k, const double *dX, int ldx, 
     return psoci_fail(c, PSOCI_ERR_INVALID_ARG, "sigma: unknown precision");
   if (!c->have_h) return psoci_fail(c, PSOCI_ERR_STATE, "sigma: Hamiltonian not built");
   if (k < 1 || ldx < k || ldy < k) return psoci_fail(c, PSOCI_ERR_INVALID_ARG, "sigma: bad k / leading dimensions");
+  if (c->direct) return psoci_direct_sigma(c, k, dX, ldx, dY, ldy);
   if (prec == PSOCI_PREC_MIXED && !c->d_val32)
     return psoci_fail(c, PSOCI_ERR_STATE, "sigma: MIXED needs the FP32 copy (PSOCI_HMODE_CSR_BOTH)");
   const int64_t n = c->nsef_total;

@@ -182,3 +182,32 @@ def test_blocks_any_pair(oracle_mod, name, ksym):
     for a, b, g in zip(A, B, got):
         st, ref = O.block(int(a), int(b))
         assert np.abs(g - ref).max() <= H_TOL, (a, b)
+
+
+@pytest.mark.parametrize("kind,kw,ksym", [
+    ("fci", dict(name="fci_6e8o"), 1),
+    ("fci", dict(name="fci_5e6o"), 2),
+    ("mrcisd", dict(nact=6, nelec=4, nvirt=8), 1),
+])
+def test_direct_sigma_matches_stored(oracle_mod, kind, kw, ksym):
+    """Direct mode (no stored elements) against the stored FP64 CSR: same products and
+    diagonal, and the same Davidson roots."""
+    from psoci_gb300 import api
+    from psoci_gb300.inputs import make_problem
+
+    p = small_problem(kw["name"], ksym) if kind == "fci" else make_problem(kind, seed=11, ksym=ksym, **kw)
+    c = _ctx(p)
+    c.build_hamiltonian(mixed=False)
+    d_ref = c.get_diag()
+    X = np.random.default_rng(4).standard_normal((c.nsef, 11))
+    Y_ref = c.sigma(X, prec=api.PREC_FP64)
+    e_ref = c.davidson(4, rtol=1e-8, mixed=False).evals
+    assert c.build_hamiltonian(direct=True) == 0
+    assert np.abs(c.get_diag() - d_ref).max() <= H_TOL
+    for prec in (api.PREC_FP64, api.PREC_MIXED):
+        Y = c.sigma(X, prec=prec)
+        assert np.abs(Y - Y_ref).max() <= SIGMA_RTOL * np.abs(Y_ref).max()
+    e = c.davidson(4, rtol=1e-8, mixed=True).evals
+    assert np.abs(e - e_ref).max() <= EIG_TOL_FP64
+    with pytest.raises(api.PsociError):
+        c.get_hamiltonian()
