@@ -1121,6 +1121,7 @@ struct FastSmem {
   int pre[PSOCI_SEG];
   uint32_t keep[PSOCI_SEG];
   uint64_t cm[PSOCI_SEG];  // connectivity of the row's marked elements (see below)
+  int8_t perm[PSOCI_SEG];  // evaluation order: slot -> neighbour lane, grouped by pair kind
 };
 
 // may det (aA, bA) of A and det (aB, bB) of B have a non-zero element?
@@ -1275,8 +1276,27 @@ __global__ void __launch_bounds__(WARPS_PER_CTA * 32) k_hbuild_fast(Params P) {
     // in chunks and advances through a chunk by the kept count of each row.
     const int64_t prbase = P.pr_off[I] + (k0 - P.nbroff[I]) * nsefI;
     const RowDets rowA = {ws->ra, ws->rb, ws->rph, ws->rna};  // I's determinants (A = I)
+    // evaluation order of the neighbours: grouped by pair kind (doubles, singles, spin-orbit,
+    // diagonal), ascending within a kind, so that neighbouring lanes mostly run the same
+    // branch of the element code.  Values of a row are stored in this order; each pair's
+    // offset in its row run goes to prm, which is all the assembly needs.
+    {
+      const int kd = (lane < n) ? ws->pi[lane].kind : -1;
+      const int key = (kd == K_DOUBLE) ? 0 : (kd == K_SINGLE) ? 1 : (kd == K_SO) ? 2 : (kd == K_DIAG) ? 3
+                                                                                         : (kd == K_NONE) ? 4 : 5;
+      int rank = 0, base = 0;
+#pragma unroll
+      for (int k = 0; k < 6; ++k) {
+        const unsigned m = __ballot_sync(0xffffffffu, key == k);
+        if (key == k) rank = base + __popc(m & ((1u << lane) - 1u));
+        base += __popc(m);
+      }
+      ws->perm[rank] = (int8_t)lane;
+      __syncwarp();
+    }
+    const int src = ws->perm[lane];  // the neighbour lane at evaluation slot `lane`
     for (int r = 0; r < nsefI; ++r) {
-      const uint64_t cr = (lane < n) ? C[r] : 0ull;
+      const uint64_t cr = __shfl_sync(0xffffffffu, (lane < n) ? C[r] : 0ull, src);
       const uint32_t mr = (uint32_t)((cr | (cr >> 16) | (cr >> 32) | (cr >> 48)) & 0xffffull);
       const int cm = __popc(mr);
       int inclm = cm;
@@ -1308,14 +1328,15 @@ __global__ void __launch_bounds__(WARPS_PER_CTA * 32) k_hbuild_fast(Params P) {
         bool keep = false;
         double v = 0.0;
         if (e < T) {
-          int o = 0;  // the neighbour owning element e: last lane whose prefix is <= e
+          int o = 0;  // the slot owning element e: last slot whose prefix is <= e
 #pragma unroll
           for (int step = 16; step > 0; step >>= 1)
             if (ws->pre[o + step] <= e) o += step;
           uint32_t m = ws->mrow[o];
           for (int q = e - ws->pre[o]; q > 0; --q) m &= m - 1;
           const int t = __ffs(m) - 1;
-          const PairInfo &pi = ws->pi[o];
+          const int pl = ws->perm[o];  // its neighbour lane
+          const PairInfo &pi = ws->pi[pl];
           // reference roles: the lower half of a diagonal block, block (J, I) for J > I
           const bool diag_blk = (pi.kind == K_DIAG);
           const bool flip = diag_blk ? (t > r) : (pi.swap != 0);
@@ -1325,7 +1346,7 @@ __global__ void __launch_bounds__(WARPS_PER_CTA * 32) k_hbuild_fast(Params P) {
           if (flip) conn = (conn & 9u) | ((conn & 2u) << 1) | ((conn & 4u) >> 1);
           v = sef_elem<W>(P, pi, ws->K, flip ? t : r, flip ? r : t, conn, &rowA);
           keep = (fabs(v) >= PSOCI_MIN_VALUE) || (diag_blk && t == r);
-          if (keep) atomicOr(&ws->keep[o], 1u << t);
+          if (keep) atomicOr(&ws->keep[pl], 1u << t);
         }
         const unsigned kb = __ballot_sync(0xffffffffu, keep);
         if (keep && fits) P.slab_val[(int64_t)base + kc + __popc(kb & ((1u << lane) - 1u))] = v;
@@ -1333,18 +1354,21 @@ __global__ void __launch_bounds__(WARPS_PER_CTA * 32) k_hbuild_fast(Params P) {
       }
       __syncwarp();
       const uint32_t keepm = (lane < n) ? ws->keep[lane] : 0u;
-      const int c = __popc(keepm);
-      int incl = c;
+      // offsets in the row run follow the evaluation order
+      const int cs = __popc(__shfl_sync(0xffffffffu, keepm, src));
+      int incl = cs;
 #pragma unroll
       for (int o = 1; o < 32; o <<= 1) {
         const int v = __shfl_up_sync(0xffffffffu, incl, o);
         if (lane >= o) incl += v;
       }
+      ws->pre[src] = incl - cs;  // the element loop is done with pre
+      __syncwarp();
       if (lane == 0) {
         P.seg_cnt[P.seg_rowoff[s] + r] = kc;
         P.seg_slot[P.seg_rowoff[s] + r] = (int64_t)base;
       }
-      if (lane < n) P.prm[prbase + (int64_t)lane * nsefI + r] = keepm | ((uint32_t)(incl - c) << 16);
+      if (lane < n) P.prm[prbase + (int64_t)lane * nsefI + r] = keepm | ((uint32_t)ws->pre[lane] << 16);
       cursor += (unsigned long long)kc;
       __syncwarp();
     }
@@ -1411,7 +1435,8 @@ __global__ void k_mirror_count(Params P, int64_t *row_nnz, int32_t *mk, int *err
 // the lane that owns entry e is found by binary search over the per-pair offsets.
 constexpr int ASM_THREADS = 256;
 __global__ void __launch_bounds__(ASM_THREADS) k_assemble(Params P, const int32_t *mk) {
-  __shared__ int s_off[ASM_THREADS / 32][33];     // per lane: first entry of the lane in the run
+  __shared__ int s_off[ASM_THREADS / 32][33];     // per lane: first entry of the lane in the row
+  __shared__ int s_soff[ASM_THREADS / 32][32];    // per lane: its first value in the slab run
   __shared__ uint32_t s_msk[ASM_THREADS / 32][32];  // per lane: columns t of the run, as bits
   __shared__ int32_t s_J[ASM_THREADS / 32][32];
   __shared__ int64_t s_col[ASM_THREADS / 32][32], s_rs[ASM_THREADS / 32][32];
@@ -1440,8 +1465,18 @@ __global__ void __launch_bounds__(ASM_THREADS) k_assemble(Params P, const int32_
         const int cnt = (int)P.seg_cnt[slot];
         const int64_t src0 = P.seg_slot[slot];
         const int64_t dst = __shfl_sync(0xffffffffu, mypos, r);
-        const uint32_t w = (lane < ns) ? pm[r] : ((uint32_t)cnt << 16);
-        s_off[wib][lane] = (int)(w >> 16);
+        // the row takes the pairs in neighbour order; the slab run holds them in the
+        // evaluation order, each pair at its prm offset
+        const uint32_t w = (lane < ns) ? pm[r] : 0u;
+        const int cl = __popc(w & 0xffffu);
+        int incl = cl;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const int v = __shfl_up_sync(0xffffffffu, incl, o);
+          if (lane >= o) incl += v;
+        }
+        s_off[wib][lane] = incl - cl;
+        s_soff[wib][lane] = (int)(w >> 16);
         s_msk[wib][lane] = w & 0xffffu;
         __syncwarp();
         for (int e = lane; e < cnt; e += 32) {
@@ -1452,7 +1487,7 @@ __global__ void __launch_bounds__(ASM_THREADS) k_assemble(Params P, const int32_
           uint32_t m = s_msk[wib][o];
           for (int q = e - s_off[wib][o]; q > 0; --q) m &= m - 1;
           const int t = __ffs(m) - 1;
-          const double v = P.slab_val[src0 + e];
+          const double v = P.slab_val[src0 + s_soff[wib][o] + (e - s_off[wib][o])];
           P.col[dst + e] = (int32_t)(s_col[wib][o] + t);
           P.val[dst + e] = v;
           if (P.val32) P.val32[dst + e] = (float)v;
