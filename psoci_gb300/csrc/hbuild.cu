@@ -61,6 +61,12 @@ struct PairInfo {
   double X[PSOCI_MAX_OPEN];  // single: (iex0 s|s jex0) over the open shells s of A
   uint64_t SA[PSOCI_MAX_WORDS];
   uint64_t SB[PSOCI_MAX_WORDS];  // open shells of B
+  // orbital ranges the determinant phases count electrons over, fixed for the pair:
+  //   K_DOUBLE: 0-3 strictly between ex_i and jy_j (index 2i + j), 4 between ex0 and ex1,
+  //             5 between jy0 and jy1;
+  //   K_SINGLE, K_SO: 0 strictly between ie and je, 1 below ie, 2 above je, 3 below je,
+  //             4 above ie
+  uint64_t bm[6][PSOCI_MAX_WORDS];
 };
 
 struct WarpSmem {
@@ -151,6 +157,31 @@ __device__ __forceinline__ int second_bit(const uint64_t *x) {
   }
   return lowest_bit<W>(y);
 }
+// bits lo..hi inclusive (none when lo > hi) over W words
+template <int W>
+__device__ __forceinline__ void range_mask(int lo, int hi, uint64_t *m) {
+#pragma unroll
+  for (int w = 0; w < W; ++w) {
+    int l = lo - 64 * w, h = hi - 64 * w;
+    if (lo > hi || h < 0 || l > 63) { m[w] = 0ull; continue; }
+    if (l < 0) l = 0;
+    if (h > 63) h = 63;
+    m[w] = (h == 63 ? ~0ull : ((1ull << (h + 1)) - 1ull)) & (~0ull << l);
+  }
+}
+// orbitals strictly between a and b
+template <int W>
+__device__ __forceinline__ void between_mask(int a, int b, uint64_t *m) {
+  range_mask<W>(min(a, b) + 1, max(a, b) - 1, m);
+}
+template <int W>
+__device__ __forceinline__ int popc_and(const uint64_t *x, const uint64_t *m) {
+  int c = 0;
+#pragma unroll
+  for (int w = 0; w < W; ++w) c += __popcll(x[w] & m[w]);
+  return c;
+}
+
 // register-array forms: word selection by value, so that the arrays stay in registers
 template <int W>
 __device__ __forceinline__ bool bit_w(const uint64_t (&x)[W], int p) {
@@ -712,6 +743,11 @@ __device__ void pair_setup_ab(const Params &P, int A, int B, int J, int swap, Pa
     for (int w = 0; w < W; ++w) { im[w] = im1[w] | im2[w]; jm[w] = jm1[w] | jm2[w]; }
     int ie = lowest_bit<W>(im), je = lowest_bit<W>(jm);
     pi.iex0 = ie; pi.jex0 = je;
+    between_mask<W>(ie, je, pi.bm[0]);
+    range_mask<W>(0, ie - 1, pi.bm[1]);
+    range_mask<W>(je + 1, 64 * W - 1, pi.bm[2]);
+    range_mask<W>(0, je - 1, pi.bm[3]);
+    range_mask<W>(ie + 1, 64 * W - 1, pi.bm[4]);
     if (pi.jsA != pi.jsB) {
       // spin-orbit single (PsociHamiltonian.C:223-237): +-SO/2, sign flip if jex > iex
       double v = g1(P, ie, je);
@@ -762,6 +798,12 @@ __device__ void pair_setup_ab(const Params &P, int A, int B, int J, int swap, Pa
     two_positions<W>(jm1, jm2, jy0, jy1);
     const int ex[2] = {ex0, ex1}, jy[2] = {jy0, jy1};
     pi.iex0 = ex0; pi.iex1 = ex1; pi.jex0 = jy0; pi.jex1 = jy1;
+    between_mask<W>(ex0, jy0, pi.bm[0]);
+    between_mask<W>(ex0, jy1, pi.bm[1]);
+    between_mask<W>(ex1, jy0, pi.bm[2]);
+    between_mask<W>(ex1, jy1, pi.bm[3]);
+    between_mask<W>(ex0, ex1, pi.bm[4]);
+    between_mask<W>(jy0, jy1, pi.bm[5]);
     // processDoubleExcitation (PsociHamiltonian.C:180-184)
     double v0 = g2(P, ex[0], jy[0], ex[1], jy[1]);
     double v1 = g2(P, ex[0], jy[1], ex[1], jy[0]);
@@ -821,21 +863,18 @@ __device__ __forceinline__ double det_elem(const double *eri, const PairInfo &pi
     if (nmarka > 1 || nmarkb > 1) return 0.0;
     int ncount = pha + phb;
     if (naa < nab) {
-      ncount += popc_range<W>(ba, 0, ie - 1) + popc_range<W>(ab, je + 1, 64 * W - 1);
+      ncount += popc_and<W>(ba, pi.bm[1]) + popc_and<W>(ab, pi.bm[2]);
       if ((pi.jsA + pi.jsB) % 2 == 0) ++ncount;
       else if (pi.jsA % 2 == 1) ++ncount;
     } else if (naa > nab) {
-      ncount += popc_range<W>(aa, ie + 1, 64 * W - 1) + popc_range<W>(bb, 0, je - 1);
+      ncount += popc_and<W>(aa, pi.bm[4]) + popc_and<W>(bb, pi.bm[3]);
       if ((pi.jsA + pi.jsB) % 2 != 0 && (pi.jsA % 2) == 1) ++ncount;
     } else {
       if (nmarka == 0) ++ncount;
       if (pi.jsA % 2 == 1) ++ncount;
-      if (abs(ie - je) > 1) {
-        int lo = min(ie, je) + 1, hi = max(ie, je) - 1;
-        uint64_t sp[W];
-        sel_w<W>(sp, nmarka != 0, aa, ba);
-        ncount += popc_range<W>(sp, lo, hi);
-      }
+      uint64_t sp[W];
+      sel_w<W>(sp, nmarka != 0, aa, ba);
+      ncount += popc_and<W>(sp, pi.bm[0]);  // empty unless |ie - je| > 1
     }
     return (ncount & 1) ? -pi.v0 : pi.v0;
   }
@@ -866,21 +905,22 @@ __device__ __forceinline__ double det_elem(const double *eri, const PairInfo &pi
     // one spin-orbital excitation within spin (nmarka == 1: alpha, else beta)
     uint64_t sp[W];
     sel_w<W>(sp, nmarka != 0, aa, ba);
-    int ncount = pha + phb;
-    if (abs(ie - je) > 1) ncount += popc_range<W>(sp, min(ie, je) + 1, max(ie, je) - 1);
+    int ncount = pha + phb + popc_and<W>(sp, pi.bm[0]);  // empty unless |ie - je| > 1
     double v = pi.v0;
-    // exchange with the open shells of that spin in det a, except the excited orbitals
+    // exchange with the open shells of that spin in det a, except the excited orbitals, in
+    // ascending orbital order; X is indexed by the rank among A's open shells
+    int t = 0;
 #pragma unroll
     for (int w = 0; w < W; ++w) {
       uint64_t m = sp[w] & ~(aa[w] & ba[w]);
       if ((ie >> 6) == w) m &= ~(1ull << (ie & 63));
       if ((je >> 6) == w) m &= ~(1ull << (je & 63));
-      while (m) {
-        int b = __ffsll((long long)m) - 1;
-        m &= m - 1;
-        int p = 64 * w + b;
-        int t = popc_range<W>(pi.SA, 0, p - 1);
-        v -= pi.X[t];
+      uint64_t sa = pi.SA[w];
+      while (sa) {
+        const uint64_t low = sa & (~sa + 1);
+        if (m & low) v -= pi.X[t];
+        ++t;
+        sa ^= low;
       }
     }
     return (ncount & 1) ? -v : v;
@@ -890,6 +930,15 @@ __device__ __forceinline__ double det_elem(const double *eri, const PairInfo &pi
     uint64_t xa[W], xb[W];
 #pragma unroll
     for (int w = 0; w < W; ++w) { xa[w] = aa[w] & ~ab[w]; xb[w] = ba[w] & ~bb[w]; }
+    if (pi.kind == K_DOUBLE) {
+      // the alpha electron moves ex_ia -> jy_ja, the beta one the other two orbitals (the
+      // same one when a doubly occupied orbital empties or fills); the integral
+      // (beta move | alpha move) is then the table entry of v0 (ia == ja) or v1
+      const int ia = bit_w<W>(xa, pi.iex0) ? 0 : 1, ja = bit_w<W>(ua, pi.jex0) ? 0 : 1;
+      const int ncount = pha + phb + popc_and<W>(aa, pi.bm[2 * ia + ja]) + popc_and<W>(ba, pi.bm[3 - 2 * ia - ja]);
+      const double v = (ia == ja) ? pi.v0 : pi.v1;
+      return (ncount & 1) ? -v : v;
+    }
     int iex2 = lowest_bit<W>(ua), jex2 = lowest_bit<W>(ub);
     int iex3 = lowest_bit<W>(xa), jex3 = lowest_bit<W>(xb);
     int ncount = pha + phb;
@@ -900,13 +949,11 @@ __device__ __forceinline__ double det_elem(const double *eri, const PairInfo &pi
   }
   // same-spin double (nmarka == 2: alpha, nmarka == 0: beta)
   if (pi.kind != K_DOUBLE) return 0.0;
-  uint64_t spb[W], u[W], sa[W];
+  // both electrons of one spin move ex0, ex1 -> jy0, jy1 (distinct orbitals)
+  uint64_t spb[W], sa[W];
   sel_w<W>(spb, nmarka == 2, ab, bb);
-  sel_w<W>(u, nmarka == 2, ua, ub);
   sel_w<W>(sa, nmarka != 0, aa, ba);
-  int u0 = lowest_bit<W>(u), u1 = second_bit<W>(u);
-  int ncount = pha + phb + popc_range<W>(spb, u0 + 1, u1 - 1);
-  if (pi.iex1 - pi.iex0 > 1) ncount += popc_range<W>(sa, pi.iex0 + 1, pi.iex1 - 1);
+  int ncount = pha + phb + popc_and<W>(spb, pi.bm[5]) + popc_and<W>(sa, pi.bm[4]);
   double v = pi.v0 - pi.v1;
   return (ncount & 1) ? -v : v;
 }
