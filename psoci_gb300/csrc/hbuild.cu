@@ -840,6 +840,40 @@ __device__ __forceinline__ void load_det(DetBits<W> &d, const uint64_t *alpha, c
   d.na = nalpha[i];
 }
 
+// Diagonal element of a determinant (processDiagExcitation's vnt list): Kd[0] minus the
+// exchange integral of every pair of open shells (io > jo, in the reference's order) whose
+// spins agree.  Out of line: it runs for the diagonal blocks only, and keeping its loops out
+// of the element code keeps that code compact.
+template <int W>
+__device__ __noinline__ double diag_det_elem(const uint64_t *SA, const double *Kd, const uint64_t (&aa)[W]) {
+  double v = Kd[0];
+  int mm = 0, io = 0;
+#pragma unroll
+  for (int wi = 0; wi < W; ++wi) {
+    uint64_t si_bits = SA[wi];
+    while (si_bits) {
+      const uint64_t lo_i = si_bits & (~si_bits + 1);
+      si_bits ^= lo_i;
+      const bool si = (aa[wi] & lo_i) != 0ull;
+      // open shells below this one, ascending
+      int jo = 0;
+#pragma unroll
+      for (int wj = 0; wj < W; ++wj) {
+        uint64_t sj = SA[wj];
+        while (sj && jo < io) {
+          const uint64_t lo_j = sj & (~sj + 1);
+          sj ^= lo_j;
+          ++mm;
+          if (si == ((aa[wj] & lo_j) != 0ull)) v -= Kd[mm];
+          ++jo;
+        }
+      }
+      ++io;
+    }
+  }
+  return v;
+}
+
 // <det a of A | H | det b of B> from the loaded determinants.  sef_elem calls it from a
 // single site (a loop over the determinant pairs of an SEF element), so the kernels hold
 // one copy of this body: several inlined copies overflow their instruction cache.
@@ -884,22 +918,7 @@ __device__ __forceinline__ double det_elem(const double *eri, const PairInfo &pi
   if (nmarka > 2 || nmarkb > 2) return 0.0;
   if (nmarkb == 0) {
     if (pi.kind != K_DIAG) return 0.0;  // identical determinants occur only on the diagonal
-    double v = Kd[0];
-    int sing[PSOCI_MAX_OPEN], ns = 0;
-#pragma unroll
-    for (int w = 0; w < W; ++w) {
-      uint64_t s = pi.SA[w];
-      while (s && ns < PSOCI_MAX_OPEN) { sing[ns++] = 64 * w + __ffsll((long long)s) - 1; s &= s - 1; }
-    }
-    int mm = 0;
-    for (int io = 1; io < ns; ++io) {
-      bool si = bit_w<W>(aa, sing[io]);
-      for (int jo = 0; jo < io; ++jo) {
-        ++mm;
-        if (si == bit_w<W>(aa, sing[jo])) v -= Kd[mm];
-      }
-    }
-    return v;
+    return diag_det_elem<W>(pi.SA, Kd, aa);
   }
   if (nmarkb == 1) {
     // one spin-orbital excitation within spin (nmarka == 1: alpha, else beta)
