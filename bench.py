@@ -33,7 +33,7 @@ sys.path.insert(0, ROOT)
 # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) from ncu captures of
 # a smaller case of the same space, scaled to the full launch by the units processed; the
 # captures and the scaling are summarised under profiles/.
-TRAFFIC = {("k_hbuild_fast", "mrcisd_6e8o_v64"): 2.00e10, ("k_spmm_mixed", "mrcisd_6e8o_v64"): 1.91e10}
+TRAFFIC = {("k_hbuild_fast", "mrcisd_6e8o_v64"): 1.76e10, ("k_spmm_mixed", "mrcisd_6e8o_v64"): 1.91e10}
 
 NROOTS = 8
 RTOL = 1e-5          # residual norm; |dE| ~ r^2/gap, well inside 1e-7 Eh (checked below)
@@ -467,7 +467,7 @@ def main():
     ap.add_argument("--workload", default="mrcisd_6e8o_v64")
     ap.add_argument("--ksym", type=int, default=1)
     ap.add_argument("--seed", type=int, default=1)
-    ap.add_argument("--max-subspace", type=int, default=48)
+    ap.add_argument("--max-subspace", type=int, default=40)
     ap.add_argument("--cpu-sample", type=int, default=20000, help="configurations in the CPU sigma sample")
     ap.add_argument("--cpu-rows", type=int, default=8000, help="random row configurations in the CPU build sample")
     ap.add_argument("--cpu-density-rows", type=int, default=48, help="random rows in the CPU density sample")
