@@ -40,6 +40,9 @@ constexpr int MAX_SUB = 96;       // Jacobi keeps two m x m FP64 matrices in sha
 // these products are FP64-bound.  Block partials are combined in FP64.
 
 // C_partial[blk][i*k + j] = sum over the block's rows of A[r, a0+i] * B[r, b0+j]
+// LOWP (the FP32-element phase of a mixed solve, whose sigma is good to ~1e-7 anyway): FP32
+// products summed in FP32 over a tile of 32 rows, tile sums added in float-float.
+template <bool LOWP>
 __global__ void __launch_bounds__(TN_THREADS) k_tn(int64_t n, const double *__restrict__ A, int lda, int a0, int m,
                                                    const double *__restrict__ B, int ldb, int b0, int k,
                                                    double *__restrict__ partial, int64_t rows_per_blk) {
@@ -73,7 +76,13 @@ __global__ void __launch_bounds__(TN_THREADS) k_tn(int64_t n, const double *__re
         if (idx < nout) {
           int i = idx / k, j = idx - i * k;
           float h = sh[o], l = sl[o];
-          for (int rr = 0; rr < rows; ++rr) ff_fma(h, l, As[rr * m + i], Bs[rr * k + j]);
+          if (LOWP) {
+            float t = 0.f;
+            for (int rr = 0; rr < rows; ++rr) t = __fmaf_rn(As[rr * m + i].x, Bs[rr * k + j].x, t);
+            ff_fma(h, l, make_float2(t, 0.f), make_float2(1.f, 0.f));
+          } else {
+            for (int rr = 0; rr < rows; ++rr) ff_fma(h, l, As[rr * m + i], Bs[rr * k + j]);
+          }
           ff_renorm(h, l);
           sh[o] = h;
           sl[o] = l;
@@ -82,7 +91,13 @@ __global__ void __launch_bounds__(TN_THREADS) k_tn(int64_t n, const double *__re
     } else if (sub < S) {
       const int idx = (int)threadIdx.x - sub * nout, i = idx / k, j = idx - i * k;
       float h = sh[0], l = sl[0];
-      for (int rr = sub; rr < rows; rr += S) ff_fma(h, l, As[rr * m + i], Bs[rr * k + j]);
+      if (LOWP) {
+        float t = 0.f;
+        for (int rr = sub; rr < rows; rr += S) t = __fmaf_rn(As[rr * m + i].x, Bs[rr * k + j].x, t);
+        ff_fma(h, l, make_float2(t, 0.f), make_float2(1.f, 0.f));
+      } else {
+        for (int rr = sub; rr < rows; rr += S) ff_fma(h, l, As[rr * m + i], Bs[rr * k + j]);
+      }
       ff_renorm(h, l);
       sh[0] = h;
       sl[0] = l;
@@ -108,19 +123,32 @@ __global__ void __launch_bounds__(TN_THREADS) k_tn(int64_t n, const double *__re
   }
 }
 
-// C[i*ldc + c0 + j] = sum_b partial[b][i*k + j]   (fixed order: deterministic)
+// C[i*ldc + c0 + j] = sum_b partial[b][i*k + j]   (fixed order: deterministic).  One block
+// per group of 32 outputs; its warps sum interleaved slices of the partials (coalesced along
+// the outputs) and one warp adds the slices in warp order.
 __global__ void k_reduce_partials(const double *__restrict__ partial, int nblk, int m, int k, double *C, int ldc,
                                   int c0) {
-  int idx = blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= m * k) return;
+  __shared__ double red[8][32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;  // blockDim.x == 256
+  const int nout = m * k;
+  const int idx = blockIdx.x * 32 + lane;
   double s = 0.0;
-  for (int b = 0; b < nblk; ++b) s += partial[(int64_t)b * m * k + idx];
-  int i = idx / k, j = idx - i * k;
-  C[i * ldc + c0 + j] = s;
+  if (idx < nout)
+    for (int b = wid; b < nblk; b += 8) s += partial[(int64_t)b * nout + idx];
+  red[wid][lane] = s;
+  __syncthreads();
+  if (wid == 0 && idx < nout) {
+    double t = 0.0;
+    for (int w = 0; w < 8; ++w) t += red[w][lane];
+    const int i = idx / k, j = idx - i * k;
+    C[i * ldc + c0 + j] = t;
+  }
 }
 
 // Out[r, o0+j] = beta*Out[r, o0+j] + alpha * sum_i A[r, a0+i] * Y[i*ldy + y0 + j]
-// (float-float sums as in k_tn; alpha, beta and the update of Out in FP64)
+// (float-float sums as in k_tn, or FP32 sums when LOWP; alpha, beta and the update of Out
+// in FP64)
+template <bool LOWP>
 __global__ void __launch_bounds__(NN_THREADS) k_nn(int64_t n, const double *__restrict__ A, int lda, int a0, int m,
                                                    const double *__restrict__ Y, int ldy, int y0, int k, double alpha,
                                                    double beta, double *Out, int ldo, int o0) {
@@ -142,9 +170,16 @@ __global__ void __launch_bounds__(NN_THREADS) k_nn(int64_t n, const double *__re
     for (int e = threadIdx.x; e < 32 * k; e += blockDim.x) {
       int rr = e / k, j = e - rr * k;
       if (rr < rows) {
-        float h = 0.f, l = 0.f;
-        for (int i = 0; i < m; ++i) ff_fma(h, l, As[rr * m + i], Ys[i * k + j]);
-        const double s = (double)h + (double)l;
+        double s;
+        if (LOWP) {
+          float t = 0.f;
+          for (int i = 0; i < m; ++i) t = __fmaf_rn(As[rr * m + i].x, Ys[i * k + j].x, t);
+          s = (double)t;
+        } else {
+          float h = 0.f, l = 0.f;
+          for (int i = 0; i < m; ++i) ff_fma(h, l, As[rr * m + i], Ys[i * k + j]);
+          s = (double)h + (double)l;
+        }
         double *o = Out + (rt + rr) * ldo + o0 + j;
         *o = (beta == 0.0) ? alpha * s : fma(beta, *o, alpha * s);
       }
@@ -153,26 +188,40 @@ __global__ void __launch_bounds__(NN_THREADS) k_nn(int64_t n, const double *__re
   }
 }
 
-// R[r, j] = HX[r, j] - theta[j] * X[r, j]; partial squared norms per block
+// R[r, j] = HX[r, j] - theta[j] * X[r, j]; partial squared norms per block.  A thread takes
+// whole rows (the nr values of a row are contiguous), so each row is read once.
 __global__ void k_residual(int64_t n, int nr, const double *__restrict__ X, const double *__restrict__ HX,
                            const double *__restrict__ theta, double *__restrict__ R, double *__restrict__ partial) {
-  __shared__ double red[256];
-  for (int j = 0; j < nr; ++j) {
-    double th = theta[j];
-    double s = 0.0;
-    for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
-      double v = HX[r * nr + j] - th * X[r * nr + j];
+  __shared__ double red[16][8];  // [root][warp], blockDim.x == 256
+  double th[16], s[16];
+#pragma unroll
+  for (int j = 0; j < 16; ++j) {
+    th[j] = (j < nr) ? theta[j] : 0.0;
+    s[j] = 0.0;
+  }
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+#pragma unroll
+    for (int j = 0; j < 16; ++j) {
+      if (j >= nr) break;
+      const double v = HX[r * nr + j] - th[j] * X[r * nr + j];
       R[r * nr + j] = v;
-      s = fma(v, v, s);
+      s[j] = fma(v, v, s[j]);
     }
-    red[threadIdx.x] = s;
-    __syncthreads();
-    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
-      if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
-      __syncthreads();
-    }
-    if (threadIdx.x == 0) partial[(int64_t)blockIdx.x * nr + j] = red[0];
-    __syncthreads();
+  }
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int j = 0; j < 16; ++j) {
+    if (j >= nr) break;
+    double v = s[j];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0) red[j][wid] = v;
+  }
+  __syncthreads();
+  if ((int)threadIdx.x < nr) {
+    double t = 0.0;
+    for (int w = 0; w < 8; ++w) t += red[threadIdx.x][w];
+    partial[(int64_t)blockIdx.x * nr + threadIdx.x] = t;
   }
 }
 
@@ -409,6 +458,11 @@ struct Work {
   int64_t *idx = nullptr;
   int nblk = 0;
   int64_t rows_per_blk = 0;
+  // FP32 subspace products allowed (the FP32-element phase of a mixed solve): used for the
+  // orthonormalisation and the new columns of G, whose errors (~1e-7) stay below what that
+  // phase resolves; Ritz vectors, their images and collapses keep float-float sums, since
+  // the residuals are formed from them
+  bool lowp = false;
   std::vector<cudaEvent_t> ev;
   ~Work() {
     psoci_free(V); psoci_free(HV); psoci_free(G); psoci_free(Y); psoci_free(theta); psoci_free(X); psoci_free(HX);
@@ -420,26 +474,35 @@ struct Work {
 
 // C (ldc, column offset c0) = A[:, a0:a0+m]^T B[:, b0:b0+k]
 psoci_status tn(Work &w, const double *A, int lda, int a0, int m, const double *B, int ldb, int b0, int k, double *C,
-                int ldc, int c0) {
+                int ldc, int c0, bool lowp_ok = false) {
+  const bool lowp = w.lowp && lowp_ok;
   psoci_ctx *c = w.c;
   if (m * k > TN_THREADS * TN_MAXOUT) return psoci_fail(c, PSOCI_ERR_INVALID_ARG, "tn: block too large");
   size_t smem = sizeof(double) * std::max(TN_ROWS * (m + k), TN_THREADS);
   psoci_note_launch();
-  k_tn<<<w.nblk, TN_THREADS, smem, c->stream>>>(w.N, A, lda, a0, m, B, ldb, b0, k, w.partial, w.rows_per_blk);
+  if (lowp)
+    k_tn<true><<<w.nblk, TN_THREADS, smem, c->stream>>>(w.N, A, lda, a0, m, B, ldb, b0, k, w.partial, w.rows_per_blk);
+  else
+    k_tn<false><<<w.nblk, TN_THREADS, smem, c->stream>>>(w.N, A, lda, a0, m, B, ldb, b0, k, w.partial, w.rows_per_blk);
   psoci_note_launch();
-  k_reduce_partials<<<(m * k + 127) / 128, 128, 0, c->stream>>>(w.partial, w.nblk, m, k, C, ldc, c0);
+  k_reduce_partials<<<(m * k + 31) / 32, 256, 0, c->stream>>>(w.partial, w.nblk, m, k, C, ldc, c0);
   PSOCI_CUDA(c, cudaGetLastError());
   return PSOCI_OK;
 }
 
 psoci_status nn(Work &w, const double *A, int lda, int a0, int m, const double *Y, int ldy, int y0, int k, double alpha,
-                double beta, double *Out, int ldo, int o0) {
+                double beta, double *Out, int ldo, int o0, bool lowp_ok = false) {
+  const bool lowp = w.lowp && lowp_ok;
   psoci_ctx *c = w.c;
   size_t smem = sizeof(double) * (m * k + 32 * m);
   int blocks = (int)std::min<int64_t>((w.N + 31) / 32, 152 * 8);
   psoci_note_launch();
-  k_nn<<<std::max(blocks, 1), NN_THREADS, smem, c->stream>>>(w.N, A, lda, a0, m, Y, ldy, y0, k, alpha, beta, Out, ldo,
-                                                             o0);
+  if (lowp)
+    k_nn<true><<<std::max(blocks, 1), NN_THREADS, smem, c->stream>>>(w.N, A, lda, a0, m, Y, ldy, y0, k, alpha, beta,
+                                                                     Out, ldo, o0);
+  else
+    k_nn<false><<<std::max(blocks, 1), NN_THREADS, smem, c->stream>>>(w.N, A, lda, a0, m, Y, ldy, y0, k, alpha, beta,
+                                                                      Out, ldo, o0);
   PSOCI_CUDA(c, cudaGetLastError());
   return PSOCI_OK;
 }
@@ -465,18 +528,18 @@ psoci_status orthonormalize(Work &w, int m, int b, int *bk) {
   // squared norms before the projection: a column that loses all but 1e-10 of its norm
   // against V (or the block's earlier columns) carries no new direction and is dropped
   double *ref = w.small + (size_t)ld * ld / 2;
-  if ((s = tn(w, w.T, tld, 0, b, w.T, tld, 0, b, ref, b, 0))) return s;
+  if ((s = tn(w, w.T, tld, 0, b, w.T, tld, 0, b, ref, b, 0, true))) return s;
   for (int pass = 0; pass < 2 && m > 0; ++pass) {
     // C = V^T T (m x b) into w.small (ld = b), T -= V C
-    if ((s = tn(w, w.V, ld, 0, m, w.T, tld, 0, b, w.small, b, 0))) return s;
-    if ((s = nn(w, w.V, ld, 0, m, w.small, b, 0, b, -1.0, 1.0, w.T, tld, 0))) return s;
+    if ((s = tn(w, w.V, ld, 0, m, w.T, tld, 0, b, w.small, b, 0, true))) return s;
+    if ((s = nn(w, w.V, ld, 0, m, w.small, b, 0, b, -1.0, 1.0, w.T, tld, 0, true))) return s;
   }
   // Cholesky-QR twice: first into tmp, then into V[:, m:]
   int nk = b;
   for (int pass = 0; pass < 2; ++pass) {
     const double *src = (pass == 0) ? w.T : w.tmp;
     int srcld = (pass == 0) ? tld : w.nr;
-    if ((s = tn(w, src, srcld, 0, nk, src, srcld, 0, nk, w.small, nk, 0))) return s;
+    if ((s = tn(w, src, srcld, 0, nk, src, srcld, 0, nk, w.small, nk, 0, true))) return s;
     psoci_note_launch();
     k_cholqr_factor<<<1, 32, 0, c->stream>>>(w.small, nk, pass == 0 ? ref : nullptr, b, 1e-10, w.F, w.ibuf);
     PSOCI_CUDA(c, cudaGetLastError());
@@ -485,9 +548,9 @@ psoci_status orthonormalize(Work &w, int m, int b, int *bk) {
     PSOCI_CUDA(c, cudaStreamSynchronize(c->stream));
     if (nk2 == 0) { *bk = 0; return PSOCI_OK; }
     if (pass == 0) {
-      if ((s = nn(w, w.T, tld, 0, nk, w.F, nk, 0, nk2, 1.0, 0.0, w.tmp, w.nr, 0))) return s;
+      if ((s = nn(w, w.T, tld, 0, nk, w.F, nk, 0, nk2, 1.0, 0.0, w.tmp, w.nr, 0, true))) return s;
     } else {
-      if ((s = nn(w, w.tmp, w.nr, 0, nk, w.F, nk, 0, nk2, 1.0, 0.0, w.V, ld, m))) return s;
+      if ((s = nn(w, w.tmp, w.nr, 0, nk, w.F, nk, 0, nk2, 1.0, 0.0, w.V, ld, m, true))) return s;
     }
     nk = nk2;
   }
@@ -541,8 +604,10 @@ psoci_status psoci_davidson_impl(psoci_ctx *c, const psoci_dav_opts *o, double *
   cudaStream_t st = c->stream;
   const size_t jac_smem = sizeof(double) * 2 * MAX_SUB * MAX_SUB;
   PSOCI_CUDA(c, cudaFuncSetAttribute(k_jacobi, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)jac_smem));
-  PSOCI_CUDA(c, cudaFuncSetAttribute(k_nn, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024));
-  PSOCI_CUDA(c, cudaFuncSetAttribute(k_tn, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024));
+  PSOCI_CUDA(c, cudaFuncSetAttribute(k_nn<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024));
+  PSOCI_CUDA(c, cudaFuncSetAttribute(k_tn<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024));
+  PSOCI_CUDA(c, cudaFuncSetAttribute(k_nn<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024));
+  PSOCI_CUDA(c, cudaFuncSetAttribute(k_tn<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024));
   PSOCI_CUDA(c, cudaMemsetAsync(w.V, 0, sizeof(double) * N * ld, st));
   PSOCI_CUDA(c, cudaMemsetAsync(w.G, 0, sizeof(double) * ld * ld, st));
 
@@ -556,6 +621,7 @@ psoci_status psoci_davidson_impl(psoci_ctx *c, const psoci_dav_opts *o, double *
                     [&](int64_t a, int64_t b) { return hdiag[a] < hdiag[b] || (hdiag[a] == hdiag[b] && a < b); });
   psoci_prec prec = o->prec;
   bool refine_phase = (prec != PSOCI_PREC_MIXED);  // FP64 and FF iterate to rtol directly
+  w.lowp = (prec == PSOCI_PREC_MIXED);
   const double tol_mixed = std::max(rtol, 1e-5);
   int m = nr;
   if (c->guess_k > 0 && (int64_t)c->guess.size() == (int64_t)c->guess_k * N) {
@@ -629,6 +695,7 @@ psoci_status psoci_davidson_impl(psoci_ctx *c, const psoci_dav_opts *o, double *
         // FP64 refinement: restart from the Ritz vectors with exact (FP64) H products
         refine_phase = true;
         prec = (o->refine == 2) ? PSOCI_PREC_FP64 : PSOCI_PREC_FF;
+        w.lowp = false;
         if ((s = nn(w, w.V, ld, 0, m, w.Y, ld, 0, nr, 1.0, 0.0, w.T, nr, 0))) return s;
         int bk = 0;
         if ((s = orthonormalize(w, 0, nr, &bk))) return s;
@@ -670,7 +737,7 @@ psoci_status psoci_davidson_impl(psoci_ctx *c, const psoci_dav_opts *o, double *
     if (bk == 0) { result = PSOCI_ERR_NOT_CONVERGED; break; }
     if ((s = sigma_block(w, w.V + m, ld, w.HV + m, ld, bk, prec))) return s;
     sigma_calls += bk;
-    if ((s = tn(w, w.V, ld, 0, m + bk, w.HV, ld, m, bk, w.G, ld, m))) return s;
+    if ((s = tn(w, w.V, ld, 0, m + bk, w.HV, ld, m, bk, w.G, ld, m, true))) return s;
     psoci_note_launch();
     k_symmetrize<<<1, 256, 0, st>>>(w.G, ld, m, m + bk);
     PSOCI_CUDA(c, cudaGetLastError());
