@@ -32,6 +32,7 @@ def nvcc() -> str:
 def _compile(src: str, extra: list[str]) -> str:
     obj = os.path.join(LIBDIR, os.path.splitext(src)[0] + ".o")
     cmd = [nvcc(), ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden",
+           "-Xcompiler", "-pthread",
            "-I" + CSRC, "-c", os.path.join(CSRC, src), "-o", obj] + PER_FILE.get(src, []) + extra
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
@@ -60,7 +61,7 @@ def build(force: bool = False, extra: list[str] | None = None, verbose: bool = F
     with cf.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
         objs = list(ex.map(lambda s: _compile(s, extra), SOURCES))
     tmp = LIB + ".tmp"
-    cmd = [nvcc(), ARCH, "-shared", "-o", tmp] + objs
+    cmd = [nvcc(), ARCH, "-shared", "-Xcompiler", "-pthread", "-o", tmp] + objs
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")

@@ -127,29 +127,43 @@ psoci_status psoci_set_configs(psoci_ctx *c, int nbf, int nelec, int ksym, int m
   const int W = (nbf + 63) / 64;
   std::vector<uint64_t> e1((size_t)nconf * W, 0), e2((size_t)nconf * W, 0);
   std::vector<int32_t> nopen(nconf);
-  for (int i = 0; i < nconf; ++i) {
-    const uint8_t *o = occ + (size_t)i * nbf;
-    int ne = 0, no = 0;
-    for (int p = 0; p < nbf; ++p) {
-      if (o[p] > 2) {
-        char b[128];
-        snprintf(b, sizeof(b), "set_configs: configuration %d orbital %d occupation %d", i, p, (int)o[p]);
-        return psoci_fail(c, PSOCI_ERR_INVALID_ARG, b);
-      }
-      ne += o[p];
-      no += (o[p] == 1);
-      if (o[p] >= 1) e1[(size_t)i * W + p / 64] |= 1ull << (p % 64);
-      if (o[p] == 2) e2[(size_t)i * W + p / 64] |= 1ull << (p % 64);
-    }
-    if (ne != nelec) {
+  // bit-planes and checks on the host's cores; each range keeps its first failing
+  // configuration, and the lowest one is reported, with the serial loop's message
+  struct Bad {
+    int i = -1;
+    psoci_status st = PSOCI_OK;
+    std::string msg;
+  };
+  std::vector<Bad> bad(std::max<unsigned>(1u, std::thread::hardware_concurrency()));
+  const int nthr = psoci_parallel_ranges(nconf, [&](int64_t lo, int64_t hi, int t) {
+    for (int64_t ii = lo; ii < hi; ++ii) {
+      const int i = (int)ii;
+      const uint8_t *o = occ + (size_t)i * nbf;
+      int ne = 0, no = 0;
       char b[128];
-      snprintf(b, sizeof(b), "set_configs: configuration %d holds %d electrons, expected %d", i, ne, nelec);
-      return psoci_fail(c, PSOCI_ERR_INVALID_ARG, b);
+      for (int p = 0; p < nbf; ++p) {
+        if (o[p] > 2) {
+          snprintf(b, sizeof(b), "set_configs: configuration %d orbital %d occupation %d", i, p, (int)o[p]);
+          bad[t] = {i, PSOCI_ERR_INVALID_ARG, b};
+          return;
+        }
+        ne += o[p];
+        no += (o[p] == 1);
+        if (o[p] >= 1) e1[(size_t)i * W + p / 64] |= 1ull << (p % 64);
+        if (o[p] == 2) e2[(size_t)i * W + p / 64] |= 1ull << (p % 64);
+      }
+      if (ne != nelec) {
+        snprintf(b, sizeof(b), "set_configs: configuration %d holds %d electrons, expected %d", i, ne, nelec);
+        bad[t] = {i, PSOCI_ERR_INVALID_ARG, b};
+        return;
+      }
+      if (no > PSOCI_MAX_OPEN) { bad[t] = {i, PSOCI_ERR_UNSUPPORTED, "set_configs: more than 11 open shells"}; return; }
+      if (jsym[i] < 1) { bad[t] = {i, PSOCI_ERR_INVALID_ARG, "set_configs: jsym labels are 1-based"}; return; }
+      nopen[i] = no;
     }
-    if (no > PSOCI_MAX_OPEN) return psoci_fail(c, PSOCI_ERR_UNSUPPORTED, "set_configs: more than 11 open shells");
-    if (jsym[i] < 1) return psoci_fail(c, PSOCI_ERR_INVALID_ARG, "set_configs: jsym labels are 1-based");
-    nopen[i] = no;
-  }
+  });
+  for (int t = 0; t < nthr; ++t)
+    if (bad[t].i >= 0) return psoci_fail(c, bad[t].st, bad[t].msg);  // ranges ascend: the first is the lowest
   psoci_status s;
   if ((s = set_device(c))) return s;
   psoci_h_release(c);

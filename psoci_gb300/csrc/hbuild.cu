@@ -2131,37 +2131,51 @@ psoci_status psoci_join_prepare(psoci_ctx *c) {
   const int n = c->nconf, nbf = c->nbf;
   const uint8_t *occ = c->h_occ.data();
   // split: orbitals >= s hold at most two electrons in every configuration
-  int s = 0;
-  for (int i = 0; i < n; ++i) {
-    const uint8_t *o = occ + (size_t)i * nbf;
-    int e = 0, si = 0;
-    for (int q = nbf - 1; q >= 0; --q) {
-      e += o[q];
-      if (e >= 3) { si = q + 1; break; }
+  // (the configuration loops run on the host's cores; only the numbering of lo patterns by
+  // first appearance is sequential)
+  std::vector<int> smax(std::max<unsigned>(1u, std::thread::hardware_concurrency()), 0);
+  const int nthr = psoci_parallel_ranges(n, [&](int64_t lo, int64_t hi, int t) {
+    int sm = 0;
+    for (int64_t i = lo; i < hi; ++i) {
+      const uint8_t *o = occ + (size_t)i * nbf;
+      int e = 0, si = 0;
+      for (int q = nbf - 1; q >= 0; --q) {
+        e += o[q];
+        if (e >= 3) { si = q + 1; break; }
+      }
+      sm = std::max(sm, si);
     }
-    s = std::max(s, si);
-  }
+    smax[t] = sm;
+  });
+  int s = 0;
+  for (int t = 0; t < nthr; ++t) s = std::max(s, smax[t]);
   const int nh = nbf - s;
   if (s > 12 || nh < 1) return PSOCI_OK;
   const int64_t G = 1 + nh + (int64_t)nh * (nh + 1) / 2;
   std::vector<int32_t> gid(n), lid(n), keyid((size_t)1 << (2 * s), -1);
-  std::vector<uint32_t> lokey;
+  std::vector<uint32_t> lokey, keys(n);
+  psoci_parallel_ranges(n, [&](int64_t lo, int64_t hi, int) {
+    for (int64_t i = lo; i < hi; ++i) {
+      const uint8_t *o = occ + (size_t)i * nbf;
+      uint32_t key = 0;
+      for (int q = 0; q < s; ++q) {
+        if (o[q] >= 1) key |= 1u << q;
+        if (o[q] == 2) key |= 1u << (s + q);
+      }
+      int pa = -1, pb = -1, kind = 0;
+      for (int q = s; q < nbf; ++q) {
+        if (o[q] == 0) continue;
+        if (o[q] == 2) { kind = 3; pa = q - s; }
+        else if (pa < 0) { kind = 1; pa = q - s; }
+        else { kind = 2; pb = q - s; }
+      }
+      gid[i] = (kind == 0) ? 0 : (kind == 1) ? 1 + pa
+               : (int32_t)(1 + nh + (kind == 3 ? (int64_t)pa * (pa + 1) / 2 + pa : (int64_t)pb * (pb + 1) / 2 + pa));
+      keys[i] = key;
+    }
+  });
   for (int i = 0; i < n; ++i) {
-    const uint8_t *o = occ + (size_t)i * nbf;
-    uint32_t key = 0;
-    for (int q = 0; q < s; ++q) {
-      if (o[q] >= 1) key |= 1u << q;
-      if (o[q] == 2) key |= 1u << (s + q);
-    }
-    int pa = -1, pb = -1, kind = 0;
-    for (int q = s; q < nbf; ++q) {
-      if (o[q] == 0) continue;
-      if (o[q] == 2) { kind = 3; pa = q - s; }
-      else if (pa < 0) { kind = 1; pa = q - s; }
-      else { kind = 2; pb = q - s; }
-    }
-    gid[i] = (kind == 0) ? 0 : (kind == 1) ? 1 + pa
-             : (int32_t)(1 + nh + (kind == 3 ? (int64_t)pa * (pa + 1) / 2 + pa : (int64_t)pb * (pb + 1) / 2 + pa));
+    const uint32_t key = keys[i];
     if (keyid[key] < 0) { keyid[key] = (int32_t)lokey.size(); lokey.push_back(key); }
     lid[i] = keyid[key];
     if (i > 0 && gid[i] < gid[i - 1]) return PSOCI_OK;  // hi patterns must ascend

@@ -3,7 +3,9 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <algorithm>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/psoci_gpu.h"
@@ -115,6 +117,24 @@ struct psoci_ctx {
   float *d_x32 = nullptr;
   size_t x32_cap = 0;
 };
+
+// host loops over configurations: f(lo, hi, t) on contiguous ranges of [0, n), one thread
+// per host core (ranges of at least 16384), t = 0..threads-1; returns the thread count
+template <class F>
+int psoci_parallel_ranges(int64_t n, F &&f) {
+  int nt = (int)std::thread::hardware_concurrency();
+  if (nt < 1) nt = 1;
+  nt = (int)std::min<int64_t>(nt, std::max<int64_t>(1, n / 16384));
+  if (nt <= 1) {
+    f((int64_t)0, n, 0);
+    return 1;
+  }
+  std::vector<std::thread> th;
+  th.reserve(nt);
+  for (int t = 0; t < nt; ++t) th.emplace_back([&f, n, nt, t]() { f(n * t / nt, n * (t + 1) / nt, t); });
+  for (auto &x : th) x.join();
+  return nt;
+}
 
 // error helpers -----------------------------------------------------------------------
 psoci_status psoci_fail(psoci_ctx *c, psoci_status s, const std::string &msg);

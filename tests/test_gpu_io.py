@@ -125,3 +125,25 @@ def test_bad_inputs_rejected():
             c.set_configs(p.nbf, p.nelec + 1, p.ksym, p.mx_open, p.jsym, p.occ)
         with pytest.raises(api.PsociError):  # sigma before any H
             c.sigma(np.zeros((3, 1)))
+
+
+def test_bad_inputs_reported_in_order_on_large_lists():
+    """Large configuration lists are checked on all host cores; the lowest failing
+    configuration is the one reported, with its own message."""
+    from psoci_gb300 import api
+    from psoci_gb300.inputs import named_workload
+
+    p = named_workload("mrcisd_6e8o_v16", seed=1, ksym=1)
+    assert p.nconf > 40000
+    with api.Context(0) as c:
+        occ = p.occ.copy()
+        occ[40000, 3] = 3
+        nel = occ[30001].astype(int)
+        q = int(np.nonzero(nel == 0)[0][0])
+        occ[30001, q] = 1  # one electron too many
+        with pytest.raises(api.PsociError, match="configuration 30001 holds"):
+            c.set_configs(p.nbf, p.nelec, p.ksym, p.mx_open, p.jsym, occ)
+        occ[30001, q] = 0
+        with pytest.raises(api.PsociError, match="configuration 40000 orbital 3 occupation 3"):
+            c.set_configs(p.nbf, p.nelec, p.ksym, p.mx_open, p.jsym, occ)
+        c.set_configs(p.nbf, p.nelec, p.ksym, p.mx_open, p.jsym, p.occ)
