@@ -1201,7 +1201,9 @@ __device__ __forceinline__ bool det_connected(bool so, const uint64_t *aA, const
   return naA == naB && ua + ub <= 2;
 }
 
-template <int W>
+// DIRECT (direct mode): segments over the full neighbour lists; instead of storing the kept
+// elements, Y[row, 0:kvec] += element * X[column, 0:kvec], added atomically per row.
+template <int W, bool DIRECT = false>
 __global__ void __launch_bounds__(WARPS_PER_CTA * 32) k_hbuild_fast(Params P) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   FastSmem<W> *ws = reinterpret_cast<FastSmem<W> *>(smem_raw) + (threadIdx.x >> 5);
@@ -1340,7 +1342,7 @@ __global__ void __launch_bounds__(WARPS_PER_CTA * 32) k_hbuild_fast(Params P) {
     // whatever the spread of marks over the neighbours.  Kept values are compacted in the
     // same order, so each row stays in ascending column order.  Each warp takes slab space
     // in chunks and advances through a chunk by the kept count of each row.
-    const int64_t prbase = P.pr_off[I] + (k0 - P.nbroff[I]) * nsefI;
+    const int64_t prbase = DIRECT ? 0 : P.pr_off[I] + (k0 - P.nbroff[I]) * nsefI;
     const RowDets rowA = {ws->ra, ws->rb, ws->rph, ws->rna};  // I's determinants (A = I)
     // evaluation order of the neighbours: grouped by pair kind (doubles, singles, spin-orbit,
     // diagonal), ascending within a kind, so that neighbouring lanes mostly run the same
@@ -1376,13 +1378,16 @@ __global__ void __launch_bounds__(WARPS_PER_CTA * 32) k_hbuild_fast(Params P) {
       ws->mrow[lane] = mr;
       ws->cm[lane] = cr;
       ws->keep[lane] = 0u;
-      if (cursor + T > chunk_end) {  // room for every marked element of the row
+      if (!DIRECT && cursor + T > chunk_end) {  // room for every marked element of the row
         const unsigned long long len = (unsigned long long)max(T, SLAB_CHUNK);
         unsigned long long b = 0;
         if (lane == 0) b = atomicAdd(P.slab_counter, len);
         cursor = __shfl_sync(0xffffffffu, b, 0);
         chunk_end = cursor + len;
       }
+      double acc[8];
+#pragma unroll
+      for (int q = 0; q < 8; ++q) acc[q] = 0.0;
       const unsigned long long base = cursor;
       // chunks beyond the slab capacity are counted but not written; the host sees the
       // final counter, enlarges the slab and evaluates again
@@ -1410,13 +1415,33 @@ __global__ void __launch_bounds__(WARPS_PER_CTA * 32) k_hbuild_fast(Params P) {
           unsigned conn = (unsigned)((co & 1ull) | ((co >> 15) & 2ull) | ((co >> 30) & 4ull) | ((co >> 45) & 8ull));
           // a diagonal block is symmetric: the transposed element swaps the determinant roles
           if (flip) conn = (conn & 9u) | ((conn & 2u) << 1) | ((conn & 4u) >> 1);
-          v = sef_elem<W>(P, pi, ws->K, flip ? t : r, flip ? r : t, conn, &rowA);
+          // A's determinants come from shared memory when A = I (every lower pair; a pair
+          // J > I of the direct mode has A = J, read from the tables)
+          v = sef_elem<W>(P, pi, ws->K, flip ? t : r, flip ? r : t, conn, (DIRECT && pi.swap) ? nullptr : &rowA);
           keep = (fabs(v) >= PSOCI_MIN_VALUE) || (diag_blk && t == r);
-          if (keep) atomicOr(&ws->keep[pl], 1u << t);
+          if (DIRECT) {
+            if (keep) {
+              const double *xr = P.dx + (pi.colbase + t) * P.ldx;
+#pragma unroll
+              for (int q = 0; q < 8; ++q)
+                if (q < P.kvec) acc[q] = fma(v, xr[q], acc[q]);
+            }
+          } else if (keep) {
+            atomicOr(&ws->keep[pl], 1u << t);
+          }
         }
-        const unsigned kb = __ballot_sync(0xffffffffu, keep);
-        if (keep && fits) P.slab_val[(int64_t)base + kc + __popc(kb & ((1u << lane) - 1u))] = v;
-        kc += __popc(kb);
+        if (!DIRECT) {
+          const unsigned kb = __ballot_sync(0xffffffffu, keep);
+          if (keep && fits) P.slab_val[(int64_t)base + kc + __popc(kb & ((1u << lane) - 1u))] = v;
+          kc += __popc(kb);
+        }
+      }
+      if (DIRECT) {
+        const double tot = reduce_scatter8_f64(acc, lane);
+        const int q = lane >> 2;
+        if ((lane & 3) == 0 && q < P.kvec && tot != 0.0) atomicAdd(P.dy + (P.sefoff[I] + r) * P.ldy + q, tot);
+        __syncwarp();
+        continue;
       }
       __syncwarp();
       const uint32_t keepm = (lane < n) ? ws->keep[lane] : 0u;
@@ -2091,13 +2116,22 @@ psoci_status run_direct_sigma(psoci_ctx *c, int k, const double *dX, int ldx, do
   const int64_t N = c->nsef_total;
   PSOCI_CUDA(c, cudaMemset2DAsync(dY, sizeof(double) * ldy, 0, sizeof(double) * k, N, st));
   if (P.nseg == 0) return PSOCI_OK;
-  const size_t smem = sizeof(WarpSmem) * WARPS_PER_CTA;
-  PSOCI_CUDA(c, cudaFuncSetAttribute(k_hbuild<W, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  // configurations of at most 32 determinants: the connectivity-marking kernel, evaluating
+  // only the elements that can be non-zero; otherwise the generic one
+  const bool fast = c->max_ndet <= FAST_MAXDET;
+  const size_t smem = fast ? sizeof(FastSmem<W>) * WARPS_PER_CTA : sizeof(WarpSmem) * WARPS_PER_CTA;
+  if (fast)
+    PSOCI_CUDA(c, cudaFuncSetAttribute(k_hbuild_fast<W, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  else
+    PSOCI_CUDA(c, cudaFuncSetAttribute(k_hbuild<W, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>((P.nseg + WARPS_PER_CTA - 1) / WARPS_PER_CTA, 152 * 16));
   for (int q0 = 0; q0 < k; q0 += 8) {
     P.dx = dX + q0; P.dy = dY + q0; P.ldx = ldx; P.ldy = ldy; P.kvec = std::min(8, k - q0);
     psoci_note_launch();
-    k_hbuild<W, 2><<<blocks, WARPS_PER_CTA * 32, smem, st>>>(P);
+    if (fast)
+      k_hbuild_fast<W, true><<<blocks, WARPS_PER_CTA * 32, smem, st>>>(P);
+    else
+      k_hbuild<W, 2><<<blocks, WARPS_PER_CTA * 32, smem, st>>>(P);
     PSOCI_CUDA(c, cudaGetLastError());
   }
   return PSOCI_OK;
