@@ -46,9 +46,12 @@ template <bool LOWP>
 __global__ void __launch_bounds__(TN_THREADS) k_tn(int64_t n, const double *__restrict__ A, int lda, int a0, int m,
                                                    const double *__restrict__ B, int ldb, int b0, int k,
                                                    double *__restrict__ partial, int64_t rows_per_blk) {
+  // rows per tile: LOWP has little arithmetic per row, so its tiles are larger (fewer
+  // barriers and load latencies per row)
+  constexpr int TR = LOWP ? 4 * TN_ROWS : TN_ROWS;
   extern __shared__ double sm[];
-  float2 *As = reinterpret_cast<float2 *>(sm);   // [TN_ROWS][m]
-  float2 *Bs = As + TN_ROWS * m;                 // [TN_ROWS][k]
+  float2 *As = reinterpret_cast<float2 *>(sm);   // [TR][m]
+  float2 *Bs = As + TR * m;                      // [TR][k]
   const int nout = m * k;
   // fewer outputs than threads: S threads share each output, splitting the tile's rows
   const int S = (nout >= TN_THREADS) ? 1 : TN_THREADS / nout;
@@ -58,13 +61,13 @@ __global__ void __launch_bounds__(TN_THREADS) k_tn(int64_t n, const double *__re
   for (int o = 0; o < TN_MAXOUT; ++o) { sh[o] = 0.f; sl[o] = 0.f; }
   int64_t r0 = (int64_t)blockIdx.x * rows_per_blk;
   int64_t r1 = min(n, r0 + rows_per_blk);
-  for (int64_t rt = r0; rt < r1; rt += TN_ROWS) {
-    int rows = (int)min((int64_t)TN_ROWS, r1 - rt);
-    for (int e = threadIdx.x; e < TN_ROWS * m; e += blockDim.x) {
+  for (int64_t rt = r0; rt < r1; rt += TR) {
+    int rows = (int)min((int64_t)TR, r1 - rt);
+    for (int e = threadIdx.x; e < TR * m; e += blockDim.x) {
       int rr = e / m, i = e - rr * m;
       As[e] = (rr < rows) ? split_f64(A[(rt + rr) * lda + a0 + i]) : make_float2(0.f, 0.f);
     }
-    for (int e = threadIdx.x; e < TN_ROWS * k; e += blockDim.x) {
+    for (int e = threadIdx.x; e < TR * k; e += blockDim.x) {
       int rr = e / k, j = e - rr * k;
       Bs[e] = (rr < rows) ? split_f64(B[(rt + rr) * ldb + b0 + j]) : make_float2(0.f, 0.f);
     }
@@ -154,20 +157,21 @@ __global__ void __launch_bounds__(NN_THREADS) k_nn(int64_t n, const double *__re
                                                    double beta, double *Out, int ldo, int o0) {
   extern __shared__ double sm[];
   float2 *Ys = reinterpret_cast<float2 *>(sm);  // [m][k]
-  float2 *As = Ys + m * k;                      // [32][m]
+  constexpr int TR = LOWP ? 128 : 32;  // rows per tile (larger when the arithmetic is light)
+  float2 *As = Ys + m * k;              // [TR][m]
   for (int e = threadIdx.x; e < m * k; e += blockDim.x) {
     int i = e / k, j = e - i * k;
     Ys[e] = split_f64(Y[i * ldy + y0 + j]);
   }
   __syncthreads();
-  for (int64_t rt = (int64_t)blockIdx.x * 32; rt < n; rt += (int64_t)gridDim.x * 32) {
-    int rows = (int)min((int64_t)32, n - rt);
-    for (int e = threadIdx.x; e < 32 * m; e += blockDim.x) {
+  for (int64_t rt = (int64_t)blockIdx.x * TR; rt < n; rt += (int64_t)gridDim.x * TR) {
+    int rows = (int)min((int64_t)TR, n - rt);
+    for (int e = threadIdx.x; e < TR * m; e += blockDim.x) {
       int rr = e / m, i = e - rr * m;
       As[e] = (rr < rows) ? split_f64(A[(rt + rr) * lda + a0 + i]) : make_float2(0.f, 0.f);
     }
     __syncthreads();
-    for (int e = threadIdx.x; e < 32 * k; e += blockDim.x) {
+    for (int e = threadIdx.x; e < TR * k; e += blockDim.x) {
       int rr = e / k, j = e - rr * k;
       if (rr < rows) {
         double s;
@@ -478,7 +482,8 @@ psoci_status tn(Work &w, const double *A, int lda, int a0, int m, const double *
   const bool lowp = w.lowp && lowp_ok;
   psoci_ctx *c = w.c;
   if (m * k > TN_THREADS * TN_MAXOUT) return psoci_fail(c, PSOCI_ERR_INVALID_ARG, "tn: block too large");
-  size_t smem = sizeof(double) * std::max(TN_ROWS * (m + k), TN_THREADS);
+  const int tr = lowp ? 4 * TN_ROWS : TN_ROWS;  // rows per tile (k_tn)
+  size_t smem = sizeof(double) * std::max(tr * (m + k), TN_THREADS);
   psoci_note_launch();
   if (lowp)
     k_tn<true><<<w.nblk, TN_THREADS, smem, c->stream>>>(w.N, A, lda, a0, m, B, ldb, b0, k, w.partial, w.rows_per_blk);
@@ -494,8 +499,9 @@ psoci_status nn(Work &w, const double *A, int lda, int a0, int m, const double *
                 double beta, double *Out, int ldo, int o0, bool lowp_ok = false) {
   const bool lowp = w.lowp && lowp_ok;
   psoci_ctx *c = w.c;
-  size_t smem = sizeof(double) * (m * k + 32 * m);
-  int blocks = (int)std::min<int64_t>((w.N + 31) / 32, 152 * 8);
+  const int tr = lowp ? 128 : 32;  // rows per tile (k_nn)
+  size_t smem = sizeof(double) * (m * k + tr * m);
+  int blocks = (int)std::min<int64_t>((w.N + tr - 1) / tr, 152 * 8);
   psoci_note_launch();
   if (lowp)
     k_nn<true><<<std::max(blocks, 1), NN_THREADS, smem, c->stream>>>(w.N, A, lda, a0, m, Y, ldy, y0, k, alpha, beta,
@@ -604,8 +610,8 @@ psoci_status psoci_davidson_impl(psoci_ctx *c, const psoci_dav_opts *o, double *
   cudaStream_t st = c->stream;
   const size_t jac_smem = sizeof(double) * 2 * MAX_SUB * MAX_SUB;
   PSOCI_CUDA(c, cudaFuncSetAttribute(k_jacobi, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)jac_smem));
-  PSOCI_CUDA(c, cudaFuncSetAttribute(k_nn<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024));
-  PSOCI_CUDA(c, cudaFuncSetAttribute(k_tn<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024));
+  PSOCI_CUDA(c, cudaFuncSetAttribute(k_nn<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 128 * 1024));
+  PSOCI_CUDA(c, cudaFuncSetAttribute(k_tn<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 128 * 1024));
   PSOCI_CUDA(c, cudaFuncSetAttribute(k_nn<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024));
   PSOCI_CUDA(c, cudaFuncSetAttribute(k_tn<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024));
   PSOCI_CUDA(c, cudaMemsetAsync(w.V, 0, sizeof(double) * N * ld, st));
