@@ -124,6 +124,18 @@ __device__ __forceinline__ void ldg_row8(float (&f)[8], const float *p) {
       : "l"(p));
 }
 
+// the first XS (4 or 8) floats at p (aligned to XS floats) in one load
+template <int XS>
+__device__ __forceinline__ void ldg_row(float (&f)[8], const float *p) {
+  if (XS == 8) {
+    ldg_row8(f, p);
+  } else {
+    const float4 v = __ldg(reinterpret_cast<const float4 *>(p));
+    f[0] = v.x; f[1] = v.y; f[2] = v.z; f[3] = v.w;
+    f[4] = f[5] = f[6] = f[7] = 0.f;
+  }
+}
+
 // Kahan step: the rounding error of every addition is carried in c and fed back
 __device__ __forceinline__ void kahan_add(float &s, float &c, float prod) {
   const float yv = __fsub_rn(prod, c);
@@ -142,8 +154,10 @@ __global__ void __launch_bounds__(SIG_THREADS) k_spmm_mixed(int64_t nrows, const
                                                             const float *__restrict__ val,
                                                             const float *__restrict__ x, double *__restrict__ y,
                                                             int ldy) {
-  // x: FP32 inputs with a row stride of 8 floats (32 bytes, 32-byte aligned) whatever K is, so
-  // every gather is one 256-bit load (sm_100+) — one L1 wavefront per gathered row
+  // x: FP32 inputs with a row stride of XS floats (8 = 32 bytes for K > 4, 4 = 16 bytes for
+  // K <= 4; aligned to the stride), so every gather is one 256- or 128-bit load — one L1
+  // wavefront per gathered row, and half the bytes when the block is narrow
+  constexpr int XS = (K <= 4) ? 4 : 8;
   const int lane = threadIdx.x & 31;
   const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
@@ -163,7 +177,7 @@ __global__ void __launch_bounds__(SIG_THREADS) k_spmm_mixed(int64_t nrows, const
         vv[u] = ldg_stream(val + t + 32 * u);
       }
 #pragma unroll
-      for (int u = 0; u < 4; ++u) ldg_row8(xx[u], x + (int64_t)cc[u] * 8);
+      for (int u = 0; u < 4; ++u) ldg_row<XS>(xx[u], x + (int64_t)cc[u] * XS);
 #pragma unroll
       for (int u = 0; u < 4; ++u)
 #pragma unroll
@@ -173,7 +187,7 @@ __global__ void __launch_bounds__(SIG_THREADS) k_spmm_mixed(int64_t nrows, const
       const int c = ldg_stream(col + t);
       const float v = ldg_stream(val + t);
       float xv[8];
-      ldg_row8(xv, x + (int64_t)c * 8);
+      ldg_row<XS>(xv, x + (int64_t)c * XS);
 #pragma unroll
       for (int q = 0; q < K; ++q) kahan_add(s[q], cmp[q], __fmul_rn(v, xv[q]));
     }
@@ -287,16 +301,18 @@ __global__ void k_split_x(int64_t n, int k, const double *__restrict__ x, int ld
   }
 }
 
-// X (FP64, leading dim ldx, k <= 8 columns) -> X32 (FP32, row stride 8); one thread per row
+// X (FP64, leading dim ldx, k <= 8 columns) -> X32 (FP32, row stride 4 when k <= 4, else 8,
+// zero padded); one thread per row
 __global__ void k_to_f32(int64_t n, int k, const double *__restrict__ x, int ldx, float *__restrict__ x32) {
+  const int xs = (k <= 4) ? 4 : 8;
   for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
     const double *src = x + r * ldx;
-    float4 *dst = reinterpret_cast<float4 *>(x32 + r * 8);  // row stride 8, zero padded
+    float4 *dst = reinterpret_cast<float4 *>(x32 + r * xs);
     float f[8];
 #pragma unroll
     for (int q = 0; q < 8; ++q) f[q] = (q < k) ? (float)src[q] : 0.f;
     dst[0] = make_float4(f[0], f[1], f[2], f[3]);
-    dst[1] = make_float4(f[4], f[5], f[6], f[7]);
+    if (xs == 8) dst[1] = make_float4(f[4], f[5], f[6], f[7]);
   }
 }
 

@@ -124,7 +124,7 @@ def test_sigma_fp64_and_mixed(oracle_mod):
     rp, ci, va = O.build_lower(4)
     c.build_hamiltonian(mixed=True)
     rng = np.random.default_rng(0)
-    for k in (1, 3, 8, 11):
+    for k in (1, 3, 4, 5, 8, 11):
         X = rng.standard_normal((c.nsef, k))
         Yref = O.sigma_lower(rp, ci, va, X.T.copy()).T
         Y = c.sigma(X)
