@@ -231,6 +231,41 @@ __device__ __forceinline__ int excitation(const uint64_t *e1A, const uint64_t *e
   return ni;
 }
 
+// The same, with the first two positions of each side returned in registers (no local
+// arrays): ex0 <= ex1 removed from A, jy0 <= jy1 added in B, -1 where absent.
+template <int W>
+__device__ __forceinline__ int excitation_r(const uint64_t *e1A, const uint64_t *e2A, const uint64_t *e1B,
+                                            const uint64_t *e2B, int &ex0, int &ex1, int &jy0, int &jy1) {
+  int ni = 0, nj = 0;
+  ex0 = ex1 = jy0 = jy1 = -1;
+#pragma unroll
+  for (int w = 0; w < W; ++w) {
+    const uint64_t i1 = e1A[w] & ~e1B[w], i2 = e2A[w] & ~e2B[w];
+    const uint64_t j1 = e1B[w] & ~e1A[w], j2 = e2B[w] & ~e2A[w];
+    uint64_t u = i1 | i2;
+    while (u) {
+      const int b = __ffsll((long long)u) - 1;
+      u &= u - 1;
+      const int p = 64 * w + b;
+      const int both = (int)((i1 >> b) & (i2 >> b) & 1ull);
+      if (ni == 0) { ex0 = p; if (both) ex1 = p; }
+      else if (ni == 1) ex1 = p;
+      ni += 1 + both;
+    }
+    u = j1 | j2;
+    while (u) {
+      const int b = __ffsll((long long)u) - 1;
+      u &= u - 1;
+      const int p = 64 * w + b;
+      const int both = (int)((j1 >> b) & (j2 >> b) & 1ull);
+      if (nj == 0) { jy0 = p; if (both) jy1 = p; }
+      else if (nj == 1) jy1 = p;
+      nj += 1 + both;
+    }
+  }
+  return ni;
+}
+
 // Screen, stage 1: configurations within two excitations of i (sum |occ_i - occ_j| <= 4,
 // the orbmap test of PsociGADeterminants.C:2249-2277).  One thread per row configuration;
 // tiles of column configurations are staged in shared memory and read by broadcast, so each
@@ -512,13 +547,14 @@ __global__ void __launch_bounds__(256) k_join(Params P, JoinTabs J, int64_t *cnt
               const uint32_t key = J.lokey[lp];
               b1[0] |= key & lomask;
               b2[0] |= key >> J.s;
-              int ex[2], jy[2];
-              const int ni = (j <= (int)i) ? excitation<W>(a1, a2, b1, b2, ex, jy) : excitation<W>(b1, b2, a1, a2, ex, jy);
+              // the tests below are symmetric in the two configurations' roles
+              int ex0, ex1, jy0, jy1;
+              const int ni = excitation_r<W>(a1, a2, b1, b2, ex0, ex1, jy0, jy1);
               if (ni == 2) {
-                keep = double_block_kept(__ldg(P.eri + canon4(ex[0], jy[0], ex[1], jy[1])),
-                                         __ldg(P.eri + canon4(ex[0], jy[1], ex[1], jy[0])));
+                keep = double_block_kept(__ldg(P.eri + canon4(ex0, jy0, ex1, jy1)),
+                                         __ldg(P.eri + canon4(ex0, jy1, ex1, jy0)));
               } else if (ni == 1 && __ldg(P.jsym + j) != js_i) {
-                keep = __ldg(P.one + tri64(ex[0], jy[0])) != 0.0;
+                keep = __ldg(P.one + tri64(ex0, jy0)) != 0.0;
               }
             }
           }
