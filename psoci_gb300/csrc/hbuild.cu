@@ -404,7 +404,28 @@ struct JoinTabs {
   const uint32_t *lokey;
   const int64_t *goff;    // per hi pattern g: its list of hi patterns h to visit ...
   const uint32_t *glist;  // ... h | d_hi(g, h) << 28, ascending h
+  const uint32_t *dkept;  // double_block_kept of (ex0 <= ex1) -> (jy0 <= jy1), bit tri(ex)*NT + tri(jy)
+  int64_t nt;             // NT = nbf(nbf+1)/2
 };
+
+// The pruning decision of every double excitation, as bits: word q holds the pairs
+// (a, b), a = tri(ex0, ex1), b = tri(jy0, jy1), with a * NT + b in [32q, 32q + 32).  The
+// same integrals and test as the per-candidate form, so the same decisions.
+__global__ void k_double_kept(int64_t nt, const int2 *__restrict__ pairs, const double *__restrict__ eri,
+                              uint32_t *bits) {
+  const int64_t nwords = (nt * nt + 31) / 32;
+  for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < nwords; q += (int64_t)gridDim.x * blockDim.x) {
+    uint32_t w = 0u;
+    for (int u = 0; u < 32; ++u) {
+      const int64_t e = q * 32 + u;
+      if (e >= nt * nt) break;
+      const int2 x = pairs[e / nt], y = pairs[e % nt];  // (ex0, ex1), (jy0, jy1), ascending
+      const bool k = double_block_kept(__ldg(eri + canon4(x.x, y.x, x.y, y.y)), __ldg(eri + canon4(x.x, y.y, x.y, y.x)));
+      w |= (uint32_t)k << u;
+    }
+    bits[q] = w;
+  }
+}
 
 template <int W>
 __device__ __forceinline__ void set_bit_w(uint64_t (&x)[W], int p) {
@@ -551,8 +572,8 @@ __global__ void __launch_bounds__(256) k_join(Params P, JoinTabs J, int64_t *cnt
               int ex0, ex1, jy0, jy1;
               const int ni = excitation_r<W>(a1, a2, b1, b2, ex0, ex1, jy0, jy1);
               if (ni == 2) {
-                keep = double_block_kept(__ldg(P.eri + canon4(ex0, jy0, ex1, jy1)),
-                                         __ldg(P.eri + canon4(ex0, jy1, ex1, jy0)));
+                const int64_t e = ((int64_t)ex1 * (ex1 + 1) / 2 + ex0) * J.nt + (int64_t)jy1 * (jy1 + 1) / 2 + jy0;
+                keep = (__ldg(J.dkept + (e >> 5)) >> (e & 31)) & 1u;
               } else if (ni == 1 && __ldg(P.jsym + j) != js_i) {
                 keep = __ldg(P.one + tri64(ex0, jy0)) != 0.0;
               }
@@ -1776,6 +1797,8 @@ psoci_status run_build(psoci_ctx *c, psoci_hmode mode, int64_t *nnz_out) {
   double *d_slabval = nullptr;
   int32_t *d_jslab = nullptr;
   int64_t *d_jstart = nullptr;
+  int2 *d_tpairs = nullptr;
+  uint32_t *d_dkept = nullptr;
   cudaEvent_t ev[6] = {};
   auto cleanup = [&]() {
     for (auto &e : ev)
@@ -1784,6 +1807,7 @@ psoci_status run_build(psoci_ctx *c, psoci_hmode mode, int64_t *nnz_out) {
     psoci_free(d_candoff); psoci_free(d_cand);
     psoci_free(d_nlow); psoci_free(d_prrows); psoci_free(d_proff); psoci_free(d_mk); psoci_free(d_prm);
     psoci_free(d_err); psoci_free(d_slabval); psoci_free(d_jslab); psoci_free(d_jstart);
+    psoci_free(d_tpairs); psoci_free(d_dkept);
     psoci_free(d_gcnt); psoci_free(d_goff); psoci_free(d_glist);
     psoci_free(d_cnt); psoci_free(d_nbroff); psoci_free(d_nseg); psoci_free(d_nrow); psoci_free(d_segoff);
     psoci_free(d_rowslot); psoci_free(d_segk0); psoci_free(d_segrow); psoci_free(d_segcnt); psoci_free(d_rownnz);
@@ -1820,7 +1844,7 @@ psoci_status run_build(psoci_ctx *c, psoci_hmode mode, int64_t *nnz_out) {
   if (c->join_ok) {
     // by lookup, with the integral pruning fused
     JoinTabs J = {c->join_s, c->join_G, c->join_L, c->d_jgid, c->d_jlid, c->d_jT, c->d_jlnoff, c->d_jln,
-                  c->d_jhdec, c->d_jlokey, nullptr, nullptr};
+                  c->d_jhdec, c->d_jlokey, nullptr, nullptr, nullptr, 0};
     // hi-pattern lists (depend on the integrals, so built here)
     const int G = c->join_G;
     TRY(psoci_alloc(c, &d_gcnt, G + 1));
@@ -1837,6 +1861,22 @@ psoci_status run_build(psoci_ctx *c, psoci_hmode mode, int64_t *nnz_out) {
     k_group_lists<W, 1><<<gblocks, 256, 0, st>>>(J, c->d_eri, nullptr, d_glist);
     TRYC(cudaGetLastError());
     J.glist = d_glist;
+    {
+      // pruning bits of all double excitations (depend on the integrals)
+      const int64_t nt = (int64_t)c->nbf * (c->nbf + 1) / 2;
+      std::vector<int2> pairs((size_t)nt);
+      for (int a = 0; a < c->nbf; ++a)
+        for (int b = 0; b <= a; ++b) pairs[(size_t)a * (a + 1) / 2 + b] = make_int2(b, a);  // (low, high)
+      TRY(psoci_alloc(c, &d_tpairs, nt));
+      TRY(psoci_alloc(c, &d_dkept, (nt * nt + 31) / 32));
+      TRYC(cudaMemcpyAsync(d_tpairs, pairs.data(), sizeof(int2) * nt, cudaMemcpyHostToDevice, st));
+      psoci_note_launch();
+      k_double_kept<<<152 * 8, 256, 0, st>>>(nt, d_tpairs, c->d_eri, d_dkept);
+      TRYC(cudaGetLastError());
+      TRYC(cudaStreamSynchronize(st));  // pairs is a host buffer
+      J.dkept = d_dkept;
+      J.nt = nt;
+    }
     TRY(psoci_alloc(c, &d_cnt, n + 1));
     TRY(psoci_alloc(c, &d_tot, n + 1));
     TRY(psoci_alloc(c, &d_candoff, n + 1));
