@@ -437,6 +437,33 @@ __global__ void k_jacobi(const double *G, int ld, int m, double *theta, double *
   if (tid == 0) *status = converged ? sweeps : -1;
 }
 
+// initial guess from the lowest diagonal block: map[row] = position of the row in idx
+__global__ void k_map_set(const int64_t *idx, int M, int32_t *map) {
+  for (int i = threadIdx.x; i < M; i += blockDim.x) map[idx[i]] = i;
+}
+
+// Hs[i*M + j] = H[idx[i], idx[j]] from the stored rows (one warp per row)
+__global__ void k_extract_block(const int64_t *__restrict__ rowptr, const int32_t *__restrict__ col,
+                                const double *__restrict__ val, const int64_t *__restrict__ idx, int M,
+                                const int32_t *__restrict__ map, double *Hs) {
+  const int lane = threadIdx.x & 31;
+  const int i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (i >= M) return;
+  const int64_t row = idx[i];
+  for (int64_t t = rowptr[row] + lane; t < rowptr[row + 1]; t += 32) {
+    const int j = map[col[t]];
+    if (j >= 0) Hs[(int64_t)i * M + j] = val[t];
+  }
+}
+
+// V[idx[i], j] = Y[i, j]: the block's lowest eigenvectors as the first basis vectors
+__global__ void k_scatter_guess(const double *Y, int ldy, const int64_t *idx, int M, int nr, double *V, int ld) {
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < M * nr; e += gridDim.x * blockDim.x) {
+    const int i = e / nr, j = e - i * nr;
+    V[idx[i] * ld + j] = Y[(int64_t)i * ldy + j];
+  }
+}
+
 __global__ void k_set_unit(double *V, int ld, int c0, const int64_t *idx, int nr) {
   int j = threadIdx.x;
   if (j < nr) V[idx[j] * ld + c0 + j] = 1.0;
@@ -617,13 +644,15 @@ psoci_status psoci_davidson_impl(psoci_ctx *c, const psoci_dav_opts *o, double *
   PSOCI_CUDA(c, cudaMemsetAsync(w.V, 0, sizeof(double) * N * ld, st));
   PSOCI_CUDA(c, cudaMemsetAsync(w.G, 0, sizeof(double) * ld * ld, st));
 
-  // guess: unit vectors on the nr lowest diagonal elements
+  // guess: the lowest eigenvectors of H restricted to the M lowest diagonal elements (a
+  // stored matrix), else unit vectors on the nr lowest diagonal elements
   std::vector<double> hdiag(N);
   PSOCI_CUDA(c, cudaMemcpyAsync(hdiag.data(), c->d_diag, sizeof(double) * N, cudaMemcpyDeviceToHost, st));
   PSOCI_CUDA(c, cudaStreamSynchronize(st));
+  const int M = (int)std::min<int64_t>(MAX_SUB, N);
   std::vector<int64_t> order(N);
   std::iota(order.begin(), order.end(), 0);
-  std::partial_sort(order.begin(), order.begin() + nr, order.end(),
+  std::partial_sort(order.begin(), order.begin() + M, order.end(),
                     [&](int64_t a, int64_t b) { return hdiag[a] < hdiag[b] || (hdiag[a] == hdiag[b] && a < b); });
   psoci_prec prec = o->prec;
   bool refine_phase = (prec != PSOCI_PREC_MIXED);  // FP64 and FF iterate to rtol directly
@@ -644,6 +673,36 @@ psoci_status psoci_davidson_impl(psoci_ctx *c, const psoci_dav_opts *o, double *
     if (bk < 1) return psoci_fail(c, PSOCI_ERR_NUMERIC, "davidson: restart vectors are linearly dependent");
     m = bk;
     PSOCI_CUDA(c, cudaStreamSynchronize(st));
+  } else if (!c->direct && c->d_val && M > nr) {
+    int64_t *gidx = nullptr;
+    int32_t *map = nullptr;
+    double *Hs = nullptr, *Ys = nullptr, *ths = nullptr;
+    int *jst = nullptr;
+    auto release = [&]() {
+      psoci_free(gidx); psoci_free(map); psoci_free(Hs); psoci_free(Ys); psoci_free(ths); psoci_free(jst);
+    };
+    if ((s = psoci_alloc(c, &gidx, M)) || (s = psoci_alloc(c, &map, N)) || (s = psoci_alloc(c, &Hs, (size_t)M * M)) ||
+        (s = psoci_alloc(c, &Ys, (size_t)M * M)) || (s = psoci_alloc(c, &ths, M)) || (s = psoci_alloc(c, &jst, 1))) {
+      release();
+      return s;
+    }
+    cudaError_t e = cudaMemcpyAsync(gidx, order.data(), sizeof(int64_t) * M, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(map, 0xff, sizeof(int32_t) * N, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(Hs, 0, sizeof(double) * M * M, st);
+    if (e == cudaSuccess) {
+      psoci_note_launch();
+      k_map_set<<<1, 128, 0, st>>>(gidx, M, map);
+      psoci_note_launch();
+      k_extract_block<<<(M + 7) / 8, 256, 0, st>>>(c->d_rowptr, c->d_col, c->d_val, gidx, M, map, Hs);
+      psoci_note_launch();
+      k_jacobi<<<1, 256, jac_smem, st>>>(Hs, M, M, ths, Ys, 60, jst);
+      psoci_note_launch();
+      k_scatter_guess<<<1, 256, 0, st>>>(Ys, M, gidx, M, nr, w.V, ld);
+      e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    release();
+    if (e != cudaSuccess) return psoci_cuda_fail(c, e, "davidson: initial block");
   } else {
     PSOCI_CUDA(c, cudaMemcpyAsync(w.idx, order.data(), sizeof(int64_t) * nr, cudaMemcpyHostToDevice, st));
     psoci_note_launch();
