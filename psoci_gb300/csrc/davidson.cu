@@ -695,7 +695,7 @@ psoci_status psoci_davidson_impl(psoci_ctx *c, const psoci_dav_opts *o, double *
       psoci_note_launch();
       k_extract_block<<<(M + 7) / 8, 256, 0, st>>>(c->d_rowptr, c->d_col, c->d_val, gidx, M, map, Hs);
       psoci_note_launch();
-      k_jacobi<<<1, 256, jac_smem, st>>>(Hs, M, M, ths, Ys, 60, jst);
+      k_jacobi<<<1, 256, jac_smem, st>>>(Hs, M, M, ths, Ys, 6, jst);  // a few sweeps: a guess
       psoci_note_launch();
       k_scatter_guess<<<1, 256, 0, st>>>(Ys, M, gidx, M, nr, w.V, ld);
       e = cudaGetLastError();
@@ -717,7 +717,9 @@ psoci_status psoci_davidson_impl(psoci_ctx *c, const psoci_dav_opts *o, double *
 
   std::vector<double> h_norm(nr), h_theta(ld);
   std::vector<int> sel;
-  bool done = false;
+  bool done = false, stalled = false;
+  double best_mixed = HUGE_VAL;  // smallest largest-residual of the FP32-element phase so far
+  int no_gain = 0;               // iterations since it last fell by 30%
   psoci_status result = PSOCI_OK;
   int jstat = 0;
   while (!done) {
@@ -746,6 +748,17 @@ psoci_status psoci_davidson_impl(psoci_ctx *c, const psoci_dav_opts *o, double *
       h_norm[j] = std::sqrt(h_norm[j]);
     }
     const double tol = refine_phase ? rtol : tol_mixed;
+    if (!refine_phase) {
+      // the FP32-element phase has a residual floor (FP32 elements, FP32 subspace products);
+      // when the largest residual stops falling near it, refine from there
+      const double mx = *std::max_element(h_norm.begin(), h_norm.end());
+      if (mx < 0.7 * best_mixed) {
+        best_mixed = mx;
+        no_gain = 0;
+      } else if (++no_gain >= 4 && best_mixed < 1e-3) {
+        stalled = true;
+      }
+    }
     sel.clear();
     for (int j = 0; j < nr; ++j)
       if (h_norm[j] > tol) {
@@ -755,7 +768,8 @@ psoci_status psoci_davidson_impl(psoci_ctx *c, const psoci_dav_opts *o, double *
     if (c->verbose)
       fprintf(stderr, "psoci davidson it=%d m=%d %s max|r|=%.3e e0=%.12f jacobi=%d\n", iters, m,
               refine_phase ? "fp64" : "mixed", *std::max_element(h_norm.begin(), h_norm.end()), h_theta[0], jstat);
-    if (sel.empty()) {
+    if (sel.empty() || stalled) {
+      stalled = false;
       if (!refine_phase && o->refine) {
         // FP64 refinement: restart from the Ritz vectors with exact (FP64) H products
         refine_phase = true;
@@ -799,7 +813,17 @@ psoci_status psoci_davidson_impl(psoci_ctx *c, const psoci_dav_opts *o, double *
     }
     int bk = 0;
     if ((s = orthonormalize(w, m, nsel, &bk))) return s;
-    if (bk == 0) { result = PSOCI_ERR_NOT_CONVERGED; break; }
+    if (bk == 0) {
+      // no new direction survived the orthonormalisation: in the FP32-element phase the
+      // basis has reached what that phase resolves, so refine from the current Ritz vectors
+      // (next pass); otherwise the solve is stuck
+      if (!refine_phase && o->refine) {
+        stalled = true;
+        continue;
+      }
+      result = PSOCI_ERR_NOT_CONVERGED;
+      break;
+    }
     if ((s = sigma_block(w, w.V + m, ld, w.HV + m, ld, bk, prec))) return s;
     sigma_calls += bk;
     if ((s = tn(w, w.V, ld, 0, m + bk, w.HV, ld, m, bk, w.G, ld, m, true))) return s;
