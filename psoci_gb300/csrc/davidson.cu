@@ -695,7 +695,7 @@ psoci_status psoci_davidson_impl(psoci_ctx *c, const psoci_dav_opts *o, double *
       psoci_note_launch();
       k_extract_block<<<(M + 7) / 8, 256, 0, st>>>(c->d_rowptr, c->d_col, c->d_val, gidx, M, map, Hs);
       psoci_note_launch();
-      k_jacobi<<<1, 256, jac_smem, st>>>(Hs, M, M, ths, Ys, 6, jst);  // a few sweeps: a guess
+      k_jacobi<<<1, 256, jac_smem, st>>>(Hs, M, M, ths, Ys, 3, jst);  // a few sweeps: a guess
       psoci_note_launch();
       k_scatter_guess<<<1, 256, 0, st>>>(Ys, M, gidx, M, nr, w.V, ld);
       e = cudaGetLastError();
