@@ -201,6 +201,13 @@ typedef struct {
 PSOCI_API psoci_status psoci_davidson(psoci_ctx *ctx, const psoci_dav_opts *opts, double *evals,
                             double *evecs, double *rnorms, psoci_dav_stats *stats);
 
+/* Eigenpairs of a symmetric n x n matrix G (row stride ldg; the halves are averaged): the
+ * eigen-solve of PsociGAsubspace::diagSubspaceGOP (PsociGAsubspace.C:1088-1171, LAPACK dsygv)
+ * with the unit metric of an orthonormal basis, as psoci_davidson runs it.  w[n] ascending;
+ * Y (row stride ldy) column c = eigenvector c.  Householder tridiagonalisation and implicit
+ * QR with the Wilkinson shift.  Host computation; needs no context or device. */
+PSOCI_API psoci_status psoci_subspace_eigen(int n, const double *G, int ldg, double *w, double *Y, int ldy);
+
 /* Initial guess for the next psoci_davidson (the reference's -r vector restart,
  * driver.PSOCI.splittest.C:962-972): k vectors of length N, root-major (vector r at r*N).
  * Missing roots are completed with unit vectors on the lowest diagonal elements.

@@ -94,6 +94,7 @@ SIGNATURES = {
     "psoci_density1": (ctypes.c_int, [_P, ctypes.c_int, _DP, _DP]),
     "psoci_density1_device": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p]),
     "psoci_natural_orbitals": (ctypes.c_int, [ctypes.c_int, _DP, _I32P, _DP, _DP, _I32P]),
+    "psoci_subspace_eigen": (ctypes.c_int, [ctypes.c_int, _DP, ctypes.c_int, _DP, _DP, ctypes.c_int]),
     "psoci_write_vectors": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int, ctypes.c_int64, ctypes.c_int, _DP,
                                            ctypes.c_char_p]),
     "psoci_read_vectors": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int, ctypes.c_int64, ctypes.c_int, _DP, _IP]),
@@ -369,6 +370,22 @@ def natural_orbitals(dens_packed, orb_sym):
         e += n
         v += n * n
     return occ, blocks
+
+
+def subspace_eigen(G):
+    """Eigenpairs of a symmetric matrix as the Davidson solver's Rayleigh-Ritz step computes
+    them: (w ascending [n], Y [n, n] with column c = eigenvector c)."""
+    lib = load_library()
+    g = np.ascontiguousarray(G, np.float64)
+    n = g.shape[0]
+    if g.ndim != 2 or g.shape[1] != n or n < 1:
+        raise ValueError(f"subspace_eigen: square matrix expected, got {g.shape}")
+    w = np.zeros(n)
+    Y = np.zeros((n, n))
+    st = lib.psoci_subspace_eigen(n, _ptr(g, _DP), n, _ptr(w, _DP), _ptr(Y, _DP), n)
+    if st != PSOCI_OK:
+        raise PsociError(st, "subspace_eigen")
+    return w, Y
 
 
 def write_vectors(path: str, vecs: np.ndarray, binary: bool = False, title: str = ""):

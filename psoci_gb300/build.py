@@ -18,7 +18,7 @@ LIBDIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(LIBDIR, "libpsoci_gpu.so")
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 SOURCES = ["util.cu", "dets.cu", "hbuild.cu", "sigma.cu", "davidson.cu", "capi.cu", "io.cu", "noalloc.cu", "density.cu",
-           "natorb.cpp"]
+           "natorb.cpp", "symeig.cpp"]
 PER_FILE = {"hbuild.cu": ["--fmad=false"]}
 
 

@@ -22,6 +22,7 @@
 #include <cmath>
 #include <cstdio>
 #include <numeric>
+#include <type_traits>
 #include <vector>
 
 #include "ffmath.cuh"
@@ -29,100 +30,141 @@
 
 namespace {
 
-constexpr int TN_THREADS = 256;
-constexpr int TN_ROWS = 32;       // rows staged per tile
-constexpr int TN_MAXOUT = 8;      // outputs per thread => m*k <= 2048
-constexpr int NN_THREADS = 256;
+constexpr int TS_THREADS = 256;   // k_tn block size
+constexpr int TN_MAXK = 16;       // k_tn: B columns (two groups of 8 outputs per i)
+constexpr int TN_TILE = 256;      // k_tn: rows of B staged per tile
+constexpr int NN_THREADS = 128;   // k_nn block size
+constexpr int NN_MAXK = 32;       // k_nn: Y columns (four groups of 8 outputs per row)
 constexpr int MAX_SUB = 96;       // Jacobi keeps two m x m FP64 matrices in shared memory
 
 // The tall-skinny products below run in float-float arithmetic on the FP32 pipe (see
 // ffmath.cuh): on GB300 the FP64 pipe issues ~2 FMA/clk/SM against 128 FP32 lanes, and
 // these products are FP64-bound.  Block partials are combined in FP64.
-
-// C_partial[blk][i*k + j] = sum over the block's rows of A[r, a0+i] * B[r, b0+j]
-// LOWP (the FP32-element phase of a mixed solve, whose sigma is good to ~1e-7 anyway): FP32
-// products summed in FP32 over a tile of 32 rows, tile sums added in float-float.
+//
+// LOWP (the FP32-element phase of a mixed solve, whose sigma is good to ~1e-7 anyway):
+// elements truncated to FP32 (the high word of the float-float split: integer operations
+// only), products summed in FP32 over a tile, tile sums added in float-float.
+//
+// Register tiling: a thread owns 8 outputs and, per row, reads one element of the tall
+// operand straight from global memory (coalesced across the warp, several rows in flight)
+// and 8 broadcast elements of the other operand from shared memory, so the inner loop
+// issues 8 float-float FMAs per load of its own.
 template <bool LOWP>
-__global__ void __launch_bounds__(TN_THREADS) k_tn(int64_t n, const double *__restrict__ A, int lda, int a0, int m,
+using ts_elt = typename std::conditional<LOWP, float, float2>::type;
+
+template <bool LOWP>
+__device__ __forceinline__ ts_elt<LOWP> ts_load(double x) {
+  if constexpr (LOWP) return split_f64(x).x;
+  else return split_f64(x);
+}
+
+// 8 consecutive elements from 16-byte aligned shared memory
+template <bool LOWP>
+__device__ __forceinline__ void ts_load8(const ts_elt<LOWP> *p, ts_elt<LOWP> (&v)[8]) {
+  const float4 *q = reinterpret_cast<const float4 *>(p);
+  if constexpr (LOWP) {
+    const float4 u = q[0], w = q[1];
+    v[0] = u.x; v[1] = u.y; v[2] = u.z; v[3] = u.w;
+    v[4] = w.x; v[5] = w.y; v[6] = w.z; v[7] = w.w;
+  } else {
+#pragma unroll
+    for (int t = 0; t < 4; ++t) {
+      const float4 u = q[t];
+      v[2 * t] = make_float2(u.x, u.y);
+      v[2 * t + 1] = make_float2(u.z, u.w);
+    }
+  }
+}
+
+// acc[j] += a * b[j] for the 8 outputs of a thread (float-float, or FP32 when LOWP)
+template <bool LOWP>
+__device__ __forceinline__ void ts_fma8(float (&h)[8], float (&l)[8], ts_elt<LOWP> a, const ts_elt<LOWP> (&b)[8]) {
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    if constexpr (LOWP) h[j] = __fmaf_rn(a, b[j], h[j]);
+    else ff_fma(h[j], l[j], a, b[j]);
+  }
+}
+
+// partial[blk][i*k + j] = sum over the block's rows r of A[r, a0+i] * B[r, b0+j]
+// (m <= MAX_SUB, k <= TN_MAXK).  Thread: output group g = (i, jb), the 8 outputs
+// j in [8jb, 8jb+8) of row i of C, over the rows sub, sub+S, ... of each tile; B's tile is
+// split into shared memory once, A is read from global memory (lanes of a warp take
+// consecutive i of one row).  The S shares of a group are added in FP64 at the end, in a
+// fixed order.
+template <bool LOWP>
+__global__ void __launch_bounds__(TS_THREADS) k_tn(int64_t n, const double *__restrict__ A, int lda, int a0, int m,
                                                    const double *__restrict__ B, int ldb, int b0, int k,
                                                    double *__restrict__ partial, int64_t rows_per_blk) {
-  // rows per tile: LOWP has little arithmetic per row, so its tiles are larger (fewer
-  // barriers and load latencies per row)
-  constexpr int TR = LOWP ? 4 * TN_ROWS : TN_ROWS;
+  using E = ts_elt<LOWP>;
   extern __shared__ double sm[];
-  float2 *As = reinterpret_cast<float2 *>(sm);   // [TR][m]
-  float2 *Bs = As + TR * m;                      // [TR][k]
-  const int nout = m * k;
-  // fewer outputs than threads: S threads share each output, splitting the tile's rows
-  const int S = (nout >= TN_THREADS) ? 1 : TN_THREADS / nout;
-  const int sub = (S > 1) ? (int)threadIdx.x / nout : 0;
-  float sh[TN_MAXOUT], sl[TN_MAXOUT];
+  const int kp = (k + 7) & ~7;                 // B rows padded with zeros to whole groups (8 or 16)
+  const int ksh = (kp == 8) ? 3 : 4;
+  E *Bs = reinterpret_cast<E *>(sm);           // [TN_TILE][kp]
+  const int tid = threadIdx.x;
+  const int G = m * (kp >> 3);
+  const int S = max(1, TS_THREADS / G);
+  const int g = tid % G, sub = tid / G;
+  const int i = g % m, jb = g / m;
+  const bool act = sub < S;
+  float h[8], l[8], t[8];
 #pragma unroll
-  for (int o = 0; o < TN_MAXOUT; ++o) { sh[o] = 0.f; sl[o] = 0.f; }
-  int64_t r0 = (int64_t)blockIdx.x * rows_per_blk;
-  int64_t r1 = min(n, r0 + rows_per_blk);
-  for (int64_t rt = r0; rt < r1; rt += TR) {
-    int rows = (int)min((int64_t)TR, r1 - rt);
-    for (int e = threadIdx.x; e < TR * m; e += blockDim.x) {
-      int rr = e / m, i = e - rr * m;
-      As[e] = (rr < rows) ? split_f64(A[(rt + rr) * lda + a0 + i]) : make_float2(0.f, 0.f);
-    }
-    for (int e = threadIdx.x; e < TR * k; e += blockDim.x) {
-      int rr = e / k, j = e - rr * k;
-      Bs[e] = (rr < rows) ? split_f64(B[(rt + rr) * ldb + b0 + j]) : make_float2(0.f, 0.f);
+  for (int j = 0; j < 8; ++j) { h[j] = 0.f; l[j] = 0.f; }
+  const int64_t r0 = (int64_t)blockIdx.x * rows_per_blk;
+  const int64_t r1 = min(n, r0 + rows_per_blk);
+  const double *ai = A + a0 + i;
+  for (int64_t rt = r0; rt < r1; rt += TN_TILE) {
+    const int rows = (int)min((int64_t)TN_TILE, r1 - rt);
+#pragma unroll 4
+    for (int e = tid; e < (TN_TILE << ksh); e += TS_THREADS) {
+      const int rr = e >> ksh, j = e & (kp - 1);
+      Bs[e] = (rr < rows && j < k) ? ts_load<LOWP>(B[(rt + rr) * ldb + b0 + j]) : E{};
     }
     __syncthreads();
-    if (S == 1) {
+    if (act) {
 #pragma unroll
-      for (int o = 0; o < TN_MAXOUT; ++o) {
-        int idx = threadIdx.x + o * TN_THREADS;
-        if (idx < nout) {
-          int i = idx / k, j = idx - i * k;
-          float h = sh[o], l = sl[o];
-          if (LOWP) {
-            float t = 0.f;
-            for (int rr = 0; rr < rows; ++rr) t = __fmaf_rn(As[rr * m + i].x, Bs[rr * k + j].x, t);
-            ff_fma(h, l, make_float2(t, 0.f), make_float2(1.f, 0.f));
-          } else {
-            for (int rr = 0; rr < rows; ++rr) ff_fma(h, l, As[rr * m + i], Bs[rr * k + j]);
-          }
-          ff_renorm(h, l);
-          sh[o] = h;
-          sl[o] = l;
+      for (int j = 0; j < 8; ++j) t[j] = 0.f;
+      const double *ar = ai + rt * lda;
+      int rr = sub;
+      for (; rr + 3 * S < rows; rr += 4 * S) {  // four rows in flight
+        double av[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) av[u] = __ldg(ar + (int64_t)(rr + u * S) * lda);
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          E b[8];
+          ts_load8<LOWP>(Bs + ((rr + u * S) << ksh) + 8 * jb, b);
+          if constexpr (LOWP) ts_fma8<true>(t, l, ts_load<true>(av[u]), b);
+          else ts_fma8<false>(h, l, ts_load<false>(av[u]), b);
         }
       }
-    } else if (sub < S) {
-      const int idx = (int)threadIdx.x - sub * nout, i = idx / k, j = idx - i * k;
-      float h = sh[0], l = sl[0];
-      if (LOWP) {
-        float t = 0.f;
-        for (int rr = sub; rr < rows; rr += S) t = __fmaf_rn(As[rr * m + i].x, Bs[rr * k + j].x, t);
-        ff_fma(h, l, make_float2(t, 0.f), make_float2(1.f, 0.f));
-      } else {
-        for (int rr = sub; rr < rows; rr += S) ff_fma(h, l, As[rr * m + i], Bs[rr * k + j]);
+      for (; rr < rows; rr += S) {
+        E b[8];
+        ts_load8<LOWP>(Bs + (rr << ksh) + 8 * jb, b);
+        if constexpr (LOWP) ts_fma8<true>(t, l, ts_load<true>(__ldg(ar + (int64_t)rr * lda)), b);
+        else ts_fma8<false>(h, l, ts_load<false>(__ldg(ar + (int64_t)rr * lda)), b);
       }
-      ff_renorm(h, l);
-      sh[0] = h;
-      sl[0] = l;
+      if constexpr (LOWP)
+#pragma unroll
+        for (int j = 0; j < 8; ++j) ff_fma(h[j], l[j], make_float2(t[j], 0.f), make_float2(1.f, 0.f));
+#pragma unroll
+      for (int j = 0; j < 8; ++j) ff_renorm(h[j], l[j]);
     }
     __syncthreads();
   }
-  if (S == 1) {
+  // combine the S shares of each output in FP64 (the tile is no longer needed)
+  double *red = sm;  // [S][G][8]
+  if (act)
 #pragma unroll
-    for (int o = 0; o < TN_MAXOUT; ++o) {
-      int idx = threadIdx.x + o * TN_THREADS;
-      if (idx < nout) partial[(int64_t)blockIdx.x * nout + idx] = (double)sh[o] + (double)sl[o];
-    }
-  } else {
-    // combine the S shares of each output in FP64, in a fixed order
-    double *red = sm;  // the tiles are no longer needed
-    red[threadIdx.x] = (sub < S) ? (double)sh[0] + (double)sl[0] : 0.0;
-    __syncthreads();
-    if ((int)threadIdx.x < nout) {
-      double t = 0.0;
-      for (int q = 0; q < S; ++q) t += red[threadIdx.x + q * nout];
-      partial[(int64_t)blockIdx.x * nout + threadIdx.x] = t;
-    }
+    for (int j = 0; j < 8; ++j) red[(sub * G + g) * 8 + j] = (double)h[j] + (double)l[j];
+  __syncthreads();
+  const int nout = m * k;
+  for (int o = tid; o < G * 8; o += TS_THREADS) {
+    const int g2 = o >> 3, jj = (g2 / m) * 8 + (o & 7);
+    if (jj >= k) continue;
+    double s = 0.0;
+    for (int q = 0; q < S; ++q) s += red[(q * G + g2) * 8 + (o & 7)];
+    partial[(int64_t)blockIdx.x * nout + (g2 % m) * k + jj] = s;
   }
 }
 
@@ -149,46 +191,59 @@ __global__ void k_reduce_partials(const double *__restrict__ partial, int nblk, 
 }
 
 // Out[r, o0+j] = beta*Out[r, o0+j] + alpha * sum_i A[r, a0+i] * Y[i*ldy + y0 + j]
-// (float-float sums as in k_tn, or FP32 sums when LOWP; alpha, beta and the update of Out
-// in FP64)
+// (m <= MAX_SUB, k <= NN_MAXK; float-float sums, or FP32 sums when LOWP; alpha, beta and
+// the update of Out in FP64).  Thread: one row and the 8 outputs of group jb; a block takes
+// NN_THREADS/jbp rows (jbp = groups rounded up to a power of two).  Y is split into shared
+// memory once per block; the thread reads its row of A from global memory, two elements
+// per load where the rows are 16-byte aligned, several loads in flight.  No barrier after
+// the staging of Y.
 template <bool LOWP>
 __global__ void __launch_bounds__(NN_THREADS) k_nn(int64_t n, const double *__restrict__ A, int lda, int a0, int m,
                                                    const double *__restrict__ Y, int ldy, int y0, int k, double alpha,
-                                                   double beta, double *Out, int ldo, int o0) {
+                                                   double beta, double *Out, int ldo, int o0, int jbp) {
+  using E = ts_elt<LOWP>;
   extern __shared__ double sm[];
-  float2 *Ys = reinterpret_cast<float2 *>(sm);  // [m][k]
-  constexpr int TR = LOWP ? 128 : 32;  // rows per tile (larger when the arithmetic is light)
-  float2 *As = Ys + m * k;              // [TR][m]
-  for (int e = threadIdx.x; e < m * k; e += blockDim.x) {
-    int i = e / k, j = e - i * k;
-    Ys[e] = split_f64(Y[i * ldy + y0 + j]);
+  const int kp = (k + 7) & ~7;
+  E *Ys = reinterpret_cast<E *>(sm);  // [m][kp], 16-byte aligned rows
+  const int tid = threadIdx.x;
+  for (int e = tid; e < m * kp; e += NN_THREADS) {
+    const int i = e / kp, j = e - i * kp;
+    Ys[e] = (j < k) ? ts_load<LOWP>(Y[i * ldy + y0 + j]) : E{};
   }
   __syncthreads();
-  for (int64_t rt = (int64_t)blockIdx.x * TR; rt < n; rt += (int64_t)gridDim.x * TR) {
-    int rows = (int)min((int64_t)TR, n - rt);
-    for (int e = threadIdx.x; e < TR * m; e += blockDim.x) {
-      int rr = e / m, i = e - rr * m;
-      As[e] = (rr < rows) ? split_f64(A[(rt + rr) * lda + a0 + i]) : make_float2(0.f, 0.f);
+  const int TR = NN_THREADS / jbp;
+  const int rr = tid % TR, jb = tid / TR;
+  const int64_t r = (int64_t)blockIdx.x * TR + rr;
+  if (8 * jb >= k || r >= n) return;
+  const double *ar = A + r * lda + a0;
+  const E *yj = Ys + 8 * jb;
+  float h[8], l[8];
+#pragma unroll
+  for (int j = 0; j < 8; ++j) { h[j] = 0.f; l[j] = 0.f; }
+  int i = 0;
+  if (((lda | a0) & 1) == 0) {
+#pragma unroll 4
+    for (; i + 1 < m; i += 2) {
+      const double2 v = __ldg(reinterpret_cast<const double2 *>(ar + i));
+      E y[8];
+      ts_load8<LOWP>(yj + i * kp, y);
+      ts_fma8<LOWP>(h, l, ts_load<LOWP>(v.x), y);
+      ts_load8<LOWP>(yj + (i + 1) * kp, y);
+      ts_fma8<LOWP>(h, l, ts_load<LOWP>(v.y), y);
     }
-    __syncthreads();
-    for (int e = threadIdx.x; e < TR * k; e += blockDim.x) {
-      int rr = e / k, j = e - rr * k;
-      if (rr < rows) {
-        double s;
-        if (LOWP) {
-          float t = 0.f;
-          for (int i = 0; i < m; ++i) t = __fmaf_rn(As[rr * m + i].x, Ys[i * k + j].x, t);
-          s = (double)t;
-        } else {
-          float h = 0.f, l = 0.f;
-          for (int i = 0; i < m; ++i) ff_fma(h, l, As[rr * m + i], Ys[i * k + j]);
-          s = (double)h + (double)l;
-        }
-        double *o = Out + (rt + rr) * ldo + o0 + j;
-        *o = (beta == 0.0) ? alpha * s : fma(beta, *o, alpha * s);
-      }
-    }
-    __syncthreads();
+  }
+#pragma unroll 4
+  for (; i < m; ++i) {
+    E y[8];
+    ts_load8<LOWP>(yj + i * kp, y);
+    ts_fma8<LOWP>(h, l, ts_load<LOWP>(__ldg(ar + i)), y);
+  }
+  double *o = Out + r * ldo + o0 + 8 * jb;
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    if (8 * jb + j >= k) break;
+    const double s = LOWP ? (double)h[j] : (double)h[j] + (double)l[j];
+    o[j] = (beta == 0.0) ? alpha * s : fma(beta, o[j], alpha * s);
   }
 }
 
@@ -237,18 +292,47 @@ __global__ void k_sum_cols(const double *partial, int nblk, int nr, double *out)
   out[j] = s;
 }
 
-// T[r, c] = R[r, sel[c]] / (D[r] - theta[sel[c]]) where |D - theta| > dmin, else R
+// T[r, c] = R[r, sel[c]] / (D[r] - theta[sel[c]]) where |D - theta| > dmin, else R.
+// The correction is a search direction (the basis is orthonormalised right after), so the
+// quotient is formed on the FP32 pipe: D - theta exactly enough in float-float (the
+// guard decision sees ~2^-48 relative error), then an FP32 quotient (~2^-23 relative) —
+// a slightly perturbed diagonal preconditioner.  FP64 division on GB300 is a sequence of
+// FP64-pipe instructions and bounded the kernel.  Consecutive threads take consecutive
+// elements of T (coalesced stores); U: 32-bit index arithmetic where n * nsel fits.
+__device__ __forceinline__ double f32_to_f64_bits(float f) {
+  // exact widening by bit manipulation (normal numbers and zero; others -> NaN or 0)
+  const unsigned u = (unsigned)__float_as_int(f);
+  const unsigned long long sign = (unsigned long long)(u & 0x80000000u) << 32;
+  const unsigned e = (u >> 23) & 0xff;
+  if (e == 0) return __longlong_as_double((long long)sign);
+  if (e == 0xff) return __longlong_as_double((long long)(sign | 0x7ff8000000000000ull));
+  const unsigned long long bits = sign | ((unsigned long long)(e + 1023 - 127) << 52) |
+                                  ((unsigned long long)(u & 0x7fffffu) << 29);
+  return __longlong_as_double((long long)bits);
+}
+
+template <typename U>
 __global__ void k_precond(int64_t n, int nr, const double *__restrict__ R, const double *__restrict__ D,
                           const double *__restrict__ theta, const int *__restrict__ sel, int nsel, double dmin,
                           double *__restrict__ T, int ldt) {
-  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n * nsel; e += (int64_t)gridDim.x * blockDim.x) {
-    int64_t r = e / nsel;
-    int c = (int)(e - r * nsel);
-    int j = sel[c];
-    double v = R[r * nr + j];
-    double d = D[r] - theta[j];
-    if (fabs(d) > dmin) v = v / d;
-    T[r * ldt + c] = v;
+  __shared__ float2 th[16];
+  __shared__ int js[16];
+  if ((int)threadIdx.x < nsel) {
+    js[threadIdx.x] = sel[threadIdx.x];
+    th[threadIdx.x] = split_f64(theta[sel[threadIdx.x]]);
+  }
+  __syncthreads();
+  const float dminf = (float)dmin;
+  const U total = (U)n * (U)nsel;
+  for (U e = (U)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (U)gridDim.x * blockDim.x) {
+    const U r = e / (U)nsel, c = e - r * (U)nsel;
+    const double v = R[(size_t)r * nr + js[c]];
+    const float2 dd = split_f64(D[r]);
+    const float dh = __fsub_rn(dd.x, th[c].x);                // exact when D and theta are close
+    const float d = __fadd_rn(dh, __fsub_rn(dd.y, th[c].y));
+    double t = v;
+    if (fabsf(d) > dminf) t = f32_to_f64_bits(__fdiv_rn(split_f64(v).x, d));
+    T[(size_t)r * ldt + c] = t;
   }
 }
 
@@ -321,17 +405,12 @@ __global__ void k_symmetrize(double *G, int ld, int m0, int m1) {
   }
 }
 
-// G = diag(theta[0:m]) after a collapse
-__global__ void k_diag_g(double *G, int ld, int m, const double *theta) {
-  for (int e = threadIdx.x; e < m * m; e += blockDim.x) {
-    int i = e / m, j = e % m;
-    G[i * ld + j] = (i == j) ? theta[i] : 0.0;
-  }
-}
-
-// One-CTA cyclic Jacobi (round-robin parallel ordering) for a symmetric m x m matrix.
-// Out: theta ascending, Y (ld x ld, column c = eigenvector c).  status: sweeps used, or
-// -1 if the off-diagonal norm did not fall below tolerance in max_sweeps.
+// One-CTA cyclic Jacobi (round-robin parallel ordering) for a symmetric m x m matrix: the
+// initial guess's block of H.  Out: theta ascending, Y (ld x ld, column c = eigenvector c).
+// status: sweeps used, or -1 if the off-diagonal norm did not fall below tolerance in
+// max_sweeps.  Rotations whose off-diagonal element is below 1e-13 |A|_F / m are skipped
+// (threshold Jacobi): when all are, the off-diagonal norm already passes the convergence
+// test (1e-13 |A|_F).
 __global__ void k_jacobi(const double *G, int ld, int m, double *theta, double *Y, int max_sweeps, int *status) {
   extern __shared__ double sm[];
   double *A = sm;                 // m x m
@@ -370,6 +449,7 @@ __global__ void k_jacobi(const double *G, int ld, int m, double *theta, double *
     __syncthreads();
     if (off <= 1e-26 * tot || off == 0.0) { converged = true; break; }
     ++sweeps;
+    const double rot_min = 1e-13 * sqrt(tot) / m;
     for (int rnd = 0; rnd < np - 1; ++rnd) {
       // pairs of this round
       for (int kq = tid; kq < np / 2; kq += nt) {
@@ -380,7 +460,7 @@ __global__ void k_jacobi(const double *G, int ld, int m, double *theta, double *
         double c = 1.0, s = 0.0;
         if (q < m) {
           double apq = A[p * m + q];
-          if (apq != 0.0) {
+          if (fabs(apq) > rot_min) {
             double tau = (A[q * m + q] - A[p * m + p]) / (2.0 * apq);
             double t = (tau >= 0.0 ? 1.0 : -1.0) / (fabs(tau) + sqrt(1.0 + tau * tau));
             c = 1.0 / sqrt(1.0 + t * t);
@@ -395,8 +475,8 @@ __global__ void k_jacobi(const double *G, int ld, int m, double *theta, double *
       for (int e = tid; e < (np / 2) * m; e += nt) {
         int kq = e / m, i = e % m;
         int p = pq[kq][0], q = pq[kq][1];
-        if (q >= m) continue;
         double c = cs[kq][0], s = cs[kq][1];
+        if (q >= m || s == 0.0) continue;
         double aip = A[i * m + p], aiq = A[i * m + q];
         A[i * m + p] = c * aip - s * aiq;
         A[i * m + q] = s * aip + c * aiq;
@@ -409,8 +489,8 @@ __global__ void k_jacobi(const double *G, int ld, int m, double *theta, double *
       for (int e = tid; e < (np / 2) * m; e += nt) {
         int kq = e / m, j = e % m;
         int p = pq[kq][0], q = pq[kq][1];
-        if (q >= m) continue;
         double c = cs[kq][0], s = cs[kq][1];
+        if (q >= m || s == 0.0) continue;
         double apj = A[p * m + j], aqj = A[q * m + j];
         A[p * m + j] = c * apj - s * aqj;
         A[q * m + j] = s * apj + c * aqj;
@@ -469,11 +549,15 @@ __global__ void k_set_unit(double *V, int ld, int c0, const int64_t *idx, int nr
   if (j < nr) V[idx[j] * ld + c0 + j] = 1.0;
 }
 
-__global__ void k_copy_cols(int64_t n, const double *src, int lds, int s0, double *dst, int ldd, int d0, int k) {
-  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n * k; e += (int64_t)gridDim.x * blockDim.x) {
-    int64_t r = e / k;
-    int j = (int)(e - r * k);
-    dst[r * ldd + d0 + j] = src[r * lds + s0 + j];
+// dst[r, d0+j] = src[r, s0+j], j < k; consecutive threads take consecutive elements
+// (coalesced); U: 32-bit index arithmetic where n * k fits
+template <typename U>
+__global__ void k_copy_cols(int64_t n, const double *__restrict__ src, int lds, int s0, double *__restrict__ dst,
+                            int ldd, int d0, int k) {
+  const U total = (U)n * (U)k;
+  for (U e = (U)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (U)gridDim.x * blockDim.x) {
+    const U r = e / (U)k, j = e - r * (U)k;
+    dst[(size_t)r * ldd + d0 + j] = src[(size_t)r * lds + s0 + j];
   }
 }
 
@@ -508,14 +592,16 @@ psoci_status tn(Work &w, const double *A, int lda, int a0, int m, const double *
                 int ldc, int c0, bool lowp_ok = false) {
   const bool lowp = w.lowp && lowp_ok;
   psoci_ctx *c = w.c;
-  if (m * k > TN_THREADS * TN_MAXOUT) return psoci_fail(c, PSOCI_ERR_INVALID_ARG, "tn: block too large");
-  const int tr = lowp ? 4 * TN_ROWS : TN_ROWS;  // rows per tile (k_tn)
-  size_t smem = sizeof(double) * std::max(tr * (m + k), TN_THREADS);
+  if (m < 1 || k < 1 || m > MAX_SUB || k > TN_MAXK) return psoci_fail(c, PSOCI_ERR_INVALID_ARG, "tn: block too large");
+  // B's tile, and at least the 16 KB of the FP64 combination of the shares
+  const int kp = (k + 7) & ~7;
+  const size_t smem = std::max<size_t>((size_t)TN_TILE * kp * (lowp ? sizeof(float) : sizeof(float2)),
+                                       sizeof(double) * TS_THREADS * 8);
   psoci_note_launch();
   if (lowp)
-    k_tn<true><<<w.nblk, TN_THREADS, smem, c->stream>>>(w.N, A, lda, a0, m, B, ldb, b0, k, w.partial, w.rows_per_blk);
+    k_tn<true><<<w.nblk, TS_THREADS, smem, c->stream>>>(w.N, A, lda, a0, m, B, ldb, b0, k, w.partial, w.rows_per_blk);
   else
-    k_tn<false><<<w.nblk, TN_THREADS, smem, c->stream>>>(w.N, A, lda, a0, m, B, ldb, b0, k, w.partial, w.rows_per_blk);
+    k_tn<false><<<w.nblk, TS_THREADS, smem, c->stream>>>(w.N, A, lda, a0, m, B, ldb, b0, k, w.partial, w.rows_per_blk);
   psoci_note_launch();
   k_reduce_partials<<<(m * k + 31) / 32, 256, 0, c->stream>>>(w.partial, w.nblk, m, k, C, ldc, c0);
   PSOCI_CUDA(c, cudaGetLastError());
@@ -526,18 +612,29 @@ psoci_status nn(Work &w, const double *A, int lda, int a0, int m, const double *
                 double beta, double *Out, int ldo, int o0, bool lowp_ok = false) {
   const bool lowp = w.lowp && lowp_ok;
   psoci_ctx *c = w.c;
-  const int tr = lowp ? 128 : 32;  // rows per tile (k_nn)
-  size_t smem = sizeof(double) * (m * k + tr * m);
-  int blocks = (int)std::min<int64_t>((w.N + tr - 1) / tr, 152 * 8);
+  if (m < 1 || k < 1 || m > MAX_SUB || k > NN_MAXK) return psoci_fail(c, PSOCI_ERR_INVALID_ARG, "nn: block too large");
+  const int groups = (k + 7) / 8;
+  const int jbp = groups == 1 ? 1 : groups == 2 ? 2 : 4;  // groups rounded up to a power of two
+  const int tr = NN_THREADS / jbp;                         // rows per block
+  const size_t smem = (lowp ? sizeof(float) : sizeof(float2)) * (size_t)m * 8 * groups;
+  const int64_t blocks = (w.N + tr - 1) / tr;
   psoci_note_launch();
   if (lowp)
-    k_nn<true><<<std::max(blocks, 1), NN_THREADS, smem, c->stream>>>(w.N, A, lda, a0, m, Y, ldy, y0, k, alpha, beta,
-                                                                     Out, ldo, o0);
+    k_nn<true><<<(unsigned)blocks, NN_THREADS, smem, c->stream>>>(w.N, A, lda, a0, m, Y, ldy, y0, k, alpha, beta, Out,
+                                                                  ldo, o0, jbp);
   else
-    k_nn<false><<<std::max(blocks, 1), NN_THREADS, smem, c->stream>>>(w.N, A, lda, a0, m, Y, ldy, y0, k, alpha, beta,
-                                                                      Out, ldo, o0);
+    k_nn<false><<<(unsigned)blocks, NN_THREADS, smem, c->stream>>>(w.N, A, lda, a0, m, Y, ldy, y0, k, alpha, beta, Out,
+                                                                   ldo, o0, jbp);
   PSOCI_CUDA(c, cudaGetLastError());
   return PSOCI_OK;
+}
+
+void copy_cols(Work &w, const double *src, int lds, double *dst, int ldd, int k) {
+  psoci_note_launch();
+  if (w.N * 32 < (int64_t)UINT32_MAX)
+    k_copy_cols<uint32_t><<<152 * 8, 256, 0, w.c->stream>>>(w.N, src, lds, 0, dst, ldd, 0, k);
+  else
+    k_copy_cols<uint64_t><<<152 * 8, 256, 0, w.c->stream>>>(w.N, src, lds, 0, dst, ldd, 0, k);
 }
 
 psoci_status sigma_block(Work &w, const double *X, int ldx, double *Y, int ldy, int k, psoci_prec prec) {
@@ -627,7 +724,7 @@ psoci_status psoci_davidson_impl(psoci_ctx *c, const psoci_dav_opts *o, double *
       (s = psoci_alloc(c, &w.theta, ld)) || (s = psoci_alloc(c, &w.X, (size_t)N * nr)) ||
       (s = psoci_alloc(c, &w.HX, (size_t)N * nr)) || (s = psoci_alloc(c, &w.R, (size_t)N * nr)) ||
       (s = psoci_alloc(c, &w.T, (size_t)N * nr)) || (s = psoci_alloc(c, &w.tmp, (size_t)N * std::max(nr, 2 * nr))) ||
-      (s = psoci_alloc(c, &w.partial, (size_t)w.nblk * TN_THREADS * TN_MAXOUT)) ||
+      (s = psoci_alloc(c, &w.partial, (size_t)w.nblk * MAX_SUB * TN_MAXK)) ||
       (s = psoci_alloc(c, &w.small, (size_t)ld * ld)) || (s = psoci_alloc(c, &w.F, 16 * 16)) ||
       (s = psoci_alloc(c, &w.norms, 16)) || (s = psoci_alloc(c, &w.sel, 16)) || (s = psoci_alloc(c, &w.ibuf, 4)) ||
       (s = psoci_alloc(c, &w.idx, 16)))
@@ -637,10 +734,6 @@ psoci_status psoci_davidson_impl(psoci_ctx *c, const psoci_dav_opts *o, double *
   cudaStream_t st = c->stream;
   const size_t jac_smem = sizeof(double) * 2 * MAX_SUB * MAX_SUB;
   PSOCI_CUDA(c, cudaFuncSetAttribute(k_jacobi, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)jac_smem));
-  PSOCI_CUDA(c, cudaFuncSetAttribute(k_nn<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 128 * 1024));
-  PSOCI_CUDA(c, cudaFuncSetAttribute(k_tn<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 128 * 1024));
-  PSOCI_CUDA(c, cudaFuncSetAttribute(k_nn<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024));
-  PSOCI_CUDA(c, cudaFuncSetAttribute(k_tn<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024));
   PSOCI_CUDA(c, cudaMemsetAsync(w.V, 0, sizeof(double) * N * ld, st));
   PSOCI_CUDA(c, cudaMemsetAsync(w.G, 0, sizeof(double) * ld * ld, st));
 
@@ -715,20 +808,26 @@ psoci_status psoci_davidson_impl(psoci_ctx *c, const psoci_dav_opts *o, double *
   psoci_note_launch();
   k_symmetrize<<<1, 256, 0, st>>>(w.G, ld, 0, m);
 
-  std::vector<double> h_norm(nr), h_theta(ld);
+  std::vector<double> h_norm(nr), h_theta(ld), h_g((size_t)ld * ld), h_y((size_t)ld * ld);
   std::vector<int> sel;
   bool done = false, stalled = false;
   double best_mixed = HUGE_VAL;  // smallest largest-residual of the FP32-element phase so far
   int no_gain = 0;               // iterations since it last fell by 30%
   psoci_status result = PSOCI_OK;
-  int jstat = 0;
   while (!done) {
     if (iters >= max_iter) { result = PSOCI_ERR_NOT_CONVERGED; break; }
     ++iters;
     if (refine_phase && prec != o->prec) ++refine_iters;
-    psoci_note_launch();
-    k_jacobi<<<1, 256, jac_smem, st>>>(w.G, ld, m, w.theta, w.Y, 60, w.ibuf);
-    PSOCI_CUDA(c, cudaGetLastError());
+    // Rayleigh-Ritz on the host (the reference's dsygv; the basis is orthonormal, so the
+    // metric is the identity): G down, eigenpairs up
+    PSOCI_CUDA(c, cudaMemcpy2DAsync(h_g.data(), sizeof(double) * ld, w.G, sizeof(double) * ld, sizeof(double) * m, m,
+                                    cudaMemcpyDeviceToHost, st));
+    PSOCI_CUDA(c, cudaStreamSynchronize(st));
+    if (psoci_subspace_eigen(m, h_g.data(), ld, h_theta.data(), h_y.data(), ld) != PSOCI_OK)
+      return psoci_fail(c, PSOCI_ERR_NUMERIC, "davidson: subspace eigen-solve failed");
+    PSOCI_CUDA(c, cudaMemcpy2DAsync(w.Y, sizeof(double) * ld, h_y.data(), sizeof(double) * ld, sizeof(double) * m, m,
+                                    cudaMemcpyHostToDevice, st));
+    PSOCI_CUDA(c, cudaMemcpyAsync(w.theta, h_theta.data(), sizeof(double) * m, cudaMemcpyHostToDevice, st));
     // Ritz vectors, their images and residuals
     if ((s = nn(w, w.V, ld, 0, m, w.Y, ld, 0, nr, 1.0, 0.0, w.X, nr, 0))) return s;
     if ((s = nn(w, w.HV, ld, 0, m, w.Y, ld, 0, nr, 1.0, 0.0, w.HX, nr, 0))) return s;
@@ -739,8 +838,6 @@ psoci_status psoci_davidson_impl(psoci_ctx *c, const psoci_dav_opts *o, double *
     k_sum_cols<<<1, 32, 0, st>>>(w.partial, rb, nr, w.norms);
     PSOCI_CUDA(c, cudaGetLastError());
     PSOCI_CUDA(c, cudaMemcpyAsync(h_norm.data(), w.norms, sizeof(double) * nr, cudaMemcpyDeviceToHost, st));
-    PSOCI_CUDA(c, cudaMemcpyAsync(h_theta.data(), w.theta, sizeof(double) * m, cudaMemcpyDeviceToHost, st));
-    PSOCI_CUDA(c, cudaMemcpyAsync(&jstat, w.ibuf, sizeof(int), cudaMemcpyDeviceToHost, st));
     PSOCI_CUDA(c, cudaStreamSynchronize(st));
     for (int j = 0; j < nr; ++j) {
       if (!std::isfinite(h_norm[j]) || !std::isfinite(h_theta[j]))
@@ -766,8 +863,8 @@ psoci_status psoci_davidson_impl(psoci_ctx *c, const psoci_dav_opts *o, double *
         if (!o->block) break;
       }
     if (c->verbose)
-      fprintf(stderr, "psoci davidson it=%d m=%d %s max|r|=%.3e e0=%.12f jacobi=%d\n", iters, m,
-              refine_phase ? "fp64" : "mixed", *std::max_element(h_norm.begin(), h_norm.end()), h_theta[0], jstat);
+      fprintf(stderr, "psoci davidson it=%d m=%d %s max|r|=%.3e e0=%.12f\n", iters, m, refine_phase ? "fp64" : "mixed",
+              *std::max_element(h_norm.begin(), h_norm.end()), h_theta[0]);
     if (sel.empty() || stalled) {
       stalled = false;
       if (!refine_phase && o->refine) {
@@ -793,21 +890,26 @@ psoci_status psoci_davidson_impl(psoci_ctx *c, const psoci_dav_opts *o, double *
     int nsel = (int)sel.size();
     PSOCI_CUDA(c, cudaMemcpyAsync(w.sel, sel.data(), sizeof(int) * nsel, cudaMemcpyHostToDevice, st));
     psoci_note_launch();
-    k_precond<<<(int)std::min<int64_t>((N * nsel + 255) / 256, 152 * 16), 256, 0, st>>>(N, nr, w.R, c->d_diag, w.theta,
-                                                                                         w.sel, nsel, dmin, w.T, nr);
+    {
+      const int pb = (int)std::min<int64_t>((N * nsel + 255) / 256, 152 * 16);
+      if (N * 32 < (int64_t)UINT32_MAX)
+        k_precond<uint32_t><<<pb, 256, 0, st>>>(N, nr, w.R, c->d_diag, w.theta, w.sel, nsel, dmin, w.T, nr);
+      else
+        k_precond<uint64_t><<<pb, 256, 0, st>>>(N, nr, w.R, c->d_diag, w.theta, w.sel, nsel, dmin, w.T, nr);
+    }
     PSOCI_CUDA(c, cudaGetLastError());
     if (m + nsel > maxsub) {
       // collapse onto the lowest keep Ritz vectors (reference: 2*nroots), V and HV alike
-      int keep = std::min(m, std::max(nr, std::min(2 * nr, maxsub - nsel)));
+      const int keep = std::min(m, std::max(nr, std::min(2 * nr, maxsub - nsel)));
       if ((s = nn(w, w.V, ld, 0, m, w.Y, ld, 0, keep, 1.0, 0.0, w.tmp, 2 * nr, 0))) return s;
-      psoci_note_launch();
-      k_copy_cols<<<152 * 8, 256, 0, st>>>(N, w.tmp, 2 * nr, 0, w.V, ld, 0, keep);
+      copy_cols(w, w.tmp, 2 * nr, w.V, ld, keep);
       if ((s = nn(w, w.HV, ld, 0, m, w.Y, ld, 0, keep, 1.0, 0.0, w.tmp, 2 * nr, 0))) return s;
-      psoci_note_launch();
-      k_copy_cols<<<152 * 8, 256, 0, st>>>(N, w.tmp, 2 * nr, 0, w.HV, ld, 0, keep);
-      psoci_note_launch();
-      k_diag_g<<<1, 256, 0, st>>>(w.G, ld, keep, w.theta);
-      PSOCI_CUDA(c, cudaGetLastError());
+      copy_cols(w, w.tmp, 2 * nr, w.HV, ld, keep);
+      // G = diag(theta[0:keep]) over the new basis
+      std::fill(h_g.begin(), h_g.end(), 0.0);
+      for (int i = 0; i < keep; ++i) h_g[(size_t)i * ld + i] = h_theta[i];
+      PSOCI_CUDA(c, cudaMemcpy2DAsync(w.G, sizeof(double) * ld, h_g.data(), sizeof(double) * ld,
+                                      sizeof(double) * keep, keep, cudaMemcpyHostToDevice, st));
       m = keep;
       ++collapses;
     }
