@@ -519,7 +519,7 @@ __global__ void k_jacobi(const double *G, int ld, int m, double *theta, double *
 
 // initial guess from the lowest diagonal block: map[row] = position of the row in idx
 __global__ void k_map_set(const int64_t *idx, int M, int32_t *map) {
-  for (int i = threadIdx.x; i < M; i += blockDim.x) map[idx[i]] = i;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < M; i += gridDim.x * blockDim.x) map[idx[i]] = i;
 }
 
 // Hs[i*M + j] = H[idx[i], idx[j]] from the stored rows (one warp per row)
@@ -561,6 +561,34 @@ __global__ void k_copy_cols(int64_t n, const double *__restrict__ src, int lds, 
   }
 }
 
+// Y[i, j] = sum_l A[i*n + l] X[l*ldx + j], j < k (k <= 16): the dense guess block applied in
+// FP64.  One warp per row (lanes stride the row, coalesced), k sums reduced across lanes.
+__global__ void k_dense_mv(int n, const double *__restrict__ A, const double *__restrict__ X, int ldx,
+                           double *__restrict__ Y, int ldy, int k) {
+  const int lane = threadIdx.x & 31;
+  const int i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (i >= n) return;
+  double acc[16];
+#pragma unroll
+  for (int j = 0; j < 16; ++j) acc[j] = 0.0;
+  const double *a = A + (int64_t)i * n;
+  for (int l = lane; l < n; l += 32) {
+    const double h = a[l];
+    const double *x = X + (int64_t)l * ldx;
+#pragma unroll
+    for (int j = 0; j < 16; ++j)
+      if (j < k) acc[j] = fma(h, x[j], acc[j]);
+  }
+#pragma unroll
+  for (int j = 0; j < 16; ++j) {
+    if (j >= k) break;
+    double v = acc[j];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0) Y[(int64_t)i * ldy + j] = v;
+  }
+}
+
 struct Work {
   psoci_ctx *c = nullptr;
   int64_t N = 0;
@@ -571,6 +599,9 @@ struct Work {
   float *x32 = nullptr;
   int *sel = nullptr, *ibuf = nullptr;
   int64_t *idx = nullptr;
+  // the operator: the context's Hamiltonian, or (dense != nullptr) a dense N x N FP64 block
+  // of it, the initial guess's subproblem
+  const double *dense = nullptr;
   int nblk = 0;
   int64_t rows_per_blk = 0;
   // FP32 subspace products allowed (the FP32-element phase of a mixed solve): used for the
@@ -644,7 +675,14 @@ psoci_status sigma_block(Work &w, const double *X, int ldx, double *Y, int ldy, 
   w.ev.push_back(e0);
   w.ev.push_back(e1);
   cudaEventRecord(e0, w.c->stream);
-  psoci_status s = psoci_sigma_launch(w.c, k, X, ldx, Y, ldy, prec, w.x32);
+  psoci_status s = PSOCI_OK;
+  if (w.dense) {
+    psoci_note_launch();
+    k_dense_mv<<<(unsigned)((w.N + 7) / 8), 256, 0, w.c->stream>>>((int)w.N, w.dense, X, ldx, Y, ldy, k);
+    if (cudaGetLastError() != cudaSuccess) s = psoci_fail(w.c, PSOCI_ERR_CUDA, "davidson: guess block product");
+  } else {
+    s = psoci_sigma_launch(w.c, k, X, ldx, Y, ldy, prec, w.x32);
+  }
   cudaEventRecord(e1, w.c->stream);
   return s;
 }
@@ -690,11 +728,17 @@ psoci_status orthonormalize(Work &w, int m, int b, int *bk) {
 
 }  // namespace
 
-psoci_status psoci_davidson_impl(psoci_ctx *c, const psoci_dav_opts *o, double *evals, double *evecs, double *rnorms,
-                                 psoci_dav_stats *stats) {
-  if (!c->have_h) return psoci_fail(c, PSOCI_ERR_STATE, "davidson: Hamiltonian not built");
-  if (!o) return psoci_fail(c, PSOCI_ERR_INVALID_ARG, "davidson: null options");
-  const int64_t N = c->nsef_total;
+namespace {
+
+constexpr int GUESS_M = 2048;  // order of the initial guess's block of H (lowest diagonal elements)
+
+// The solver over an operator of order N with diagonal diag (device): the context's
+// Hamiltonian (dense == nullptr), or a dense block of it for the initial guess (inner: unit
+// vectors as its own guess, no error text on non-convergence).  dX_out (device, N x nroots
+// row-major) receives the last Ritz vectors, converged or not.
+psoci_status davidson_run(psoci_ctx *c, int64_t N, const double *diag, const double *dense, const psoci_dav_opts *o,
+                          bool inner, double *evals, double *evecs, double *rnorms, psoci_dav_stats *stats,
+                          double *dX_out) {
   const int nr = o->nroots;
   if (nr < 1 || nr > 16 || nr > N) return psoci_fail(c, PSOCI_ERR_INVALID_ARG, "davidson: nroots must be 1..16 and <= N");
   int maxsub = o->max_subspace > 0 ? o->max_subspace : 4 * nr;
@@ -703,7 +747,7 @@ psoci_status psoci_davidson_impl(psoci_ctx *c, const psoci_dav_opts *o, double *
   if (maxsub < 2 * nr && N >= 2 * nr) return psoci_fail(c, PSOCI_ERR_INVALID_ARG, "davidson: subspace too small");
   if (o->prec != PSOCI_PREC_FP64 && o->prec != PSOCI_PREC_MIXED && o->prec != PSOCI_PREC_FF)
     return psoci_fail(c, PSOCI_ERR_INVALID_ARG, "davidson: unknown precision");
-  if (o->prec == PSOCI_PREC_MIXED && !c->d_val32 && !c->direct)
+  if (o->prec == PSOCI_PREC_MIXED && !dense && !c->d_val32 && !c->direct)
     return psoci_fail(c, PSOCI_ERR_STATE, "davidson: MIXED needs PSOCI_HMODE_CSR_BOTH");
   const double rtol = o->rtol > 0 ? o->rtol : 1e-6;
   const double dmin = o->precond_min > 0 ? o->precond_min : 1e-3;
@@ -713,6 +757,7 @@ psoci_status psoci_davidson_impl(psoci_ctx *c, const psoci_dav_opts *o, double *
   Work w;
   w.c = c;
   w.N = N;
+  w.dense = dense;
   w.nr = nr;
   w.ld = (maxsub + 1) & ~1;
   const int ld = w.ld;
@@ -740,9 +785,9 @@ psoci_status psoci_davidson_impl(psoci_ctx *c, const psoci_dav_opts *o, double *
   // guess: the lowest eigenvectors of H restricted to the M lowest diagonal elements (a
   // stored matrix), else unit vectors on the nr lowest diagonal elements
   std::vector<double> hdiag(N);
-  PSOCI_CUDA(c, cudaMemcpyAsync(hdiag.data(), c->d_diag, sizeof(double) * N, cudaMemcpyDeviceToHost, st));
+  PSOCI_CUDA(c, cudaMemcpyAsync(hdiag.data(), diag, sizeof(double) * N, cudaMemcpyDeviceToHost, st));
   PSOCI_CUDA(c, cudaStreamSynchronize(st));
-  const int M = (int)std::min<int64_t>(MAX_SUB, N);
+  const int M = inner ? nr : (int)std::min<int64_t>(GUESS_M, N);
   std::vector<int64_t> order(N);
   std::iota(order.begin(), order.end(), 0);
   std::partial_sort(order.begin(), order.begin() + M, order.end(),
@@ -752,7 +797,7 @@ psoci_status psoci_davidson_impl(psoci_ctx *c, const psoci_dav_opts *o, double *
   w.lowp = (prec == PSOCI_PREC_MIXED);
   const double tol_mixed = std::max(rtol, 1e-5);
   int m = nr;
-  if (c->guess_k > 0 && (int64_t)c->guess.size() == (int64_t)c->guess_k * N) {
+  if (!inner && c->guess_k > 0 && (int64_t)c->guess.size() == (int64_t)c->guess_k * N) {
     // restart vectors first, unit vectors on the lowest diagonal elements for the rest;
     // orthonormalised like any new block
     std::vector<double> t0((size_t)N * nr, 0.0);
@@ -766,16 +811,22 @@ psoci_status psoci_davidson_impl(psoci_ctx *c, const psoci_dav_opts *o, double *
     if (bk < 1) return psoci_fail(c, PSOCI_ERR_NUMERIC, "davidson: restart vectors are linearly dependent");
     m = bk;
     PSOCI_CUDA(c, cudaStreamSynchronize(st));
-  } else if (!c->direct && c->d_val && M > nr) {
+  } else if (!inner && !c->direct && c->d_val && M > nr) {
+    // the block of H on the M lowest diagonal elements (a stored matrix), its lowest
+    // eigenvectors scattered into V: a one-CTA Jacobi when it fits in shared memory, else
+    // this solver run on the dense block (FP64, residuals to 1e-4)
     int64_t *gidx = nullptr;
     int32_t *map = nullptr;
-    double *Hs = nullptr, *Ys = nullptr, *ths = nullptr;
+    double *Hs = nullptr, *Ys = nullptr, *ths = nullptr, *dg = nullptr;
     int *jst = nullptr;
     auto release = [&]() {
       psoci_free(gidx); psoci_free(map); psoci_free(Hs); psoci_free(Ys); psoci_free(ths); psoci_free(jst);
+      psoci_free(dg);
     };
+    const bool small = M <= MAX_SUB;
     if ((s = psoci_alloc(c, &gidx, M)) || (s = psoci_alloc(c, &map, N)) || (s = psoci_alloc(c, &Hs, (size_t)M * M)) ||
-        (s = psoci_alloc(c, &Ys, (size_t)M * M)) || (s = psoci_alloc(c, &ths, M)) || (s = psoci_alloc(c, &jst, 1))) {
+        (s = psoci_alloc(c, &Ys, small ? (size_t)M * M : (size_t)M * nr)) || (s = psoci_alloc(c, &ths, M)) ||
+        (s = psoci_alloc(c, &jst, 1)) || (s = psoci_alloc(c, &dg, M))) {
       release();
       return s;
     }
@@ -784,14 +835,37 @@ psoci_status psoci_davidson_impl(psoci_ctx *c, const psoci_dav_opts *o, double *
     if (e == cudaSuccess) e = cudaMemsetAsync(Hs, 0, sizeof(double) * M * M, st);
     if (e == cudaSuccess) {
       psoci_note_launch();
-      k_map_set<<<1, 128, 0, st>>>(gidx, M, map);
+      k_map_set<<<(M + 127) / 128, 128, 0, st>>>(gidx, M, map);
       psoci_note_launch();
       k_extract_block<<<(M + 7) / 8, 256, 0, st>>>(c->d_rowptr, c->d_col, c->d_val, gidx, M, map, Hs);
+      e = cudaGetLastError();
+    }
+    if (e == cudaSuccess && small) {
       psoci_note_launch();
-      k_jacobi<<<1, 256, jac_smem, st>>>(Hs, M, M, ths, Ys, 3, jst);  // a few sweeps: a guess
+      k_jacobi<<<1, 256, jac_smem, st>>>(Hs, M, M, ths, Ys, 60, jst);
       psoci_note_launch();
       k_scatter_guess<<<1, 256, 0, st>>>(Ys, M, gidx, M, nr, w.V, ld);
       e = cudaGetLastError();
+    } else if (e == cudaSuccess) {
+      // diagonal of the block (stride M + 1), then the inner solve
+      e = cudaMemcpy2DAsync(dg, sizeof(double), Hs, sizeof(double) * (M + 1), sizeof(double), M,
+                            cudaMemcpyDeviceToDevice, st);
+      if (e == cudaSuccess) {
+        psoci_dav_opts oi = *o;
+        oi.rtol = 1e-4;
+        oi.prec = PSOCI_PREC_FP64;
+        oi.refine = 0;
+        oi.block = 1;
+        oi.max_iter = 100;
+        const psoci_status si = davidson_run(c, M, dg, Hs, &oi, true, nullptr, nullptr, nullptr, nullptr, Ys);
+        if (si != PSOCI_OK && si != PSOCI_ERR_NOT_CONVERGED) {
+          release();
+          return si;
+        }
+        psoci_note_launch();
+        k_scatter_guess<<<(M * nr + 255) / 256, 256, 0, st>>>(Ys, nr, gidx, M, nr, w.V, ld);
+        e = cudaGetLastError();
+      }
     }
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     release();
@@ -863,8 +937,8 @@ psoci_status psoci_davidson_impl(psoci_ctx *c, const psoci_dav_opts *o, double *
         if (!o->block) break;
       }
     if (c->verbose)
-      fprintf(stderr, "psoci davidson it=%d m=%d %s max|r|=%.3e e0=%.12f\n", iters, m, refine_phase ? "fp64" : "mixed",
-              *std::max_element(h_norm.begin(), h_norm.end()), h_theta[0]);
+      fprintf(stderr, "psoci davidson%s it=%d m=%d %s max|r|=%.3e e0=%.12f\n", inner ? " (guess block)" : "", iters, m,
+              refine_phase ? "fp64" : "mixed", *std::max_element(h_norm.begin(), h_norm.end()), h_theta[0]);
     if (sel.empty() || stalled) {
       stalled = false;
       if (!refine_phase && o->refine) {
@@ -893,9 +967,9 @@ psoci_status psoci_davidson_impl(psoci_ctx *c, const psoci_dav_opts *o, double *
     {
       const int pb = (int)std::min<int64_t>((N * nsel + 255) / 256, 152 * 16);
       if (N * 32 < (int64_t)UINT32_MAX)
-        k_precond<uint32_t><<<pb, 256, 0, st>>>(N, nr, w.R, c->d_diag, w.theta, w.sel, nsel, dmin, w.T, nr);
+        k_precond<uint32_t><<<pb, 256, 0, st>>>(N, nr, w.R, diag, w.theta, w.sel, nsel, dmin, w.T, nr);
       else
-        k_precond<uint64_t><<<pb, 256, 0, st>>>(N, nr, w.R, c->d_diag, w.theta, w.sel, nsel, dmin, w.T, nr);
+        k_precond<uint64_t><<<pb, 256, 0, st>>>(N, nr, w.R, diag, w.theta, w.sel, nsel, dmin, w.T, nr);
     }
     PSOCI_CUDA(c, cudaGetLastError());
     if (m + nsel > maxsub) {
@@ -957,6 +1031,17 @@ psoci_status psoci_davidson_impl(psoci_ctx *c, const psoci_dav_opts *o, double *
     }
     stats->sigma_seconds = sig;
   }
-  if (result != PSOCI_OK) return psoci_fail(c, result, "davidson: did not converge within the iteration limit");
+  if (dX_out) PSOCI_CUDA(c, cudaMemcpyAsync(dX_out, w.X, sizeof(double) * N * nr, cudaMemcpyDeviceToDevice, st));
+  if (result != PSOCI_OK)
+    return inner ? result : psoci_fail(c, result, "davidson: did not converge within the iteration limit");
   return PSOCI_OK;
+}
+
+}  // namespace
+
+psoci_status psoci_davidson_impl(psoci_ctx *c, const psoci_dav_opts *o, double *evals, double *evecs, double *rnorms,
+                                 psoci_dav_stats *stats) {
+  if (!c->have_h) return psoci_fail(c, PSOCI_ERR_STATE, "davidson: Hamiltonian not built");
+  if (!o) return psoci_fail(c, PSOCI_ERR_INVALID_ARG, "davidson: null options");
+  return davidson_run(c, c->nsef_total, c->d_diag, nullptr, o, false, evals, evecs, rnorms, stats, nullptr);
 }
