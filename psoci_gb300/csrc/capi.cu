@@ -72,6 +72,9 @@ psoci_status psoci_create(psoci_ctx **out, const psoci_opts *opts) {
     delete c;
     return PSOCI_ERR_CUDA;
   }
+  size_t free_b = 0, total_b = 0;
+  if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess) c->pool_cap = total_b / 2;
+  cudaGetLastError();
   *out = c;
   return PSOCI_OK;
 }
@@ -81,6 +84,9 @@ void psoci_destroy(psoci_ctx *c) {
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
   release_all(c);
+  psoci_pool_flush(c);
+  psoci_pool_forget(c);
+  c->pool_cap = 0;
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
 }

@@ -4,6 +4,7 @@
 #include <stdint.h>
 
 #include <algorithm>
+#include <map>
 #include <string>
 #include <thread>
 #include <vector>
@@ -28,6 +29,9 @@ struct psoci_ctx {
   int verbose = 0;
   cudaStream_t stream = nullptr;
   std::string err;
+  // released device blocks kept for reuse (size -> pointer), see psoci_alloc
+  std::multimap<size_t, void *> pool;
+  size_t pool_bytes = 0, pool_cap = 0;
 
   // integrals
   int nbf = 0;
@@ -145,13 +149,24 @@ psoci_status psoci_cuda_fail(psoci_ctx *c, cudaError_t e, const char *where);
     if (_e != cudaSuccess) return psoci_cuda_fail((c), _e, #call);     \
   } while (0)
 
+// Device memory of a context goes through a cache (util.cu): a released block is kept for
+// a later allocation of the same context of at most 25% smaller size, so a repeated build
+// or solve reuses its buffers instead of paying cudaFree (which waits for the device) and
+// cudaMalloc (page mapping) for tens of GB each time.  Reuse waits for the context's stream
+// first, as cudaFree would have.  The cache holds at most half the device memory, is
+// emptied when cudaMalloc fails (and the allocation retried) and on psoci_destroy.
+void *psoci_device_alloc(psoci_ctx *c, size_t bytes, cudaError_t *err);
+void psoci_device_free(void *p);
+void psoci_pool_flush(psoci_ctx *c);
+void psoci_pool_forget(psoci_ctx *c);
+
 template <typename T>
 psoci_status psoci_alloc(psoci_ctx *c, T **p, size_t count) {
-  if (*p) { cudaFree(*p); *p = nullptr; }
+  if (*p) { psoci_device_free((void *)*p); *p = nullptr; }
   if (count == 0) count = 1;
-  cudaError_t e = cudaMalloc((void **)p, count * sizeof(T));
-  if (e != cudaSuccess) {
-    *p = nullptr;
+  cudaError_t e = cudaSuccess;
+  *p = (T *)psoci_device_alloc(c, count * sizeof(T), &e);
+  if (!*p) {
     cudaGetLastError();
     return psoci_fail(c, e == cudaErrorMemoryAllocation ? PSOCI_ERR_NOMEM : PSOCI_ERR_CUDA,
                       std::string("cudaMalloc: ") + cudaGetErrorString(e));
@@ -160,7 +175,7 @@ psoci_status psoci_alloc(psoci_ctx *c, T **p, size_t count) {
 }
 template <typename T>
 void psoci_free(T *&p) {
-  if (p) cudaFree(p);
+  psoci_device_free((void *)p);
   p = nullptr;
 }
 

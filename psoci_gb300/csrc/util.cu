@@ -1,6 +1,8 @@
 // Error helpers and the device-wide exclusive scan used by the builders.
 #include <atomic>
 #include <cstdio>
+#include <mutex>
+#include <unordered_map>
 
 #include "psoci_internal.cuh"
 
@@ -12,6 +14,95 @@ extern "C" unsigned long long psoci_launch_count(void) { return g_launches.load(
 psoci_status psoci_fail(psoci_ctx *c, psoci_status s, const std::string &msg) {
   if (c) c->err = msg;
   return s;
+}
+
+// The device-memory cache of psoci_alloc.  Owner and size of every live block, process-wide
+// (a block may be released while another context's call is running).
+namespace {
+std::mutex g_blocks_mu;
+std::unordered_map<void *, std::pair<psoci_ctx *, size_t>> g_blocks;
+}  // namespace
+
+void *psoci_device_alloc(psoci_ctx *c, size_t bytes, cudaError_t *err) {
+  if (bytes == 0) bytes = 1;
+  void *p = nullptr;
+  if (!c) {
+    *err = cudaMalloc(&p, bytes);
+    return (*err == cudaSuccess) ? p : nullptr;
+  }
+  auto it = c->pool.lower_bound(bytes);
+  if (it != c->pool.end() && it->first - bytes <= bytes / 4) {
+    const size_t sz = it->first;
+    p = it->second;
+    c->pool.erase(it);
+    c->pool_bytes -= sz;
+    // work of this context that used the block before its release ends first (cudaFree
+    // would have waited for it)
+    const cudaError_t e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) {
+      cudaFree(p);
+      *err = e;
+      return nullptr;
+    }
+    std::lock_guard<std::mutex> g(g_blocks_mu);
+    g_blocks[p] = {c, sz};
+    *err = cudaSuccess;
+    return p;
+  }
+  cudaError_t e = cudaMalloc(&p, bytes);
+  if (e == cudaErrorMemoryAllocation && !c->pool.empty()) {
+    cudaGetLastError();
+    psoci_pool_flush(c);
+    e = cudaMalloc(&p, bytes);
+  }
+  if (e != cudaSuccess) {
+    *err = e;
+    return nullptr;
+  }
+  std::lock_guard<std::mutex> g(g_blocks_mu);
+  g_blocks[p] = {c, bytes};
+  *err = cudaSuccess;
+  return p;
+}
+
+void psoci_device_free(void *p) {
+  if (!p) return;
+  psoci_ctx *c = nullptr;
+  size_t sz = 0;
+  {
+    std::lock_guard<std::mutex> g(g_blocks_mu);
+    auto it = g_blocks.find(p);
+    if (it != g_blocks.end()) {
+      c = it->second.first;
+      sz = it->second.second;
+      g_blocks.erase(it);
+    }
+  }
+  if (c && c->pool_bytes + sz <= c->pool_cap) {
+    c->pool.insert({sz, p});
+    c->pool_bytes += sz;
+    return;
+  }
+  cudaFree(p);
+}
+
+void psoci_pool_flush(psoci_ctx *c) {
+  for (auto &kv : c->pool) cudaFree(kv.second);
+  c->pool.clear();
+  c->pool_bytes = 0;
+}
+
+// blocks of a context that is going away and were never released
+void psoci_pool_forget(psoci_ctx *c) {
+  std::lock_guard<std::mutex> g(g_blocks_mu);
+  for (auto it = g_blocks.begin(); it != g_blocks.end();) {
+    if (it->second.first == c) {
+      cudaFree(it->first);
+      it = g_blocks.erase(it);
+    } else {
+      ++it;
+    }
+  }
 }
 
 psoci_status psoci_cuda_fail(psoci_ctx *c, cudaError_t e, const char *where) {
