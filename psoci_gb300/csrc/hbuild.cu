@@ -2236,6 +2236,15 @@ void psoci_join_release(psoci_ctx *c) {
 // configurations are numbered in ascending (hi pattern, lo pattern) order with lo patterns
 // numbered by first appearance, and the tables stay small; otherwise the all-pairs screen
 // is used.  Not qualifying is not an error.
+namespace {
+// the configuration of each (lo pattern, hi pattern) cell; the pairs are unique
+__global__ void k_fill_T(int n, const int32_t *__restrict__ gid, const int32_t *__restrict__ lid, int64_t G,
+                         int32_t *__restrict__ T) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    T[(int64_t)lid[i] * G + gid[i]] = i;
+}
+}  // namespace
+
 psoci_status psoci_join_prepare(psoci_ctx *c) {
   psoci_join_release(c);
   const int n = c->nconf, nbf = c->nbf;
@@ -2325,25 +2334,46 @@ psoci_status psoci_join_prepare(psoci_ctx *c) {
       if (gid[i] == gid[i - 1] && lid[i] <= lid[i - 1]) return PSOCI_OK;
   }
   if (G * L > ((int64_t)1 << 26)) return PSOCI_OK;
-  std::vector<int32_t> T((size_t)(G * L), -1), hdec((size_t)G);
-  for (int i = 0; i < n; ++i) T[(size_t)lid[i] * G + gid[i]] = i;  // [lo pattern][hi pattern]
+  std::vector<int32_t> hdec((size_t)G);
   hdec[0] = 0;
   for (int a = 0; a < nh; ++a) hdec[1 + a] = 1 | (a << 8);
   for (int b = 0; b < nh; ++b)
     for (int a = 0; a <= b; ++a)
       hdec[1 + nh + (size_t)b * (b + 1) / 2 + a] = (a == b) ? (3 | (a << 8)) : (2 | (a << 8) | (b << 20));
-  // lo patterns within tau = 1..4 of each lo pattern (itself included), ascending
-  std::vector<int32_t> lnoff(4 * (L + 1)), ln;
-  for (int tau = 1; tau <= 4; ++tau)
-    for (int64_t l = 0; l <= L; ++l) {
-      lnoff[(tau - 1) * (L + 1) + l] = (int32_t)ln.size();
-      if (l == L) break;
-      for (int64_t m = 0; m < L; ++m)
-        if (__builtin_popcount(lokey[l] ^ lokey[m]) <= tau) ln.push_back((int32_t)m);
+  // lo patterns within tau = 1..4 of each lo pattern (itself included), ascending; lists
+  // tau-major, then by pattern.  One distance per pair, counted then written in parallel.
+  std::vector<int32_t> lnoff(4 * (L + 1)), ln, lcnt((size_t)4 * L, 0);
+  psoci_parallel_ranges(L, [&](int64_t lo, int64_t hi, int) {
+    for (int64_t l = lo; l < hi; ++l)
+      for (int64_t m = 0; m < L; ++m) {
+        const int d = __builtin_popcount(lokey[l] ^ lokey[m]);
+        for (int tau = std::max(d, 1); tau <= 4; ++tau) ++lcnt[(size_t)(tau - 1) * L + l];
+      }
+  }, 64);
+  {
+    int64_t run = 0;
+    for (int tau = 1; tau <= 4; ++tau) {
+      for (int64_t l = 0; l < L; ++l) {
+        lnoff[(tau - 1) * (L + 1) + l] = (int32_t)run;
+        run += lcnt[(size_t)(tau - 1) * L + l];
+      }
+      lnoff[(tau - 1) * (L + 1) + L] = (int32_t)run;
     }
+    ln.resize((size_t)run);
+  }
+  psoci_parallel_ranges(L, [&](int64_t lo, int64_t hi, int) {
+    for (int64_t l = lo; l < hi; ++l) {
+      int32_t pos[4];
+      for (int tau = 1; tau <= 4; ++tau) pos[tau - 1] = lnoff[(tau - 1) * (L + 1) + l];
+      for (int64_t m = 0; m < L; ++m) {
+        const int d = __builtin_popcount(lokey[l] ^ lokey[m]);
+        for (int tau = std::max(d, 1); tau <= 4; ++tau) ln[pos[tau - 1]++] = (int32_t)m;
+      }
+    }
+  }, 64);
   psoci_status st;
   if ((st = psoci_alloc(c, &c->d_jgid, n)) || (st = psoci_alloc(c, &c->d_jlid, n)) ||
-      (st = psoci_alloc(c, &c->d_jT, T.size())) || (st = psoci_alloc(c, &c->d_jlnoff, lnoff.size())) ||
+      (st = psoci_alloc(c, &c->d_jT, (size_t)(G * L))) || (st = psoci_alloc(c, &c->d_jlnoff, lnoff.size())) ||
       (st = psoci_alloc(c, &c->d_jln, ln.size())) || (st = psoci_alloc(c, &c->d_jhdec, hdec.size())) ||
       (st = psoci_alloc(c, &c->d_jlokey, lokey.size()))) {
     psoci_join_release(c);
@@ -2352,7 +2382,11 @@ psoci_status psoci_join_prepare(psoci_ctx *c) {
   cudaStream_t q = c->stream;
   PSOCI_CUDA(c, cudaMemcpyAsync(c->d_jgid, gid.data(), 4 * gid.size(), cudaMemcpyHostToDevice, q));
   PSOCI_CUDA(c, cudaMemcpyAsync(c->d_jlid, lid.data(), 4 * lid.size(), cudaMemcpyHostToDevice, q));
-  PSOCI_CUDA(c, cudaMemcpyAsync(c->d_jT, T.data(), 4 * T.size(), cudaMemcpyHostToDevice, q));
+  // T[lo pattern][hi pattern] = configuration (or -1), filled on the device
+  PSOCI_CUDA(c, cudaMemsetAsync(c->d_jT, 0xff, sizeof(int32_t) * (size_t)(G * L), q));
+  psoci_note_launch();
+  k_fill_T<<<(n + 255) / 256, 256, 0, q>>>(n, c->d_jgid, c->d_jlid, G, c->d_jT);
+  PSOCI_CUDA(c, cudaGetLastError());
   PSOCI_CUDA(c, cudaMemcpyAsync(c->d_jlnoff, lnoff.data(), 4 * lnoff.size(), cudaMemcpyHostToDevice, q));
   PSOCI_CUDA(c, cudaMemcpyAsync(c->d_jln, ln.data(), 4 * std::max<size_t>(ln.size(), 1), cudaMemcpyHostToDevice, q));
   PSOCI_CUDA(c, cudaMemcpyAsync(c->d_jhdec, hdec.data(), 4 * hdec.size(), cudaMemcpyHostToDevice, q));

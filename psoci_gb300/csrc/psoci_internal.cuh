@@ -125,10 +125,10 @@ struct psoci_ctx {
 // host loops over configurations: f(lo, hi, t) on contiguous ranges of [0, n), one thread
 // per host core (ranges of at least 16384), t = 0..threads-1; returns the thread count
 template <class F>
-int psoci_parallel_ranges(int64_t n, F &&f) {
+int psoci_parallel_ranges(int64_t n, F &&f, int64_t grain = 16384) {
   int nt = (int)std::thread::hardware_concurrency();
   if (nt < 1) nt = 1;
-  nt = (int)std::min<int64_t>(nt, std::max<int64_t>(1, n / 16384));
+  nt = (int)std::min<int64_t>(nt, std::max<int64_t>(1, n / std::max<int64_t>(grain, 1)));
   if (nt <= 1) {
     f((int64_t)0, n, 0);
     return 1;

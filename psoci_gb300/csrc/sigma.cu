@@ -117,9 +117,11 @@ __global__ void __launch_bounds__(SIG_THREADS) k_spmm_f64(int64_t nrows, const i
   }
 }
 
-// the 8 floats at p (32-byte aligned) in one 256-bit read-only load
+// the 8 floats at p (32-byte aligned) in one 256-bit load, cached in L2 only: the gathered
+// rows are rarely reused from L1 (hit rate ~9%), and skipping it took 8% off the 8-vector
+// sigma (128-bit rows of narrow blocks keep the read-only path, which was faster for them)
 __device__ __forceinline__ void ldg_row8(float (&f)[8], const float *p) {
-  asm("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+  asm("ld.global.cg.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
       : "=f"(f[0]), "=f"(f[1]), "=f"(f[2]), "=f"(f[3]), "=f"(f[4]), "=f"(f[5]), "=f"(f[6]), "=f"(f[7])
       : "l"(p));
 }
@@ -264,10 +266,10 @@ __global__ void __launch_bounds__(SIG_THREADS) k_spmm_ff(int64_t nrows, const in
       if (K == 8) {
         // 8 pairs = 64 contiguous, 64-byte-aligned bytes: two 256-bit loads
         float f[16];
-        asm("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+        asm("ld.global.cg.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
             : "=f"(f[0]), "=f"(f[1]), "=f"(f[2]), "=f"(f[3]), "=f"(f[4]), "=f"(f[5]), "=f"(f[6]), "=f"(f[7])
             : "l"(xr));
-        asm("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+        asm("ld.global.cg.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
             : "=f"(f[8]), "=f"(f[9]), "=f"(f[10]), "=f"(f[11]), "=f"(f[12]), "=f"(f[13]), "=f"(f[14]), "=f"(f[15])
             : "l"(xr + 4));
 #pragma unroll
