@@ -13,10 +13,14 @@
 // each iteration, so one pass over H serves the whole block (block = 0 keeps the
 // reference's one-vector step).  The basis is kept orthonormal (CGS2 against V, then
 // Cholesky-QR twice inside the new block), so S = I and the generalised problem of the
-// reference reduces to a symmetric one, solved by a one-CTA cyclic Jacobi in FP64.
+// reference reduces to a symmetric one, solved on the host each iteration
+// (psoci_subspace_eigen, symeig.cpp), as the reference's dsygv is.
+//
+// Initial guess: the lowest eigenvectors of H on the 3072 lowest diagonal elements, found
+// by this same solver run on that dense block (a one-CTA Jacobi for blocks of at most 96).
 //
 // Vectors are N x ld row-major: the k entries of one SEF row are contiguous, which is
-// what the sigma kernel gathers.  All subspace arithmetic is FP64.
+// what the sigma kernel gathers.  All subspace arithmetic is FP64 or float-float.
 #include <algorithm>
 #include <chrono>
 #include <cmath>
@@ -35,7 +39,7 @@ constexpr int TN_MAXK = 16;       // k_tn: B columns (two groups of 8 outputs pe
 constexpr int TN_TILE = 256;      // k_tn: rows of B staged per tile
 constexpr int NN_THREADS = 128;   // k_nn block size
 constexpr int NN_MAXK = 32;       // k_nn: Y columns (four groups of 8 outputs per row)
-constexpr int MAX_SUB = 96;       // Jacobi keeps two m x m FP64 matrices in shared memory
+constexpr int MAX_SUB = 96;       // subspace limit; the guess Jacobi keeps two m x m FP64 matrices in shared memory
 
 // The tall-skinny products below run in float-float arithmetic on the FP32 pipe (see
 // ffmath.cuh): on GB300 the FP64 pipe issues ~2 FMA/clk/SM against 128 FP32 lanes, and
@@ -730,7 +734,7 @@ psoci_status orthonormalize(Work &w, int m, int b, int *bk) {
 
 namespace {
 
-constexpr int GUESS_M = 2048;  // order of the initial guess's block of H (lowest diagonal elements)
+constexpr int GUESS_M = 3072;  // order of the initial guess's block of H (lowest diagonal elements)
 
 // The solver over an operator of order N with diagonal diag (device): the context's
 // Hamiltonian (dense == nullptr), or a dense block of it for the initial guess (inner: unit
