@@ -190,7 +190,12 @@ psoci_status psoci_set_configs(psoci_ctx *c, int nbf, int nelec, int ksym, int m
   c->nconf = nconf;
   c->words = W;
   c->h_jsym.assign(jsym, jsym + nconf);
-  c->h_occ.assign(occ, occ + (size_t)nconf * nbf);
+  // host copy of the occupations, in parallel (a repeated call with the same size reuses
+  // the buffer: no fill)
+  if (c->h_occ.size() != (size_t)nconf * nbf) c->h_occ.assign((size_t)nconf * nbf, 0);
+  psoci_parallel_ranges(nconf, [&](int64_t lo, int64_t hi, int) {
+    memcpy(c->h_occ.data() + (size_t)lo * nbf, occ + (size_t)lo * nbf, (size_t)(hi - lo) * nbf);
+  });
   c->slab_hint = 0;
   c->join_hint = 0;
   c->have_cfgs = true;

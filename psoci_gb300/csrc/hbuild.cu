@@ -2304,14 +2304,21 @@ psoci_status psoci_join_prepare(psoci_ctx *c) {
   // is a chain of constraints; a topological order of all of them (ties broken by first
   // appearance) exists unless two groups order some patterns differently.
   {
-    std::vector<std::vector<int32_t>> next((size_t)L);
-    std::vector<int32_t> indeg((size_t)L, 0);
+    // constraint edges lid[i-1] -> lid[i] within a hi pattern, as a compressed adjacency
+    std::vector<int32_t> indeg((size_t)L, 0), eoff((size_t)L + 1, 0), next;
     for (int i = 1; i < n; ++i)
       if (gid[i] == gid[i - 1]) {
         if (lid[i] == lid[i - 1]) return PSOCI_OK;  // repeated configuration
-        next[lid[i - 1]].push_back(lid[i]);
+        ++eoff[lid[i - 1] + 1];
         ++indeg[lid[i]];
       }
+    for (int64_t l = 0; l < L; ++l) eoff[l + 1] += eoff[l];
+    next.resize((size_t)eoff[L]);
+    {
+      std::vector<int32_t> fill(eoff.begin(), eoff.end() - 1);
+      for (int i = 1; i < n; ++i)
+        if (gid[i] == gid[i - 1]) next[fill[lid[i - 1]]++] = lid[i];
+    }
     std::vector<int32_t> order;
     order.reserve((size_t)L);
     std::priority_queue<int32_t, std::vector<int32_t>, std::greater<int32_t>> ready;
@@ -2321,8 +2328,8 @@ psoci_status psoci_join_prepare(psoci_ctx *c) {
       const int32_t l = ready.top();
       ready.pop();
       order.push_back(l);
-      for (int32_t m : next[l])
-        if (--indeg[m] == 0) ready.push(m);
+      for (int32_t e = eoff[l]; e < eoff[l + 1]; ++e)
+        if (--indeg[next[e]] == 0) ready.push(next[e]);
     }
     if ((int64_t)order.size() != L) return PSOCI_OK;  // contradictory orders
     std::vector<int32_t> rank((size_t)L);
