@@ -283,10 +283,16 @@ def run_ours(args):
 
     cpu = None
     cpu_den = None
+    row_check = None
+    parity_cfg1 = None
     if rank == 0 and not args.no_cpu:
-        cpu = cpu_estimate(p, args.cpu_rows, args.cpu_sample, r_fp64.sigma_calls)
+        sample = {}
+        cpu = cpu_estimate(p, args.cpu_rows, args.cpu_sample, r_fp64.sigma_calls, keep=sample)
         cpu["nnz_full_measured"] = int(nnz)
+        row_check = check_rows(ctx, p, sample)
         cpu_den = cpu_density_estimate(p, args.cpu_density_rows)
+    if rank == 0 and not args.no_parity:
+        parity_cfg1 = roots_vs_oracle("mrcis_6e8o_v40", NROOTS, args.seed, args.ksym, local)
 
     if rank == 0:
         clocks = clk.summary()
@@ -341,6 +347,8 @@ def run_ours(args):
                                     "fp64_steps": int(l_fp64)},
             "clocks": clocks,
             "cpu_baseline": cpu,
+            "row_check": row_check,
+            "parity_mrcis_6e8o_v40": parity_cfg1,
         }
         print(json.dumps(out))
     ctx.close()
@@ -351,7 +359,62 @@ def run_ours(args):
 SIGMA_VECTORS = {"mrcisd_6e8o_v64": 121, "mrcis_6e8o_v40": 137}
 
 
-def cpu_estimate(p, rows_sample, sigma_sample, sigma_vectors, seed=0):
+def check_rows(ctx, p, sample):
+    """The sampled oracle rows (the reference's lower-triangle rows of the configurations the
+    CPU build sample drew) against the same rows of the GPU's stored matrix: equal columns,
+    values within 1e-12.  Outside every timed region."""
+    cfgs = sample["configs"]
+    rp, ci, va = sample["rows"]
+    so = np.concatenate([[0], np.cumsum(p.nsef())])
+    sef_rows = np.concatenate([np.arange(so[i], so[i + 1]) for i in cfgs]).astype(np.int64)
+    grp, gci, gva = ctx.get_rows(sef_rows)
+    same, worst = True, 0.0
+    for q, r in enumerate(sef_rows):
+        a, b = grp[q], grp[q + 1]
+        cols, vals = gci[a:b], gva[a:b]
+        low = cols <= r
+        oc, ov = ci[rp[q]:rp[q + 1]], va[rp[q]:rp[q + 1]]
+        if low.sum() != len(oc) or not np.array_equal(cols[low], oc):
+            same = False
+            continue
+        if len(oc):
+            worst = max(worst, float(np.abs(vals[low] - ov).max()))
+    return {"configs_checked": int(len(cfgs)), "rows_checked": int(len(sef_rows)), "elements_checked": int(len(ci)),
+            "structure_equal": bool(same), "max_abs_dH": worst, "ok": bool(same and worst <= 1e-12),
+            "what": "oracle lower-triangle rows of the CPU build sample vs the GPU CSR rows (entries with col <= row)"}
+
+
+def roots_vs_oracle(workload, nroots, seed, ksym, device):
+    """Every root and spin-orbit splitting (E_k - E_0) of a GPU solve against ARPACK (tol 1e-13)
+    on the oracle's matrix, plain FP64 and mixed precision.  Outside every timed region."""
+    import scipy.sparse.linalg as spla
+
+    import oracle
+    from psoci_gb300 import api
+    from psoci_gb300.inputs import named_workload
+
+    oracle.build(ref=False)
+    p = named_workload(workload, seed=seed, ksym=ksym)
+    O = oracle.Oracle(p)
+    rp, ci, va = O.build_lower(os.cpu_count() or 1)
+    F = oracle.lower_to_full_scipy(rp, ci, va, O.num_sefs())
+    ref = np.sort(spla.eigsh(F, k=nroots, which="SA", tol=1e-13, ncv=max(4 * nroots, 40))[0])
+    out = {"nsef": int(O.num_sefs()), "nroots": nroots, "seed": seed, "ksym": ksym, "oracle_evals": ref.tolist()}
+    with api.Context(device) as c:
+        c.load_problem(p)
+        c.build_determinants()
+        c.build_hamiltonian(mixed=True)
+        for name, mixed in (("fp64", False), ("mixed", True)):
+            r = c.davidson(nroots, rtol=1e-8, mixed=mixed, refine=True)
+            err = r.evals - ref
+            serr = (r.evals - r.evals[0]) - (ref - ref[0])
+            out[name] = {"evals": r.evals.tolist(), "err": err.tolist(), "max_abs_err": float(np.abs(err).max()),
+                         "splitting_err": serr[1:].tolist(), "max_abs_splitting_err": float(np.abs(serr).max())}
+    out["ok"] = bool(out["fp64"]["max_abs_err"] <= 1e-10 and out["mixed"]["max_abs_err"] <= 1e-7)
+    return out
+
+
+def cpu_estimate(p, rows_sample, sigma_sample, sigma_vectors, seed=0, keep=None):
     """Seconds the oracle (C restatement of the reference's build and sigma, all host threads)
     needs for the full solve, from bounded samples:
 
@@ -374,6 +437,9 @@ def cpu_estimate(p, rows_sample, sigma_sample, sigma_vectors, seed=0):
     t0 = time.perf_counter()
     nnz_rows = O.build_rows(rows, cores)
     t_rows = time.perf_counter() - t0
+    if keep is not None:
+        keep["configs"] = rows
+        keep["rows"] = O.sample_rows()
     del O
     scale = p.nconf / ns
     t_build = t_rows * scale
@@ -472,6 +538,7 @@ def main():
     ap.add_argument("--cpu-rows", type=int, default=8000, help="random row configurations in the CPU build sample")
     ap.add_argument("--cpu-density-rows", type=int, default=48, help="random rows in the CPU density sample")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-parity", action="store_true", help="skip the 8-root check of mrcis_6e8o_v40 vs the oracle")
     ap.add_argument("--verbose", type=int, default=0)
     args = ap.parse_args()
     if args.impl == "reference":

@@ -143,6 +143,13 @@ PSOCI_API psoci_status psoci_build_stats(const psoci_ctx *ctx, psoci_build_info 
 PSOCI_API psoci_status psoci_blocks(psoci_ctx *ctx, int npairs, const int32_t *A, const int32_t *B, double *out);
 /* Host copy of the CSR (rowptr[N+1], cols[nnz], vals[nnz]); NULLs allowed. */
 PSOCI_API psoci_status psoci_get_hamiltonian(const psoci_ctx *ctx, int64_t *rowptr, int32_t *cols, double *vals);
+/* Host copy of selected rows of the stored CSR (both triangles), replacing the row fetches of
+ * PsociGAhamiltonian::fetchLocalHblock (PsociGAhamiltonian.C:11791-11852): rows[nrows] SEF
+ * indices; rowptr[nrows+1] receives the offsets of each row's entries; cols / vals (both NULL
+ * to ask for the counts only) receive rowptr[nrows] entries, rows in the order given and each
+ * in ascending column order. */
+PSOCI_API psoci_status psoci_get_rows(const psoci_ctx *ctx, int nrows, const int64_t *rows, int64_t *rowptr,
+                                      int32_t *cols, double *vals);
 /* Replaces PsociGAhamiltonian::fetchDIAG_SEF / fetchDiags (PsociGAhamiltonian.C:9014). */
 PSOCI_API psoci_status psoci_get_diag(const psoci_ctx *ctx, double *diag);
 
@@ -155,16 +162,19 @@ PSOCI_API psoci_status psoci_sigma_device(psoci_ctx *ctx, int k, const double *d
                                 int ldy, psoci_prec prec);
 
 /* Mixed-precision sigma that allocates no device memory, for callers that cannot call
- * cudaMalloc while they run: work issued inside a CUDA stream capture, host programs whose
- * own allocator owns the whole GPU memory budget, loops that must not take an allocation's
- * implicit synchronisation.  Same arguments and result as psoci_sigma_device with
- * PSOCI_PREC_MIXED, but the FP32 copy of the input is staged in a fixed 16 MiB device array
- * compiled into the library (held by every device that loads it) instead of a buffer grown
- * with cudaMalloc.  Limit: N * 8 <= 4 Mi floats, i.e. at most 524,288 SEFs; larger problems
- * get PSOCI_ERR_UNSUPPORTED.  All calls on a device share the array (each call overwrites
- * what it reads first, so nothing must start at zero); calls that overlap on the GPU race
- * and must be serialised by the caller.  The first call on a device looks up the array's
- * address and caches it: make that first call before any stream capture begins.
+ * cudaMalloc while they run: host programs whose own allocator owns the whole GPU memory
+ * budget (as the reference's Global Arrays runtime takes a fixed memory size per rank up
+ * front), and loops that must not take the implicit device synchronisation an allocation
+ * can cause.  Same arguments and result as psoci_sigma_device with PSOCI_PREC_MIXED, but
+ * the FP32 copy of the input is staged in a fixed 16 MiB device array compiled into the
+ * library (held by every device that loads it until the process exits) instead of a buffer
+ * grown with cudaMalloc.  Limit: N * 8 <= 4 Mi floats, i.e. at most 524,288 SEFs; larger
+ * problems get PSOCI_ERR_UNSUPPORTED, a direct-mode build or one without the FP32 copy
+ * PSOCI_ERR_STATE.  All calls and all contexts on a device share the array, which keeps the
+ * last call's contents (each call overwrites what it reads first, so nothing must start at
+ * zero); calls that overlap on the GPU race and must be serialised by the caller.  The first
+ * call on a device looks up the array's address (cudaGetSymbolAddress) and caches it: make
+ * that first call before any stream capture begins.
  * No counterpart in the reference. */
 PSOCI_API psoci_status psoci_sigma_mixed_noalloc(psoci_ctx *ctx, int k, const double *dX, int ldx, double *dY,
                                                  int ldy);

@@ -20,6 +20,9 @@ import subprocess
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
+# The reference's source tree: read by the reference build (Makefile target ``ref``) and by the
+# tests that compare with it; absent on hosts without it.  One environment variable sets it.
+REFERENCE_TREE = os.environ.get("PSOCI_REFERENCE_TREE", "/root/reference/psociRestart-Cori")
 REF_DIR = os.path.join(HERE, "_ref")
 ORACLE_SO = os.path.join(REF_DIR, "liboracle.so")
 REF_SO = os.path.join(REF_DIR, "libpsoci_ref.so")
@@ -37,7 +40,12 @@ def _p(a, t):
 def build(ref: bool = True) -> None:
     """Compile the C restatement (always) and the reference harness (when present)."""
     targets = ["oracle"] + (["ref"] if ref else [])
-    subprocess.run(["make", "-s", "-f", os.path.join(HERE, "Makefile")] + targets, check=True, cwd=HERE)
+    subprocess.run(["make", "-s", "-f", os.path.join(HERE, "Makefile"), f"REFDIR={REFERENCE_TREE}"] + targets,
+                   check=True, cwd=HERE)
+
+
+def reference_tree_present() -> bool:
+    return os.path.isdir(REFERENCE_TREE)
 
 
 def ref_available() -> bool:
@@ -125,6 +133,19 @@ class Oracle(_Base):
         r = np.ascontiguousarray(rows, np.int32)
         f = self._fn("build_rows", ctypes.c_long, [ctypes.c_void_p, ctypes.c_int, _c_int_p, ctypes.c_int])
         return f(self.ctx, nthreads, _p(r, _c_int_p), len(r))
+
+    def sample_rows(self):
+        """CSR of the rows kept by the last build_rows: the sampled configurations' SEF rows
+        in order, each the reference's lower-triangle row (rowptr, cols, vals)."""
+        nr, nz = ctypes.c_long(), ctypes.c_long()
+        self._fn("sample_counts", None, [ctypes.c_void_p, _c_long_p, _c_long_p])(self.ctx, ctypes.byref(nr),
+                                                                                   ctypes.byref(nz))
+        rp = np.zeros(nr.value + 1, np.int64)
+        ci = np.zeros(max(nz.value, 1), np.int32)
+        va = np.zeros(max(nz.value, 1), np.float64)
+        self._fn("copy_sample", None, [ctypes.c_void_p, _c_long_p, _c_int_p, _c_dbl_p])(
+            self.ctx, _p(rp, _c_long_p), _p(ci, _c_int_p), _p(va, _c_dbl_p))
+        return rp, ci[:nz.value], va[:nz.value]
 
     def ciden_block(self, i, j):
         ns = self.p.nsef()

@@ -56,6 +56,12 @@ struct orc_ctx {
   long *rowptr;
   int *cols;
   double *vals;
+  /* rows of the last orc_build_rows sample: the SEF rows of the sampled configurations in
+   * the order given, each the reference's lower-triangle row */
+  long s_nrows, s_nnz;
+  long *s_rowptr;
+  int *s_cols;
+  double *s_vals;
 };
 
 static inline long tri(long i, long j) { /* 0-based (max,min) -> packed position */
@@ -217,6 +223,7 @@ void orc_destroy(orc_ctx *c) {
   if (!c) return;
   free(c->one); free(c->eri); free(c->occ); free(c->cfg); free(c->dets); free(c->sefoff);
   free(c->rowptr); free(c->cols); free(c->vals);
+  free(c->s_rowptr); free(c->s_cols); free(c->s_vals);
   free(c);
 }
 
@@ -631,10 +638,39 @@ long orc_build_rows(orc_ctx *c, int nthreads, const int *rows, int nrows) {
     pthread_create(&th[t], NULL, build_worker, &args[t]);
   }
   for (int t = 0; t < nthreads; ++t) pthread_join(th[t], NULL);
-  long nnz = 0;
+  long nnz = 0, nr = 0;
+  for (int q = 0; q < nrows; ++q) nr += c->sefoff[rows[q] + 1] - c->sefoff[rows[q]];
+  free(c->s_rowptr); free(c->s_cols); free(c->s_vals);
+  c->s_rowptr = (long *)malloc(sizeof(long) * (nr + 1));
+  c->s_rowptr[0] = 0;
+  c->s_nrows = nr;
+  nr = 0;
+  for (int q = 0; q < nrows; ++q)
+    for (long r = c->sefoff[rows[q]]; r < c->sefoff[rows[q] + 1]; ++r, ++nr) c->s_rowptr[nr + 1] = c->s_rowptr[nr] + rb[r].n;
+  c->s_nnz = c->s_rowptr[nr];
+  c->s_cols = (int *)malloc(sizeof(int) * (c->s_nnz ? c->s_nnz : 1));
+  c->s_vals = (double *)malloc(sizeof(double) * (c->s_nnz ? c->s_nnz : 1));
+  nr = 0;
+  for (int q = 0; q < nrows; ++q)
+    for (long r = c->sefoff[rows[q]]; r < c->sefoff[rows[q] + 1]; ++r, ++nr) {
+      memcpy(c->s_cols + c->s_rowptr[nr], rb[r].col, sizeof(int) * rb[r].n);
+      memcpy(c->s_vals + c->s_rowptr[nr], rb[r].val, sizeof(double) * rb[r].n);
+    }
   for (long r = 0; r < N; ++r) { nnz += rb[r].n; free(rb[r].col); free(rb[r].val); }
   free(rb); free(th); free(args); free(e1); free(e2);
   return nnz;
+}
+
+/* The rows kept by the last orc_build_rows: counts, then the CSR (rowptr[nrows+1], cols,
+ * vals), rows in the order of the sampled configurations and their SEFs. */
+void orc_sample_counts(const orc_ctx *c, long *nrows, long *nnz) {
+  *nrows = c->s_nrows;
+  *nnz = c->s_nnz;
+}
+void orc_copy_sample(const orc_ctx *c, long *rowptr, int *cols, double *vals) {
+  memcpy(rowptr, c->s_rowptr, sizeof(long) * (c->s_nrows + 1));
+  memcpy(cols, c->s_cols, sizeof(int) * c->s_nnz);
+  memcpy(vals, c->s_vals, sizeof(double) * c->s_nnz);
 }
 
 /* diagonal H_rr (the reference keeps it last in each row, g_diag_sef) */

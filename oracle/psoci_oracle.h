@@ -26,6 +26,9 @@ int orc_block(const orc_ctx *c, int i, int j, double *out);
 long orc_build_lower(orc_ctx *c, int nthreads);
 void orc_copy_lower(const orc_ctx *c, long *rowptr, int *cols, double *vals);
 long orc_build_rows(orc_ctx *c, int nthreads, const int *rows, int nrows);
+/* the rows of the last orc_build_rows (the sampled configurations' SEF rows, in order) */
+void orc_sample_counts(const orc_ctx *c, long *nrows, long *nnz);
+void orc_copy_sample(const orc_ctx *c, long *rowptr, int *cols, double *vals);
 void orc_diag(const orc_ctx *c, double *diag);
 void orc_sigma_lower(long n, const long *rowptr, const int *cols, const double *vals, int k,
                      const double *x, double *y, int nthreads);

@@ -80,6 +80,7 @@ SIGNATURES = {
     "psoci_blocks": (ctypes.c_int, [_P, ctypes.c_int, _I32P, _I32P, _DP]),
     "psoci_get_hamiltonian": (ctypes.c_int, [_P, _I64P, _I32P, _DP]),
     "psoci_get_diag": (ctypes.c_int, [_P, _DP]),
+    "psoci_get_rows": (ctypes.c_int, [_P, ctypes.c_int, _I64P, _I64P, _I32P, _DP]),
     "psoci_sigma": (ctypes.c_int, [_P, ctypes.c_int, _DP, _DP, ctypes.c_int]),
     "psoci_sigma_device": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
                                           ctypes.c_int, ctypes.c_int]),
@@ -251,6 +252,17 @@ class Context:
         self._check(self.lib.psoci_get_hamiltonian(self.ctx, _ptr(rp, _I64P), _ptr(ci, _I32P), _ptr(va, _DP)),
                     "get_hamiltonian")
         return rp, ci[:self.nnz], va[:self.nnz]
+
+    def get_rows(self, rows):
+        """Selected rows of the stored CSR (both triangles): (rowptr [len(rows)+1], cols, vals)."""
+        r = np.ascontiguousarray(rows, np.int64)
+        rp = np.zeros(len(r) + 1, np.int64)
+        self._check(self.lib.psoci_get_rows(self.ctx, len(r), _ptr(r, _I64P), _ptr(rp, _I64P), None, None), "get_rows")
+        ci = np.zeros(max(int(rp[-1]), 1), np.int32)
+        va = np.zeros(max(int(rp[-1]), 1), np.float64)
+        self._check(self.lib.psoci_get_rows(self.ctx, len(r), _ptr(r, _I64P), _ptr(rp, _I64P), _ptr(ci, _I32P),
+                                            _ptr(va, _DP)), "get_rows")
+        return rp, ci[:rp[-1]], va[:rp[-1]]
 
     def get_diag(self):
         d = np.zeros(self.nsef)

@@ -28,6 +28,24 @@ void release_all(psoci_ctx *c) {
   psoci_free(c->d_y);
   psoci_free(c->d_x32);
 }
+// psoci_get_rows: lengths of the requested rows, then their columns and values, one warp
+// per row
+__global__ void k_row_lengths(int n, const int64_t *__restrict__ rows, const int64_t *__restrict__ rowptr,
+                              int64_t *__restrict__ len) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q < n) len[q] = rowptr[rows[q] + 1] - rowptr[rows[q]];
+}
+__global__ void k_row_gather(int n, const int64_t *__restrict__ rows, const int64_t *__restrict__ rowptr,
+                             const int64_t *__restrict__ outoff, const int32_t *__restrict__ col,
+                             const double *__restrict__ val, int32_t *__restrict__ ocol, double *__restrict__ oval) {
+  const int q = (int)((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+  if (q >= n) return;
+  const int64_t a = rowptr[rows[q]], m = rowptr[rows[q] + 1] - a, o = outoff[q];
+  for (int64_t e = lane; e < m; e += 32) {
+    ocol[o + e] = col[a + e];
+    oval[o + e] = val[a + e];
+  }
+}
 }  // namespace
 
 extern "C" {
@@ -75,6 +93,7 @@ psoci_status psoci_create(psoci_ctx **out, const psoci_opts *opts) {
   size_t free_b = 0, total_b = 0;
   if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess) c->pool_cap = total_b / 2;
   cudaGetLastError();
+  psoci_pool_register(c);
   *out = c;
   return PSOCI_OK;
 }
@@ -267,6 +286,58 @@ psoci_status psoci_get_hamiltonian(const psoci_ctx *cc, int64_t *rowptr, int32_t
   if (cols) PSOCI_CUDA(c, cudaMemcpy(cols, c->d_col, sizeof(int32_t) * c->nnz, cudaMemcpyDeviceToHost));
   if (vals) PSOCI_CUDA(c, cudaMemcpy(vals, c->d_val, sizeof(double) * c->nnz, cudaMemcpyDeviceToHost));
   return PSOCI_OK;
+}
+
+psoci_status psoci_get_rows(const psoci_ctx *cc, int nrows, const int64_t *rows, int64_t *rowptr, int32_t *cols,
+                            double *vals) {
+  psoci_ctx *c = const_cast<psoci_ctx *>(cc);
+  if (!c) return PSOCI_ERR_INVALID_ARG;
+  if (nrows < 0 || (nrows > 0 && (!rows || !rowptr)) || (!cols) != (!vals))
+    return psoci_fail(c, PSOCI_ERR_INVALID_ARG, "get_rows: bad arguments");
+  if (!c->have_h) return psoci_fail(c, PSOCI_ERR_STATE, "get_rows: not built");
+  if (c->direct) return psoci_fail(c, PSOCI_ERR_STATE, "get_rows: direct mode stores no matrix");
+  for (int q = 0; q < nrows; ++q)
+    if (rows[q] < 0 || rows[q] >= c->nsef_total) return psoci_fail(c, PSOCI_ERR_INVALID_ARG, "get_rows: row out of range");
+  if (rowptr) rowptr[0] = 0;
+  if (nrows == 0) return PSOCI_OK;
+  psoci_status s;
+  if ((s = set_device(c))) return s;
+  cudaStream_t st = c->stream;
+  int64_t *d_rows = nullptr, *d_len = nullptr, *d_off = nullptr;
+  int32_t *d_col = nullptr;
+  double *d_val = nullptr;
+  auto done = [&](psoci_status r) {
+    psoci_free(d_rows); psoci_free(d_len); psoci_free(d_off); psoci_free(d_col); psoci_free(d_val);
+    return r;
+  };
+  if ((s = psoci_alloc(c, &d_rows, nrows)) || (s = psoci_alloc(c, &d_len, nrows)) || (s = psoci_alloc(c, &d_off, nrows + 1)))
+    return done(s);
+  std::vector<int64_t> len(nrows);
+  cudaError_t e = cudaMemcpyAsync(d_rows, rows, sizeof(int64_t) * nrows, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) {
+    psoci_note_launch();
+    k_row_lengths<<<(nrows + 255) / 256, 256, 0, st>>>(nrows, d_rows, c->d_rowptr, d_len);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpyAsync(len.data(), d_len, sizeof(int64_t) * nrows, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return done(psoci_cuda_fail(c, e, "get_rows"));
+  for (int q = 0; q < nrows; ++q) rowptr[q + 1] = rowptr[q] + len[q];
+  const int64_t tot = rowptr[nrows];
+  if (!cols || tot == 0) return done(PSOCI_OK);
+  if ((s = psoci_alloc(c, &d_col, tot)) || (s = psoci_alloc(c, &d_val, tot))) return done(s);
+  e = cudaMemcpyAsync(d_off, rowptr, sizeof(int64_t) * (nrows + 1), cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) {
+    psoci_note_launch();
+    k_row_gather<<<(unsigned)(((int64_t)nrows * 32 + 255) / 256), 256, 0, st>>>(nrows, d_rows, c->d_rowptr, d_off,
+                                                                                 c->d_col, c->d_val, d_col, d_val);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpyAsync(cols, d_col, sizeof(int32_t) * tot, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(vals, d_val, sizeof(double) * tot, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return done(psoci_cuda_fail(c, e, "get_rows"));
+  return done(PSOCI_OK);
 }
 
 psoci_status psoci_get_diag(const psoci_ctx *cc, double *diag) {

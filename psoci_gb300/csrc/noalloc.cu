@@ -1,7 +1,6 @@
 // Mixed-precision sigma that allocates no device memory.
 //
 // Who needs it: callers that must not call cudaMalloc while they run —
-//   * code that issues work inside a CUDA stream capture (a cudaMalloc there is an error),
 //   * host programs that hand the whole GPU memory budget to their own allocator up front
 //     and forbid other allocations (as the reference's Global Arrays runtime does with its
 //     fixed per-rank memory), and
@@ -18,8 +17,9 @@
 //   * every device that loads this library keeps the 16 MiB array until the process exits;
 //   * all calls on a device share the array and it keeps the last call's contents; each call
 //     overwrites every entry it reads before reading it, so nothing has to start at zero;
-//   * calls that overlap on the GPU (other streams, other contexts on the same device) race
-//     on the array and must be serialised by the caller;
+//   * all contexts on a device share the one array; calls that overlap on the GPU (other
+//     streams, other contexts on the same device) race on it and must be serialised by the
+//     caller;
 //   * the first call on a device looks up the array's device address (cudaGetSymbolAddress)
 //     and caches it; make that first call before any stream capture begins.
 #include <mutex>

@@ -153,8 +153,10 @@ psoci_status psoci_cuda_fail(psoci_ctx *c, cudaError_t e, const char *where);
 // a later allocation of the same context of at most 25% smaller size, so a repeated build
 // or solve reuses its buffers instead of paying cudaFree (which waits for the device) and
 // cudaMalloc (page mapping) for tens of GB each time.  Reuse waits for the context's stream
-// first, as cudaFree would have.  The cache holds at most half the device memory, is
-// emptied when cudaMalloc fails (and the allocation retried) and on psoci_destroy.
+// first, as cudaFree would have.  The caches of all contexts on one device hold at most
+// half its memory together; all of them are emptied when a cudaMalloc on that device fails
+// (and the allocation is retried), and a context's own on psoci_destroy.
+void psoci_pool_register(psoci_ctx *c);
 void *psoci_device_alloc(psoci_ctx *c, size_t bytes, cudaError_t *err);
 void psoci_device_free(void *p);
 void psoci_pool_flush(psoci_ctx *c);

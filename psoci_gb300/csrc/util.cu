@@ -3,6 +3,8 @@
 #include <cstdio>
 #include <mutex>
 #include <unordered_map>
+#include <vector>
+#include <algorithm>
 
 #include "psoci_internal.cuh"
 
@@ -16,12 +18,34 @@ psoci_status psoci_fail(psoci_ctx *c, psoci_status s, const std::string &msg) {
   return s;
 }
 
-// The device-memory cache of psoci_alloc.  Owner and size of every live block, process-wide
-// (a block may be released while another context's call is running).
+// The device-memory cache of psoci_alloc.  One lock guards the owner and size of every
+// live block, every context's pool of released blocks and the bytes the pools of each
+// device hold: a block may be released on one thread while another context's call runs on
+// another, and a failed cudaMalloc empties the pools of every context on its device.
 namespace {
-std::mutex g_blocks_mu;
+std::mutex g_mu;
 std::unordered_map<void *, std::pair<psoci_ctx *, size_t>> g_blocks;
+std::unordered_map<int, size_t> g_pooled;                 // bytes in the pools, per device
+std::unordered_map<int, std::vector<psoci_ctx *>> g_ctxs; // live contexts, per device
+
+// every context's released blocks on one device go back to the driver (g_mu held);
+// cudaFree waits for the device, so no stream still uses them afterwards
+void flush_device_locked(int dev) {
+  auto it = g_ctxs.find(dev);
+  if (it != g_ctxs.end())
+    for (psoci_ctx *c : it->second) {
+      for (auto &kv : c->pool) cudaFree(kv.second);
+      c->pool.clear();
+      c->pool_bytes = 0;
+    }
+  g_pooled[dev] = 0;
+}
 }  // namespace
+
+void psoci_pool_register(psoci_ctx *c) {
+  std::lock_guard<std::mutex> g(g_mu);
+  g_ctxs[c->device].push_back(c);
+}
 
 void *psoci_device_alloc(psoci_ctx *c, size_t bytes, cudaError_t *err) {
   if (bytes == 0) bytes = 1;
@@ -30,36 +54,52 @@ void *psoci_device_alloc(psoci_ctx *c, size_t bytes, cudaError_t *err) {
     *err = cudaMalloc(&p, bytes);
     return (*err == cudaSuccess) ? p : nullptr;
   }
-  auto it = c->pool.lower_bound(bytes);
-  if (it != c->pool.end() && it->first - bytes <= bytes / 4) {
-    const size_t sz = it->first;
-    p = it->second;
-    c->pool.erase(it);
-    c->pool_bytes -= sz;
+  bool reused = false;
+  {
+    std::lock_guard<std::mutex> g(g_mu);
+    auto it = c->pool.lower_bound(bytes);
+    if (it != c->pool.end() && it->first - bytes <= bytes / 4) {
+      const size_t sz = it->first;
+      p = it->second;
+      c->pool.erase(it);
+      c->pool_bytes -= sz;
+      g_pooled[c->device] -= sz;
+      g_blocks[p] = {c, sz};
+      reused = true;
+    }
+  }
+  if (reused) {
     // work of this context that used the block before its release ends first (cudaFree
     // would have waited for it)
     const cudaError_t e = cudaStreamSynchronize(c->stream);
     if (e != cudaSuccess) {
+      {
+        std::lock_guard<std::mutex> g(g_mu);
+        g_blocks.erase(p);
+      }
       cudaFree(p);
       *err = e;
       return nullptr;
     }
-    std::lock_guard<std::mutex> g(g_blocks_mu);
-    g_blocks[p] = {c, sz};
     *err = cudaSuccess;
     return p;
   }
   cudaError_t e = cudaMalloc(&p, bytes);
-  if (e == cudaErrorMemoryAllocation && !c->pool.empty()) {
+  if (e == cudaErrorMemoryAllocation) {
     cudaGetLastError();
-    psoci_pool_flush(c);
-    e = cudaMalloc(&p, bytes);
+    bool had = false;
+    {
+      std::lock_guard<std::mutex> g(g_mu);
+      had = g_pooled[c->device] > 0;
+      if (had) flush_device_locked(c->device);
+    }
+    if (had) e = cudaMalloc(&p, bytes);
   }
   if (e != cudaSuccess) {
     *err = e;
     return nullptr;
   }
-  std::lock_guard<std::mutex> g(g_blocks_mu);
+  std::lock_guard<std::mutex> g(g_mu);
   g_blocks[p] = {c, bytes};
   *err = cudaSuccess;
   return p;
@@ -67,34 +107,37 @@ void *psoci_device_alloc(psoci_ctx *c, size_t bytes, cudaError_t *err) {
 
 void psoci_device_free(void *p) {
   if (!p) return;
-  psoci_ctx *c = nullptr;
-  size_t sz = 0;
   {
-    std::lock_guard<std::mutex> g(g_blocks_mu);
+    std::lock_guard<std::mutex> g(g_mu);
     auto it = g_blocks.find(p);
     if (it != g_blocks.end()) {
-      c = it->second.first;
-      sz = it->second.second;
+      psoci_ctx *c = it->second.first;
+      const size_t sz = it->second.second;
       g_blocks.erase(it);
+      // the cap holds for all contexts of the device together
+      if (c && g_pooled[c->device] + sz <= c->pool_cap) {
+        c->pool.insert({sz, p});
+        c->pool_bytes += sz;
+        g_pooled[c->device] += sz;
+        return;
+      }
     }
-  }
-  if (c && c->pool_bytes + sz <= c->pool_cap) {
-    c->pool.insert({sz, p});
-    c->pool_bytes += sz;
-    return;
   }
   cudaFree(p);
 }
 
 void psoci_pool_flush(psoci_ctx *c) {
+  std::lock_guard<std::mutex> g(g_mu);
   for (auto &kv : c->pool) cudaFree(kv.second);
   c->pool.clear();
+  g_pooled[c->device] -= c->pool_bytes;
   c->pool_bytes = 0;
 }
 
-// blocks of a context that is going away and were never released
+// blocks of a context that is going away and were never released; the context leaves the
+// device's list
 void psoci_pool_forget(psoci_ctx *c) {
-  std::lock_guard<std::mutex> g(g_blocks_mu);
+  std::lock_guard<std::mutex> g(g_mu);
   for (auto it = g_blocks.begin(); it != g_blocks.end();) {
     if (it->second.first == c) {
       cudaFree(it->first);
@@ -103,6 +146,8 @@ void psoci_pool_forget(psoci_ctx *c) {
       ++it;
     }
   }
+  auto &v = g_ctxs[c->device];
+  v.erase(std::remove(v.begin(), v.end(), c), v.end());
 }
 
 psoci_status psoci_cuda_fail(psoci_ctx *c, cudaError_t e, const char *where) {

@@ -64,3 +64,31 @@ SMALL_CASES = [
 
 def small_problem(name, ksym, seed=3):
     return named_workload(name, seed=seed, ksym=ksym)
+
+
+def gpu_context(p):
+    """A GPU context with the problem loaded and its determinants built."""
+    from psoci_gb300 import api
+
+    c = api.Context(0)
+    c.load_problem(p)
+    c.build_determinants()
+    return c
+
+
+def check_h_against_oracle(c, O, p, tol=1e-12, mixed=True, nthreads=0):
+    """Build H on the GPU and compare it with the oracle's lower triangle mirrored: equal
+    row pointers and columns, values and diagonal within tol.  Returns the full oracle CSR."""
+    rp, ci, va = O.build_lower(nthreads)
+    n = O.num_sefs()
+    F = lower_to_full(rp, ci, va, n)
+    c.build_hamiltonian(mixed=mixed)
+    grp, gci, gva = c.get_hamiltonian()
+    assert c.nnz == F.nnz
+    assert (grp == F.indptr).all()
+    assert (gci == F.indices).all()
+    diff = np.abs(gva - F.data).max() if F.nnz else 0.0
+    assert diff <= tol, diff
+    d = c.get_diag()
+    assert np.abs(d - O.diag()).max() <= tol
+    return F

@@ -10,7 +10,8 @@ import numpy as np
 import pytest
 import scipy.linalg as sla
 
-from helpers import SMALL_CASES, det_lists_to_bits, gpu_bits, high_open_problem, lower_to_full, small_problem
+from helpers import (SMALL_CASES, check_h_against_oracle, det_lists_to_bits, gpu_bits, gpu_context, high_open_problem,
+                     lower_to_full, small_problem)
 
 pytestmark = pytest.mark.gpu
 
@@ -22,12 +23,7 @@ EIG_TOL_MIXED = 1e-7
 
 
 def _ctx(p):
-    from psoci_gb300 import api
-
-    c = api.Context(0)
-    c.load_problem(p)
-    c.build_determinants()
-    return c
+    return gpu_context(p)
 
 
 def _check_dets(c, O, p):
@@ -46,19 +42,7 @@ def _check_dets(c, O, p):
 
 
 def _check_h(c, O, p):
-    rp, ci, va = O.build_lower(4)
-    n = O.num_sefs()
-    F = lower_to_full(rp, ci, va, n)
-    c.build_hamiltonian(mixed=True)
-    grp, gci, gva = c.get_hamiltonian()
-    assert c.nnz == F.nnz
-    assert (grp == F.indptr).all()
-    assert (gci == F.indices).all()
-    diff = np.abs(gva - F.data).max() if F.nnz else 0.0
-    assert diff <= H_TOL, diff
-    d = c.get_diag()
-    assert np.abs(d - O.diag()).max() <= H_TOL
-    return F
+    return check_h_against_oracle(c, O, p, tol=H_TOL, nthreads=4)
 
 
 @pytest.mark.parametrize("name,ksym", SMALL_CASES)

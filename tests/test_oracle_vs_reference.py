@@ -10,7 +10,7 @@ import pytest
 
 from helpers import SMALL_CASES, high_open_problem, small_problem
 
-REF_TREE = "/root/reference/psociRestart-Cori"
+from oracle import REFERENCE_TREE as REF_TREE  # noqa: E402
 pytestmark = pytest.mark.skipif(not os.path.isdir(REF_TREE), reason="reference tree not present")
 
 

@@ -12,7 +12,7 @@ import pytest
 
 from psoci_gb300 import api
 
-REF_TREE = "/root/reference/psociRestart-Cori"
+from oracle import REFERENCE_TREE as REF_TREE  # noqa: E402
 
 
 def vecs(nroots=3, n=257, seed=0):
