@@ -252,10 +252,88 @@ class PsociConstructHamiltonian {
   Device &dev_;
 };
 
-// PsociGAsubspace + PsociGAbasis (PsociGAsubspace.hpp, PsociGAbasis.hpp): the Davidson loop.
+// PsociGAbasis (PsociGAbasis.hpp): the Davidson vectors V and their products H*V, on the
+// device.  The step-level methods keep the reference's names so that its driver loop
+// (driver.PSOCI.splittest.C:1186-1311) carries over; the basis stays orthonormal.
+class PsociGAbasis {
+ public:
+  // PsociGAbasis(numSoughtRoots, hamilton, g_v, g_Hv): room for maxVectors vectors
+  PsociGAbasis(Device &d, int numSoughtRoots, int maxVectors) : dev_(d) {
+    check(dev_.get(), psoci_basis_create(dev_.get(), numSoughtRoots, maxVectors), "psoci_basis_create");
+  }
+  ~PsociGAbasis() { psoci_basis_destroy(dev_.get()); }
+  PsociGAbasis(const PsociGAbasis &) = delete;
+  PsociGAbasis &operator=(const PsociGAbasis &) = delete;
+  // PsociGAvectors::specifyDiagonalGuessVectors (PsociGAvectors.C:687-726); mode 0 the
+  // reference's unit vectors on the first SEFs, 1 the lowest diagonal elements, 2 restart
+  // vectors given to PsociGAsubspace::setGuess
+  void specifyDiagonalGuessVectors(int mode = 0) {
+    check(dev_.get(), psoci_basis_guess(dev_.get(), mode), "psoci_basis_guess");
+  }
+  // precision of the H*v products (the reference's are FP64)
+  void setProducts(psoci_prec prec) { prec_ = prec; }
+  // normAllVectors + orthonormalizeAllVectors (PsociGAbasis.C:1044, :1210): 0, or the 1-based
+  // column found linearly dependent
+  void normAllVectors() {}
+  int orthonormalizeAllVectors() {
+    int dep = 0;
+    psoci_status s = psoci_basis_orthonormalize_all(dev_.get(), &dep);
+    if (s == PSOCI_ERR_NUMERIC) return dep;
+    check(dev_.get(), s, "psoci_basis_orthonormalize_all");
+    return 0;
+  }
+  // computeHvProducts(start, num) (PsociGAbasis.C:1610)
+  int computeHvProducts(int start, int num) {
+    check(dev_.get(), psoci_basis_compute_hv(dev_.get(), start, num, prec_), "psoci_basis_compute_hv");
+    return num;
+  }
+  void setpresent_matrixProducts(int) {}  // the device basis counts its products itself
+  // preconditionAndNewVectorIncore(curroot, shift, g_rnorms, g_diag) (PsociGAbasis.C:1807-1919)
+  int preconditionAndNewVectorIncore(int curroot, double shift, double precondMin = 1e-3) {
+    check(dev_.get(), psoci_basis_precondition_new(dev_.get(), curroot, shift, precondMin),
+          "psoci_basis_precondition_new");
+    return 1;
+  }
+  // appendScratchVector (PsociGAbasis.C:362): orthonormalise, append, form its H*v
+  int appendScratchVector() {
+    int n = 0;
+    check(dev_.get(), psoci_basis_append_scratch(dev_.get(), prec_, &n), "psoci_basis_append_scratch");
+    return n;
+  }
+  // expandAndReplaceVectorsNew(g_evecs, num) (PsociGAbasis.C:483-583)
+  int expandAndReplaceVectorsNew(int num) {
+    check(dev_.get(), psoci_basis_expand_replace(dev_.get(), num), "psoci_basis_expand_replace");
+    return num;
+  }
+  int CurrentExistingRoots() const { return info(0); }
+  int CurrentNumSoughtRoots() const { return info(1); }
+  int CurrentMaxRoots() const { return info(2); }
+  int CurrentExistingHVProducts() const { return info(3); }
+  // the first k vectors, root-major (after the last expandAndReplaceVectorsNew: the solution)
+  std::vector<double> fetchVectors(int k, int64_t nsef) const {
+    std::vector<double> v((size_t)k * nsef);
+    check(dev_.get(), psoci_basis_vectors(dev_.get(), k, v.data()), "psoci_basis_vectors");
+    return v;
+  }
+  Device &device() const { return dev_; }
+
+ private:
+  int info(int which) const {
+    int e = 0, so = 0, mx = 0, pr = 0;
+    check(dev_.get(), psoci_basis_info(dev_.get(), &e, &so, &mx, &pr), "psoci_basis_info");
+    return which == 0 ? e : which == 1 ? so : which == 2 ? mx : pr;
+  }
+  Device &dev_;
+  psoci_prec prec_ = PSOCI_PREC_FP64;
+};
+
+// PsociGAsubspace (PsociGAsubspace.hpp): the projected problem of a PsociGAbasis, and the
+// whole Davidson solve in one call (solve(), the fast path: all unconverged roots per
+// iteration, mixed precision with refinement).
 class PsociGAsubspace {
  public:
   explicit PsociGAsubspace(Device &d) : dev_(d) {}
+  PsociGAsubspace(Device &d, PsociGAbasis &basis) : dev_(d), basis_(&basis) { (void)basis_; }
   struct Result {
     std::vector<double> evals, rnorms, evecs;  // evecs root-major (root r at r*N)
     psoci_dav_stats stats{};
@@ -274,9 +352,41 @@ class PsociGAsubspace {
   void setGuess(int k, const std::vector<double> &vecs) {
     check(dev_.get(), psoci_set_guess(dev_.get(), k, vecs.data()), "psoci_set_guess");
   }
+  // generateIncrementalSubspace(num) (PsociGAsubspace.C:273-366)
+  void generateIncrementalSubspace(int num) {
+    check(dev_.get(), psoci_subspace_generate_incremental(dev_.get(), num), "psoci_subspace_generate_incremental");
+  }
+  // diagSubspaceGOP (PsociGAsubspace.C:1088-1171); the eigenvalues stay for brdcstEvals
+  void diagSubspaceGOP() {
+    int e = 0;
+    check(dev_.get(), psoci_basis_info(dev_.get(), &e, nullptr, nullptr, nullptr), "psoci_basis_info");
+    evals_.assign(std::max(e, 1), 0.0);
+    check(dev_.get(), psoci_subspace_diag(dev_.get(), evals_.data()), "psoci_subspace_diag");
+  }
+  // brdcstEvals(evals): the eigenvalues of the last diagSubspaceGOP (the front of evals)
+  void brdcstEvals(std::vector<double> &evals) const {
+    if (evals.size() < evals_.size()) evals.resize(evals_.size());
+    std::copy(evals_.begin(), evals_.end(), evals.begin());
+  }
+  // computeRnormSingle(iroot, evals, rnorm) (PsociGAsubspace.C:874-1000), iroot 1-based
+  int computeRnormSingle(int iroot, const std::vector<double> &, double &rnormvec) {
+    check(dev_.get(), psoci_subspace_rnorm_single(dev_.get(), iroot, &rnormvec), "psoci_subspace_rnorm_single");
+    return 0;
+  }
+  // computeRnorms(evals, rnorms) (PsociGAsubspace.C:775-872)
+  int computeRnorms(const std::vector<double> &, std::vector<double> &rnorms) {
+    int so = 0;
+    check(dev_.get(), psoci_basis_info(dev_.get(), nullptr, &so, nullptr, nullptr), "psoci_basis_info");
+    rnorms.resize(so);
+    check(dev_.get(), psoci_subspace_rnorms(dev_.get(), rnorms.data()), "psoci_subspace_rnorms");
+    return 0;
+  }
+  void destroySubspace() {}
 
  private:
   Device &dev_;
+  PsociGAbasis *basis_ = nullptr;
+  std::vector<double> evals_;
 };
 
 // PsociNOpopulations (PsociNOpopulations.hpp): natural orbitals of the CI densities in the MO

@@ -211,6 +211,67 @@ typedef struct {
 PSOCI_API psoci_status psoci_davidson(psoci_ctx *ctx, const psoci_dav_opts *opts, double *evals,
                             double *evecs, double *rnorms, psoci_dav_stats *stats);
 
+/* Step-level Davidson: the basis and subspace of the reference's own loop
+ * (driver.PSOCI.splittest.C:1186-1311), held on the device between calls so that a host
+ * program keeps that loop as it is.  One basis per context: V and H*V (N x max_vectors), the
+ * projected matrix G = V^T H V, its eigenpairs and the residuals of the sought roots.  The
+ * vectors are kept orthonormal, so the overlap S of the reference is the identity and its
+ * generalised eigen-solve (dsygv) a symmetric one.  psoci_davidson stays the fast path.
+ * Calls that change the basis invalidate what depends on it (a new vector needs its G
+ * columns, a new G its eigen-solve, a new eigen-solve its residuals); calls made out of that
+ * order answer PSOCI_ERR_STATE.  Rebuilding the Hamiltonian of another space invalidates the
+ * basis. */
+/* PsociGAbasis(numSoughtRoots, hamilton, g_v, g_Hv) and PsociGAsubspace(basis, diag, g_rnorms)
+ * constructors (PsociGAbasis.C, PsociGAsubspace.C): room for max_vectors (nroots+1 .. 96)
+ * vectors of the built Hamiltonian's dimension; replaces an earlier basis. */
+PSOCI_API psoci_status psoci_basis_create(psoci_ctx *ctx, int nroots, int max_vectors);
+/* PsociGAsubspace::destroySubspace (PsociGAsubspace.C:194) with the basis's arrays. */
+PSOCI_API void psoci_basis_destroy(psoci_ctx *ctx);
+/* PsociGAvectors::specifyDiagonalGuessVectors (PsociGAvectors.C:687-726): nroots unit vectors;
+ * mode 0 on the first nroots SEFs (the reference), 1 on the nroots lowest diagonal elements,
+ * 2 the vectors of psoci_set_guess (the -r restart) completed as in mode 1.  No products yet. */
+PSOCI_API psoci_status psoci_basis_guess(psoci_ctx *ctx, int mode);
+/* PsociGAbasis::normAllVectors + orthonormalizeAllVectors (PsociGAbasis.C:1044, :1210) of the
+ * guess set (at most nroots vectors); a linear dependency gives PSOCI_ERR_NUMERIC with the
+ * 1-based column in *dependent_at (may be NULL). */
+PSOCI_API psoci_status psoci_basis_orthonormalize_all(psoci_ctx *ctx, int *dependent_at);
+/* PsociGAbasis::computeHvProducts(start, num) (PsociGAbasis.C:1610): H*v of vectors
+ * start..start+num-1 with the sigma of the given precision. */
+PSOCI_API psoci_status psoci_basis_compute_hv(psoci_ctx *ctx, int start, int num, psoci_prec prec);
+/* PsociGAsubspace::generateIncrementalSubspace(num) (PsociGAsubspace.C:273-366): the columns of
+ * G = V^T (H V) for the last num vectors (FP64 sums, float-float on the FP32 pipe). */
+PSOCI_API psoci_status psoci_subspace_generate_incremental(psoci_ctx *ctx, int num);
+/* PsociGAsubspace::diagSubspaceGOP + brdcstEvals (PsociGAsubspace.C:1088-1171): eigenpairs of
+ * G (host, as the reference's dsygv); evals receives the existing-count eigenvalues ascending. */
+PSOCI_API psoci_status psoci_subspace_diag(psoci_ctx *ctx, double *evals);
+/* PsociGAsubspace::computeRnormSingle (PsociGAsubspace.C:874-1000): the residual norm of Ritz
+ * vector iroot (1-based, <= nroots); the residual is kept for psoci_basis_precondition_new. */
+PSOCI_API psoci_status psoci_subspace_rnorm_single(psoci_ctx *ctx, int iroot, double *rnorm);
+/* PsociGAsubspace::computeRnorms (PsociGAsubspace.C:775-872): the residual norms of all sought
+ * roots (rnorms[nroots]); the residuals are kept. */
+PSOCI_API psoci_status psoci_subspace_rnorms(psoci_ctx *ctx, double *rnorms);
+/* PsociGAbasis::preconditionAndNewVectorIncore (PsociGAbasis.C:1807-1919): the scratch vector
+ * t_i = r_i / (D_i - shift) where |D_i - shift| > precond_min (reference 1e-3), else r_i, from
+ * the kept residual of root curroot (1-based). */
+PSOCI_API psoci_status psoci_basis_precondition_new(psoci_ctx *ctx, int curroot, double shift, double precond_min);
+/* PsociGAbasis::appendScratchVector -> appendVectors (PsociGAbasis.C:362, :725-842):
+ * orthonormalise the scratch vector against the basis, append it and form its H*v; *appended
+ * receives 1, or 0 when no new direction survived (the basis is unchanged).  A full basis
+ * answers PSOCI_ERR_STATE (the reference fails there too): call psoci_basis_expand_replace. */
+PSOCI_API psoci_status psoci_basis_append_scratch(psoci_ctx *ctx, psoci_prec prec, int *appended);
+/* PsociGAbasis::expandAndReplaceVectorsNew(evecs, num) (PsociGAbasis.C:483-583): the num lowest
+ * Ritz vectors of the last eigen-solve replace the basis, V <- V Y and H*V <- (H*V) Y without
+ * new products; G becomes diagonal.  Y spans the vectors of that eigen-solve, so a vector
+ * appended after it is dropped, as in the reference's collapse.  With num = existing after
+ * the last eigen-solve the first nroots vectors are the solution. */
+PSOCI_API psoci_status psoci_basis_expand_replace(psoci_ctx *ctx, int num);
+/* CurrentExistingRoots, CurrentNumSoughtRoots, CurrentMaxRoots, present_matrixProducts of
+ * PsociGAbasis (PsociGAbasis.C:137-173); NULLs allowed. */
+PSOCI_API psoci_status psoci_basis_info(const psoci_ctx *ctx, int *existing, int *sought, int *max_vectors,
+                                        int *products);
+/* The first k basis vectors to the host, root-major (vector j at j*N). */
+PSOCI_API psoci_status psoci_basis_vectors(psoci_ctx *ctx, int k, double *vecs);
+
 /* Eigenpairs of a symmetric n x n matrix G (row stride ldg; the halves are averaged): the
  * eigen-solve of PsociGAsubspace::diagSubspaceGOP (PsociGAsubspace.C:1088-1171, LAPACK dsygv)
  * with the unit metric of an orthonormal basis, as psoci_davidson runs it.  w[n] ascending;

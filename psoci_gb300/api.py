@@ -99,6 +99,20 @@ SIGNATURES = {
     "psoci_write_vectors": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int, ctypes.c_int64, ctypes.c_int, _DP,
                                            ctypes.c_char_p]),
     "psoci_read_vectors": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int, ctypes.c_int64, ctypes.c_int, _DP, _IP]),
+    "psoci_basis_create": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int]),
+    "psoci_basis_destroy": (None, [_P]),
+    "psoci_basis_guess": (ctypes.c_int, [_P, ctypes.c_int]),
+    "psoci_basis_orthonormalize_all": (ctypes.c_int, [_P, _IP]),
+    "psoci_basis_compute_hv": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
+    "psoci_subspace_generate_incremental": (ctypes.c_int, [_P, ctypes.c_int]),
+    "psoci_subspace_diag": (ctypes.c_int, [_P, _DP]),
+    "psoci_subspace_rnorm_single": (ctypes.c_int, [_P, ctypes.c_int, _DP]),
+    "psoci_subspace_rnorms": (ctypes.c_int, [_P, _DP]),
+    "psoci_basis_precondition_new": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_double, ctypes.c_double]),
+    "psoci_basis_append_scratch": (ctypes.c_int, [_P, ctypes.c_int, _IP]),
+    "psoci_basis_expand_replace": (ctypes.c_int, [_P, ctypes.c_int]),
+    "psoci_basis_info": (ctypes.c_int, [_P, _IP, _IP, _IP, _IP]),
+    "psoci_basis_vectors": (ctypes.c_int, [_P, ctypes.c_int, _DP]),
     "psoci_save_hamiltonian": (ctypes.c_int, [_P, ctypes.c_char_p]),
     "psoci_load_hamiltonian": (ctypes.c_int, [_P, ctypes.c_char_p]),
 }

@@ -14,6 +14,7 @@ psoci_status set_device(psoci_ctx *c) {
   return PSOCI_OK;
 }
 void release_all(psoci_ctx *c) {
+  psoci_basis_release(c);
   psoci_h_release(c);
   psoci_dets_release(c);
   psoci_join_release(c);

@@ -1049,3 +1049,451 @@ psoci_status psoci_davidson_impl(psoci_ctx *c, const psoci_dav_opts *o, double *
   if (!o) return psoci_fail(c, PSOCI_ERR_INVALID_ARG, "davidson: null options");
   return davidson_run(c, c->nsef_total, c->d_diag, nullptr, o, false, evals, evecs, rnorms, stats, nullptr);
 }
+
+// ------------------------------------------------------------------------------------
+// Step-level Davidson: the basis and subspace objects of the reference's own loop
+// (driver.PSOCI.splittest.C:1186-1311), kept on the device between calls so that a host
+// program can keep that loop line for line:
+//   PsociGAbasis    (PsociGAbasis.C)    vectors V and products HV, guess, orthonormalisation,
+//                                       H*v products, precondition, append, expand-and-replace
+//   PsociGAsubspace (PsociGAsubspace.C) new columns of the projected matrix, its eigen-solve,
+//                                       residual norms
+// The basis is kept orthonormal (CGS2 + Cholesky-QR twice, as psoci_davidson does), so the
+// overlap matrix S of generateIncrementalSubspace is the identity and diagSubspaceGOP's dsygv
+// reduces to a symmetric eigen-solve.  psoci_davidson stays the fast path: it advances all
+// unconverged roots per iteration and runs its FP32-element phase with FP32 subspace products.
+// ------------------------------------------------------------------------------------
+namespace {
+
+// R[r, col] = HX[r, col] - theta * X[r, col] (row stride ld) and the block partial sums of
+// its squares
+__global__ void k_residual_col(int64_t n, int ld, int col, const double *__restrict__ X,
+                               const double *__restrict__ HX, const double *__restrict__ theta,
+                               double *__restrict__ R, double *__restrict__ partial) {
+  __shared__ double red[8];
+  const double th = *theta;
+  double s = 0.0;
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+    const double v = HX[r * ld + col] - th * X[r * ld + col];
+    R[r * ld + col] = v;
+    s = fma(v, v, s);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < 8; ++w) t += red[w];
+    partial[blockIdx.x] = t;
+  }
+}
+
+__global__ void k_set_diag(double *G, int ld, int m, const double *theta) {
+  for (int e = threadIdx.x; e < m * m; e += blockDim.x) {
+    const int i = e / m, j = e % m;
+    G[i * ld + j] = (i == j) ? theta[i] : 0.0;
+  }
+}
+
+}  // namespace
+
+struct psoci_dav_basis {
+  Work w;
+  int nr = 0;         // sought roots
+  int maxv = 0;       // vectors the basis holds
+  int m = 0;          // existing vectors
+  int products = 0;   // vectors 0..products-1 have their H*v
+  int gcols = 0;      // columns of G formed
+  bool have_eig = false;
+  int eig_m = 0;      // basis size of the last eigen-solve (Y is eig_m x eig_m)
+  bool scratch = false;          // T[:, 0] holds a preconditioned vector ready to append
+  unsigned res_valid = 0;        // bit j: R[:, j] is the residual of root j+1 of the current eigen-solve
+  std::vector<double> h_theta, h_y, h_g;
+  double *shift = nullptr;       // device [16]: the preconditioner's shift at the root's slot
+  int64_t N = 0;
+  ~psoci_dav_basis() { psoci_free(shift); }
+};
+
+void psoci_basis_release(psoci_ctx *c) {
+  delete c->basis;
+  c->basis = nullptr;
+}
+
+namespace {
+psoci_status basis_ready(psoci_ctx *c, const char *what) {
+  if (!c) return PSOCI_ERR_INVALID_ARG;
+  if (!c->basis) return psoci_fail(c, PSOCI_ERR_STATE, std::string(what) + ": no basis (psoci_basis_create)");
+  if (!c->have_h || c->basis->N != c->nsef_total)
+    return psoci_fail(c, PSOCI_ERR_STATE, std::string(what) + ": the Hamiltonian changed since psoci_basis_create");
+  PSOCI_CUDA(c, cudaSetDevice(c->device));
+  return PSOCI_OK;
+}
+}  // namespace
+
+extern "C" {
+
+psoci_status psoci_basis_create(psoci_ctx *c, int nroots, int max_vectors) {
+  if (!c) return PSOCI_ERR_INVALID_ARG;
+  if (!c->have_h) return psoci_fail(c, PSOCI_ERR_STATE, "basis_create: Hamiltonian not built");
+  const int64_t N = c->nsef_total;
+  if (nroots < 1 || nroots > 16 || nroots > N)
+    return psoci_fail(c, PSOCI_ERR_INVALID_ARG, "basis_create: nroots must be 1..16 and <= N");
+  if (max_vectors < nroots + 1 || max_vectors > MAX_SUB || max_vectors > N)
+    return psoci_fail(c, PSOCI_ERR_INVALID_ARG, "basis_create: max_vectors must be nroots+1..96 and <= N");
+  PSOCI_CUDA(c, cudaSetDevice(c->device));
+  psoci_basis_release(c);
+  psoci_dav_basis *b = new psoci_dav_basis();
+  c->basis = b;
+  Work &w = b->w;
+  b->nr = nroots;
+  b->maxv = max_vectors;
+  b->N = N;
+  w.c = c;
+  w.N = N;
+  w.nr = nroots;
+  w.ld = (max_vectors + 1) & ~1;
+  const int ld = w.ld;
+  w.nblk = (int)std::min<int64_t>(std::max<int64_t>(1, (N + 255) / 256), 152 * 4);
+  w.rows_per_blk = (N + w.nblk - 1) / w.nblk;
+  psoci_status s;
+  if ((s = psoci_alloc(c, &w.V, (size_t)N * ld)) || (s = psoci_alloc(c, &w.HV, (size_t)N * ld)) ||
+      (s = psoci_alloc(c, &w.G, (size_t)ld * ld)) || (s = psoci_alloc(c, &w.Y, (size_t)ld * ld)) ||
+      (s = psoci_alloc(c, &w.theta, ld)) || (s = psoci_alloc(c, &w.X, (size_t)N * nroots)) ||
+      (s = psoci_alloc(c, &w.HX, (size_t)N * nroots)) || (s = psoci_alloc(c, &w.R, (size_t)N * nroots)) ||
+      (s = psoci_alloc(c, &w.T, (size_t)N * nroots)) || (s = psoci_alloc(c, &w.tmp, (size_t)N * ld)) ||
+      (s = psoci_alloc(c, &w.partial, (size_t)w.nblk * MAX_SUB * TN_MAXK)) ||
+      (s = psoci_alloc(c, &w.small, (size_t)ld * ld)) || (s = psoci_alloc(c, &w.F, 16 * 16)) ||
+      (s = psoci_alloc(c, &w.norms, 16)) || (s = psoci_alloc(c, &w.sel, 16)) || (s = psoci_alloc(c, &w.ibuf, 4)) ||
+      (s = psoci_alloc(c, &w.idx, 16)) || (s = psoci_alloc(c, &w.x32, (size_t)N * 16)) ||
+      (s = psoci_alloc(c, &b->shift, 16))) {
+    psoci_basis_release(c);
+    return s;
+  }
+  b->h_theta.assign(ld, 0.0);
+  b->h_y.assign((size_t)ld * ld, 0.0);
+  b->h_g.assign((size_t)ld * ld, 0.0);
+  PSOCI_CUDA(c, cudaMemsetAsync(w.V, 0, sizeof(double) * N * ld, c->stream));
+  PSOCI_CUDA(c, cudaMemsetAsync(w.G, 0, sizeof(double) * ld * ld, c->stream));
+  PSOCI_CUDA(c, cudaStreamSynchronize(c->stream));
+  return PSOCI_OK;
+}
+
+void psoci_basis_destroy(psoci_ctx *c) {
+  if (!c) return;
+  cudaSetDevice(c->device);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  psoci_basis_release(c);
+}
+
+psoci_status psoci_basis_guess(psoci_ctx *c, int mode) {
+  psoci_status s;
+  if ((s = basis_ready(c, "basis_guess"))) return s;
+  psoci_dav_basis *b = c->basis;
+  Work &w = b->w;
+  const int64_t N = b->N;
+  const int nr = b->nr, ld = w.ld;
+  cudaStream_t st = c->stream;
+  if (mode < 0 || mode > 2) return psoci_fail(c, PSOCI_ERR_INVALID_ARG, "basis_guess: mode must be 0, 1 or 2");
+  std::vector<int64_t> order(nr);
+  int kg = 0;
+  if (mode == 0) {
+    std::iota(order.begin(), order.end(), 0);
+  } else {
+    std::vector<double> hd(N);
+    PSOCI_CUDA(c, cudaMemcpyAsync(hd.data(), c->d_diag, sizeof(double) * N, cudaMemcpyDeviceToHost, st));
+    PSOCI_CUDA(c, cudaStreamSynchronize(st));
+    std::vector<int64_t> all(N);
+    std::iota(all.begin(), all.end(), 0);
+    std::partial_sort(all.begin(), all.begin() + nr, all.end(),
+                      [&](int64_t x, int64_t y) { return hd[x] < hd[y] || (hd[x] == hd[y] && x < y); });
+    std::copy(all.begin(), all.begin() + nr, order.begin());
+    if (mode == 2 && c->guess_k > 0 && (int64_t)c->guess.size() == (int64_t)c->guess_k * N) kg = std::min(nr, c->guess_k);
+  }
+  PSOCI_CUDA(c, cudaMemsetAsync(w.V, 0, sizeof(double) * N * ld, st));
+  PSOCI_CUDA(c, cudaMemsetAsync(w.G, 0, sizeof(double) * ld * ld, st));
+  if (kg > 0) {
+    // restart vectors (root-major on the host) into the first columns, row-major on the device
+    std::vector<double> t((size_t)N * kg);
+    for (int j = 0; j < kg; ++j)
+      for (int64_t r = 0; r < N; ++r) t[(size_t)r * kg + j] = c->guess[(size_t)j * N + r];
+    PSOCI_CUDA(c, cudaMemcpy2DAsync(w.V, sizeof(double) * ld, t.data(), sizeof(double) * kg, sizeof(double) * kg, N,
+                                    cudaMemcpyHostToDevice, st));
+  }
+  if (kg < nr) {
+    PSOCI_CUDA(c, cudaMemcpyAsync(w.idx, order.data(), sizeof(int64_t) * (nr - kg), cudaMemcpyHostToDevice, st));
+    psoci_note_launch();
+    k_set_unit<<<1, 32, 0, st>>>(w.V, ld, kg, w.idx, nr - kg);
+    PSOCI_CUDA(c, cudaGetLastError());
+  }
+  PSOCI_CUDA(c, cudaStreamSynchronize(st));
+  b->m = nr;
+  b->products = 0;
+  b->gcols = 0;
+  b->have_eig = false;
+  b->scratch = false;
+  b->res_valid = 0;
+  return PSOCI_OK;
+}
+
+psoci_status psoci_basis_orthonormalize_all(psoci_ctx *c, int *dependent_at) {
+  psoci_status s;
+  if ((s = basis_ready(c, "basis_orthonormalize_all"))) return s;
+  psoci_dav_basis *b = c->basis;
+  Work &w = b->w;
+  if (dependent_at) *dependent_at = 0;
+  if (b->m > b->nr)
+    return psoci_fail(c, PSOCI_ERR_UNSUPPORTED, "basis_orthonormalize_all: at most nroots vectors (the guess set)");
+  const int m = b->m;
+  if (m == 0) return PSOCI_OK;
+  copy_cols(w, w.V, w.ld, w.T, w.nr, m);
+  PSOCI_CUDA(c, cudaMemsetAsync(w.V, 0, sizeof(double) * b->N * w.ld, c->stream));
+  int bk = 0;
+  if ((s = orthonormalize(w, 0, m, &bk))) return s;
+  PSOCI_CUDA(c, cudaStreamSynchronize(c->stream));
+  b->products = 0;
+  b->gcols = 0;
+  b->have_eig = false;
+  b->res_valid = 0;
+  if (bk < m) {
+    b->m = bk;
+    if (dependent_at) *dependent_at = bk + 1;
+    return psoci_fail(c, PSOCI_ERR_NUMERIC, "basis_orthonormalize_all: linear dependency among the vectors");
+  }
+  return PSOCI_OK;
+}
+
+psoci_status psoci_basis_compute_hv(psoci_ctx *c, int start, int num, psoci_prec prec) {
+  psoci_status s;
+  if ((s = basis_ready(c, "basis_compute_hv"))) return s;
+  psoci_dav_basis *b = c->basis;
+  if (start < 0 || num < 1 || start + num > b->m)
+    return psoci_fail(c, PSOCI_ERR_INVALID_ARG, "basis_compute_hv: columns outside the existing vectors");
+  if (start > b->products) return psoci_fail(c, PSOCI_ERR_STATE, "basis_compute_hv: earlier products missing");
+  if (prec == PSOCI_PREC_MIXED && !c->d_val32 && !c->direct)
+    return psoci_fail(c, PSOCI_ERR_STATE, "basis_compute_hv: MIXED needs PSOCI_HMODE_CSR_BOTH");
+  Work &w = b->w;
+  if ((s = sigma_block(w, w.V + start, w.ld, w.HV + start, w.ld, num, prec))) return s;
+  PSOCI_CUDA(c, cudaStreamSynchronize(c->stream));
+  b->products = std::max(b->products, start + num);
+  return PSOCI_OK;
+}
+
+psoci_status psoci_subspace_generate_incremental(psoci_ctx *c, int num) {
+  psoci_status s;
+  if ((s = basis_ready(c, "subspace_generate_incremental"))) return s;
+  psoci_dav_basis *b = c->basis;
+  Work &w = b->w;
+  const int m = b->m;
+  if (num < 1 || num > m) return psoci_fail(c, PSOCI_ERR_INVALID_ARG, "subspace_generate_incremental: bad num");
+  if (b->products < m) return psoci_fail(c, PSOCI_ERR_STATE, "subspace_generate_incremental: H*v products missing");
+  if (m - num > b->gcols) return psoci_fail(c, PSOCI_ERR_STATE, "subspace_generate_incremental: earlier columns missing");
+  for (int c0 = m - num; c0 < m; c0 += TN_MAXK) {
+    const int k = std::min(TN_MAXK, m - c0);
+    if ((s = tn(w, w.V, w.ld, 0, m, w.HV, w.ld, c0, k, w.G, w.ld, c0))) return s;
+  }
+  psoci_note_launch();
+  k_symmetrize<<<1, 256, 0, c->stream>>>(w.G, w.ld, m - num, m);
+  PSOCI_CUDA(c, cudaGetLastError());
+  PSOCI_CUDA(c, cudaStreamSynchronize(c->stream));
+  b->gcols = m;
+  b->have_eig = false;
+  b->res_valid = 0;
+  return PSOCI_OK;
+}
+
+psoci_status psoci_subspace_diag(psoci_ctx *c, double *evals) {
+  psoci_status s;
+  if ((s = basis_ready(c, "subspace_diag"))) return s;
+  psoci_dav_basis *b = c->basis;
+  Work &w = b->w;
+  const int m = b->m, ld = w.ld;
+  if (m < 1 || b->gcols < m) return psoci_fail(c, PSOCI_ERR_STATE, "subspace_diag: projected matrix incomplete");
+  cudaStream_t st = c->stream;
+  PSOCI_CUDA(c, cudaMemcpy2DAsync(b->h_g.data(), sizeof(double) * ld, w.G, sizeof(double) * ld, sizeof(double) * m, m,
+                                  cudaMemcpyDeviceToHost, st));
+  PSOCI_CUDA(c, cudaStreamSynchronize(st));
+  if (psoci_subspace_eigen(m, b->h_g.data(), ld, b->h_theta.data(), b->h_y.data(), ld) != PSOCI_OK)
+    return psoci_fail(c, PSOCI_ERR_NUMERIC, "subspace_diag: eigen-solve failed");
+  for (int j = 0; j < m; ++j)
+    if (!std::isfinite(b->h_theta[j])) return psoci_fail(c, PSOCI_ERR_NUMERIC, "subspace_diag: non-finite Ritz value");
+  PSOCI_CUDA(c, cudaMemcpy2DAsync(w.Y, sizeof(double) * ld, b->h_y.data(), sizeof(double) * ld, sizeof(double) * m, m,
+                                  cudaMemcpyHostToDevice, st));
+  PSOCI_CUDA(c, cudaMemcpyAsync(w.theta, b->h_theta.data(), sizeof(double) * m, cudaMemcpyHostToDevice, st));
+  PSOCI_CUDA(c, cudaStreamSynchronize(st));
+  if (evals) std::copy(b->h_theta.begin(), b->h_theta.begin() + m, evals);
+  b->have_eig = true;
+  b->eig_m = m;
+  b->res_valid = 0;
+  return PSOCI_OK;
+}
+
+namespace {
+// residual of root j (0-based) of the current eigen-solve into R[:, j]; |r|^2 to *nrm2
+psoci_status basis_residual(psoci_ctx *c, int j, double *nrm2) {
+  psoci_dav_basis *b = c->basis;
+  Work &w = b->w;
+  psoci_status s;
+  const int nr = b->nr;
+  if ((s = nn(w, w.V, w.ld, 0, b->eig_m, w.Y, w.ld, j, 1, 1.0, 0.0, w.X, nr, j))) return s;
+  if ((s = nn(w, w.HV, w.ld, 0, b->eig_m, w.Y, w.ld, j, 1, 1.0, 0.0, w.HX, nr, j))) return s;
+  const int rb = (int)std::min<int64_t>((b->N + 255) / 256, 152 * 4);
+  psoci_note_launch();
+  k_residual_col<<<rb, 256, 0, c->stream>>>(b->N, nr, j, w.X, w.HX, w.theta + j, w.R, w.partial);
+  psoci_note_launch();
+  k_sum_cols<<<1, 32, 0, c->stream>>>(w.partial, rb, 1, w.norms);
+  PSOCI_CUDA(c, cudaGetLastError());
+  PSOCI_CUDA(c, cudaMemcpyAsync(nrm2, w.norms, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  PSOCI_CUDA(c, cudaStreamSynchronize(c->stream));
+  b->res_valid |= 1u << j;
+  return PSOCI_OK;
+}
+}  // namespace
+
+psoci_status psoci_subspace_rnorm_single(psoci_ctx *c, int iroot, double *rnorm) {
+  psoci_status s;
+  if ((s = basis_ready(c, "subspace_rnorm_single"))) return s;
+  psoci_dav_basis *b = c->basis;
+  if (!rnorm) return psoci_fail(c, PSOCI_ERR_INVALID_ARG, "subspace_rnorm_single: null rnorm");
+  if (!b->have_eig) return psoci_fail(c, PSOCI_ERR_STATE, "subspace_rnorm_single: no eigen-solve (psoci_subspace_diag)");
+  if (iroot < 1 || iroot > b->nr || iroot > b->eig_m)
+    return psoci_fail(c, PSOCI_ERR_INVALID_ARG, "subspace_rnorm_single: root outside 1..nroots");
+  double r2 = 0.0;
+  if ((s = basis_residual(c, iroot - 1, &r2))) return s;
+  if (!std::isfinite(r2)) return psoci_fail(c, PSOCI_ERR_NUMERIC, "subspace_rnorm_single: non-finite residual");
+  *rnorm = std::sqrt(r2);
+  return PSOCI_OK;
+}
+
+psoci_status psoci_subspace_rnorms(psoci_ctx *c, double *rnorms) {
+  psoci_status s;
+  if ((s = basis_ready(c, "subspace_rnorms"))) return s;
+  psoci_dav_basis *b = c->basis;
+  if (!rnorms) return psoci_fail(c, PSOCI_ERR_INVALID_ARG, "subspace_rnorms: null rnorms");
+  if (!b->have_eig) return psoci_fail(c, PSOCI_ERR_STATE, "subspace_rnorms: no eigen-solve (psoci_subspace_diag)");
+  const int n = std::min(b->nr, b->eig_m);
+  for (int j = 0; j < n; ++j) {
+    double r2 = 0.0;
+    if ((s = basis_residual(c, j, &r2))) return s;
+    if (!std::isfinite(r2)) return psoci_fail(c, PSOCI_ERR_NUMERIC, "subspace_rnorms: non-finite residual");
+    rnorms[j] = std::sqrt(r2);
+  }
+  return PSOCI_OK;
+}
+
+psoci_status psoci_basis_precondition_new(psoci_ctx *c, int curroot, double shift, double precond_min) {
+  psoci_status s;
+  if ((s = basis_ready(c, "basis_precondition_new"))) return s;
+  psoci_dav_basis *b = c->basis;
+  Work &w = b->w;
+  if (curroot < 1 || curroot > b->nr) return psoci_fail(c, PSOCI_ERR_INVALID_ARG, "basis_precondition_new: bad root");
+  if (!(b->res_valid & (1u << (curroot - 1))))
+    return psoci_fail(c, PSOCI_ERR_STATE, "basis_precondition_new: no residual of this root (psoci_subspace_rnorm_single)");
+  const int j = curroot - 1;
+  const double dmin = precond_min > 0 ? precond_min : 1e-3;
+  cudaStream_t st = c->stream;
+  PSOCI_CUDA(c, cudaMemcpyAsync(b->shift + j, &shift, sizeof(double), cudaMemcpyHostToDevice, st));
+  PSOCI_CUDA(c, cudaMemcpyAsync(w.sel, &j, sizeof(int), cudaMemcpyHostToDevice, st));
+  const int pb = (int)std::min<int64_t>((b->N + 255) / 256, 152 * 16);
+  psoci_note_launch();
+  if (b->N * 32 < (int64_t)UINT32_MAX)
+    k_precond<uint32_t><<<pb, 256, 0, st>>>(b->N, b->nr, w.R, c->d_diag, b->shift, w.sel, 1, dmin, w.T, b->nr);
+  else
+    k_precond<uint64_t><<<pb, 256, 0, st>>>(b->N, b->nr, w.R, c->d_diag, b->shift, w.sel, 1, dmin, w.T, b->nr);
+  PSOCI_CUDA(c, cudaGetLastError());
+  PSOCI_CUDA(c, cudaStreamSynchronize(st));
+  b->scratch = true;
+  return PSOCI_OK;
+}
+
+psoci_status psoci_basis_append_scratch(psoci_ctx *c, psoci_prec prec, int *appended) {
+  psoci_status s;
+  if ((s = basis_ready(c, "basis_append_scratch"))) return s;
+  psoci_dav_basis *b = c->basis;
+  Work &w = b->w;
+  if (appended) *appended = 0;
+  if (!b->scratch) return psoci_fail(c, PSOCI_ERR_STATE, "basis_append_scratch: no preconditioned vector");
+  if (b->m + 1 > b->maxv)
+    return psoci_fail(c, PSOCI_ERR_STATE, "basis_append_scratch: basis full (psoci_basis_expand_replace first)");
+  if (b->products < b->m) return psoci_fail(c, PSOCI_ERR_STATE, "basis_append_scratch: H*v products missing");
+  if (prec == PSOCI_PREC_MIXED && !c->d_val32 && !c->direct)
+    return psoci_fail(c, PSOCI_ERR_STATE, "basis_append_scratch: MIXED needs PSOCI_HMODE_CSR_BOTH");
+  int bk = 0;
+  if ((s = orthonormalize(w, b->m, 1, &bk))) return s;
+  b->scratch = false;
+  b->res_valid = 0;
+  if (bk == 0) return PSOCI_OK;  // no new direction: the basis is unchanged
+  if ((s = sigma_block(w, w.V + b->m, w.ld, w.HV + b->m, w.ld, bk, prec))) return s;
+  PSOCI_CUDA(c, cudaStreamSynchronize(c->stream));
+  b->m += bk;
+  b->products = b->m;
+  if (appended) *appended = bk;
+  return PSOCI_OK;
+}
+
+psoci_status psoci_basis_expand_replace(psoci_ctx *c, int num) {
+  psoci_status s;
+  if ((s = basis_ready(c, "basis_expand_replace"))) return s;
+  psoci_dav_basis *b = c->basis;
+  Work &w = b->w;
+  const int m = b->eig_m, ld = w.ld;
+  if (!b->have_eig) return psoci_fail(c, PSOCI_ERR_STATE, "basis_expand_replace: no eigen-solve (psoci_subspace_diag)");
+  if (num < 1 || num > m)
+    return psoci_fail(c, PSOCI_ERR_INVALID_ARG, "basis_expand_replace: num outside 1..vectors of the last eigen-solve");
+  if (b->products < m) return psoci_fail(c, PSOCI_ERR_STATE, "basis_expand_replace: H*v products missing");
+  // V <- V[:, :m] Y[:, :num] and HV <- HV[:, :m] Y[:, :num] (no new products), through tmp;
+  // m is the basis of the last eigen-solve, so vectors appended after it are dropped, as the
+  // reference's expansion with the subspace eigenvectors drops them
+  for (int pass = 0; pass < 2; ++pass) {
+    double *A = pass == 0 ? w.V : w.HV;
+    for (int c0 = 0; c0 < num; c0 += NN_MAXK) {
+      const int k = std::min(NN_MAXK, num - c0);
+      if ((s = nn(w, A, ld, 0, m, w.Y, ld, c0, k, 1.0, 0.0, w.tmp, ld, c0))) return s;
+    }
+    copy_cols(w, w.tmp, ld, A, ld, num);
+  }
+  psoci_note_launch();
+  k_set_diag<<<1, 256, 0, c->stream>>>(w.G, ld, num, w.theta);
+  PSOCI_CUDA(c, cudaGetLastError());
+  PSOCI_CUDA(c, cudaStreamSynchronize(c->stream));
+  // the expanded vectors are the Ritz vectors: the eigen-solve of the new G is diagonal
+  for (int i = 0; i < num; ++i)
+    for (int j = 0; j < num; ++j) b->h_y[(size_t)i * ld + j] = (i == j) ? 1.0 : 0.0;
+  PSOCI_CUDA(c, cudaMemcpy2DAsync(w.Y, sizeof(double) * ld, b->h_y.data(), sizeof(double) * ld, sizeof(double) * num,
+                                  num, cudaMemcpyHostToDevice, c->stream));
+  PSOCI_CUDA(c, cudaStreamSynchronize(c->stream));
+  b->m = num;
+  b->products = num;
+  b->gcols = num;
+  b->eig_m = num;
+  b->res_valid = 0;
+  b->scratch = false;
+  return PSOCI_OK;
+}
+
+psoci_status psoci_basis_info(const psoci_ctx *cc, int *existing, int *sought, int *max_vectors, int *products) {
+  psoci_ctx *c = const_cast<psoci_ctx *>(cc);
+  if (!c) return PSOCI_ERR_INVALID_ARG;
+  if (!c->basis) return psoci_fail(c, PSOCI_ERR_STATE, "basis_info: no basis (psoci_basis_create)");
+  if (existing) *existing = c->basis->m;
+  if (sought) *sought = c->basis->nr;
+  if (max_vectors) *max_vectors = c->basis->maxv;
+  if (products) *products = c->basis->products;
+  return PSOCI_OK;
+}
+
+psoci_status psoci_basis_vectors(psoci_ctx *c, int k, double *vecs) {
+  psoci_status s;
+  if ((s = basis_ready(c, "basis_vectors"))) return s;
+  psoci_dav_basis *b = c->basis;
+  if (!vecs || k < 1 || k > b->m) return psoci_fail(c, PSOCI_ERR_INVALID_ARG, "basis_vectors: k outside 1..existing");
+  std::vector<double> t((size_t)b->N * k);
+  PSOCI_CUDA(c, cudaMemcpy2DAsync(t.data(), sizeof(double) * k, b->w.V, sizeof(double) * b->w.ld, sizeof(double) * k,
+                                  b->N, cudaMemcpyDeviceToHost, c->stream));
+  PSOCI_CUDA(c, cudaStreamSynchronize(c->stream));
+  for (int64_t r = 0; r < b->N; ++r)
+    for (int j = 0; j < k; ++j) vecs[(size_t)j * b->N + r] = t[(size_t)r * k + j];
+  return PSOCI_OK;
+}
+
+}  // extern "C"

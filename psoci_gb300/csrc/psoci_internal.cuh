@@ -111,6 +111,9 @@ struct psoci_ctx {
   float2 *den_vs = nullptr;      // float-float copy of the roots of one pass
   size_t den_vs_cap = 0;
 
+  // step-level Davidson basis (psoci_basis_*, davidson.cu)
+  struct psoci_dav_basis *basis = nullptr;
+
   // initial guess for the next Davidson run (root-major, guess_k x nsef)
   std::vector<double> guess;
   int guess_k = 0;
@@ -201,6 +204,7 @@ void psoci_join_release(psoci_ctx *c);
 void psoci_h_release(psoci_ctx *c);
 void psoci_dets_release(psoci_ctx *c);
 void psoci_density_release(psoci_ctx *c);
+void psoci_basis_release(psoci_ctx *c);
 
 // ------------------------------------------------------------------------------------
 // device helpers

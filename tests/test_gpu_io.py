@@ -147,3 +147,38 @@ def test_bad_inputs_reported_in_order_on_large_lists():
         with pytest.raises(api.PsociError, match="configuration 40000 orbital 3 occupation 3"):
             c.set_configs(p.nbf, p.nelec, p.ksym, p.mx_open, p.jsym, occ)
         c.set_configs(p.nbf, p.nelec, p.ksym, p.mx_open, p.jsym, p.occ)
+
+
+def test_cpp_reference_loop(tmp_path, oracle_mod):
+    """-L: the reference's own Davidson loop (one vector per iteration, coarse then final
+    tolerance, collapse to 2 x roots) through the step-level PsociGAbasis / PsociGAsubspace
+    methods of the C++ mirror, against the one-call solve and the oracle's spectrum."""
+    from psoci_gb300 import build, inputs
+
+    build.build()
+    p = small_problem("fci_6e8o", 1)
+    cfg, ints = str(tmp_path / "configs"), str(tmp_path / "ints.bin")
+    inputs.write_config_file(cfg, p)
+    inputs.write_integral_file(ints, p)
+    ref = _ref_evals(oracle_mod, p, 4)
+    runs = {}
+    for name, extra in (("solve", ["-p", "0"]), ("loop", ["-L"])):
+        vec = str(tmp_path / f"v_{name}.txt")
+        out = subprocess.run([build.DRIVER, "-c", cfg, "-m", ints, "-n", "4", "-F", "1e-8", "-x", "4", "-v", vec] + extra,
+                             capture_output=True, text=True, timeout=300)
+        assert out.returncode == 0, out.stderr
+        ev = np.array([float(m.group(1)) for m in re.finditer(r"Electronic \(au\) (\S+)", out.stdout)])
+        iters = int(re.search(r"Number of total iterations is (\d+)", out.stdout).group(1))
+        coll = int(re.search(r"Number of SUBSPACE contractions is (\d+)", out.stdout).group(1))
+        runs[name] = (ev, iters, coll, vec)
+    ev_s, _, _, _ = runs["solve"]
+    ev_l, it_l, coll_l, vec_l = runs["loop"]
+    assert len(ev_l) == 4
+    assert np.abs(ev_l - ev_s).max() <= 1e-10, (ev_l, ev_s)
+    assert np.abs(ev_l - ref).max() <= 1e-10
+    assert it_l > 4 and coll_l >= 1  # one vector per iteration, with collapses
+    # the loop's vectors restart the loop: already converged at the coarse and final tolerance
+    out = subprocess.run([build.DRIVER, "-c", cfg, "-m", ints, "-n", "4", "-F", "1e-8", "-v", vec_l, "-r", "-L"],
+                         capture_output=True, text=True, timeout=300)
+    assert out.returncode == 0, out.stderr
+    assert int(re.search(r"Number of total iterations is (\d+)", out.stdout).group(1)) <= 3
