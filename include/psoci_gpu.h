@@ -300,6 +300,29 @@ PSOCI_API psoci_status psoci_density1(psoci_ctx *ctx, int k, const double *vecs,
  * The first call after new configurations also forms the configuration groups. */
 PSOCI_API psoci_status psoci_density1_device(psoci_ctx *ctx, int k, const double *dV, int64_t ldv, double *dD);
 
+/* Energy gradients with respect to the integral tables (Hellmann-Feynman): for each of k CI
+ * vectors c_r (normalised eigenvectors, root-major k x N), dE_r/d one[t] and dE_r/d eri[t] of
+ * E_r = c_r^T H c_r, in the packed layouts psoci_set_integrals takes.  grad_one (k x
+ * nbf(nbf+1)/2): the spin-free 1-particle density on entries of equal irreps (diagonal: the
+ * occupations of psoci_density1; off the diagonal: twice its value) and the spin-orbit density
+ * dE/dSO_pq on entries of unequal irreps; grad_eri (k x NNDAF(NNDAF(nbf))): the 2-particle
+ * density in the reference's canonical 8-fold packed layout (PsociIntegrals.C:889-909).
+ * There is no counterpart in the reference, whose only density is the CIDEN 1-particle
+ * density; the kernel is the adjoint of the element evaluation (PsociHamiltonian.C:139-1118):
+ * every determinant coupling adds its weight to the table entries its element reads.
+ * mode 0: every pair of configurations within two excitations, so every entry's derivative
+ * (also of integrals that are zero); mode 1: pairs whose integral prefactors are all zero are
+ * skipped and the entries of zero integrals are reported as 0 (the derivatives of the
+ * non-zero integrals, at less work).  prec: PSOCI_PREC_FP64, or PSOCI_PREC_MIXED (sums within
+ * a configuration pair in FP32, across pairs in FP64).  The state average of the k roots is
+ * the mean of the k gradients.  Needs psoci_build_determinants; the Hamiltonian is not used. */
+PSOCI_API psoci_status psoci_energy_gradient(psoci_ctx *ctx, int k, const double *vecs, int mode, psoci_prec prec,
+                                             double *grad_one, double *grad_eri);
+/* The same on device memory: dV k vectors with stride ldv (root-major), dG1 k x nbf(nbf+1)/2,
+ * dG2 k x NNDAF(NNDAF(nbf)) (overwritten); returns after the kernels have finished. */
+PSOCI_API psoci_status psoci_energy_gradient_device(psoci_ctx *ctx, int k, const double *dV, int64_t ldv, int mode,
+                                                    psoci_prec prec, double *dG1, double *dG2);
+
 /* Natural orbitals and occupations of one packed 1-particle density (the MO-basis part of
  * PsociNOpopulations::constructNaturalOrbitals, PsociNOpopulations.C:569-669: per symmetry
  * block diagonalizeNOinMObasis :456-497 with a unit metric, then sortNOinMObasis :269-344,

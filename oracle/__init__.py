@@ -171,6 +171,20 @@ class Oracle(_Base):
             self.ctx, v.shape[0], _p(v, _c_dbl_p), len(r), _p(r, _c_int_p), _p(out, _c_dbl_p))
         return out
 
+    def energy_gradient(self, vecs, nonzero_only=False, nthreads=0):
+        """dE_r / d(packed one-electron table) [k, nbf(nbf+1)/2] and dE_r / d(canonical
+        two-electron table) [k, NNDAF(NNDAF(nbf))] of E_r = v_r^T H v_r, one unit-table
+        build per entry (see psoci_oracle.c)."""
+        nthreads = nthreads or os.cpu_count() or 1
+        v = np.ascontiguousarray(np.atleast_2d(vecs), np.float64)
+        n1 = self.p.nbf * (self.p.nbf + 1) // 2
+        g1 = np.zeros((v.shape[0], n1))
+        g2 = np.zeros((v.shape[0], n1 * (n1 + 1) // 2))
+        self._fn("energy_gradient", None, [ctypes.c_void_p, ctypes.c_int, _c_dbl_p, ctypes.c_int, _c_dbl_p, _c_dbl_p,
+                                           ctypes.c_int])(self.ctx, v.shape[0], _p(v, _c_dbl_p), int(nonzero_only),
+                                                          _p(g1, _c_dbl_p), _p(g2, _c_dbl_p), nthreads)
+        return g1, g2
+
     def diag(self):
         d = np.zeros(self.num_sefs())
         self._fn("diag", None, [ctypes.c_void_p, _c_dbl_p])(self.ctx, _p(d, _c_dbl_p))

@@ -36,6 +36,9 @@ void orc_sigma_lower(long n, const long *rowptr, const int *cols, const double *
  * (vecs: k x N root-major; dens: k x nbf(nbf+1)/2). */
 int orc_ciden_block(const orc_ctx *c, int i, int j, double *out);
 void orc_density1(const orc_ctx *c, int k, const double *vecs, double *dens);
+/* energy gradients with respect to the packed tables (see psoci_oracle.c) */
+void orc_energy_gradient(const orc_ctx *c, int k, const double *vecs, int nonzero_only, double *grad_one,
+                         double *grad_eri, int nthreads);
 void orc_density1_rows(const orc_ctx *c, int k, const double *vecs, int nrows, const int *rows, double *dens);
 
 #ifdef __cplusplus

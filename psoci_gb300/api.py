@@ -94,6 +94,9 @@ SIGNATURES = {
     "psoci_set_guess": (ctypes.c_int, [_P, ctypes.c_int, _DP]),
     "psoci_density1": (ctypes.c_int, [_P, ctypes.c_int, _DP, _DP]),
     "psoci_density1_device": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p]),
+    "psoci_energy_gradient": (ctypes.c_int, [_P, ctypes.c_int, _DP, ctypes.c_int, ctypes.c_int, _DP, _DP]),
+    "psoci_energy_gradient_device": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int,
+                                                    ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]),
     "psoci_natural_orbitals": (ctypes.c_int, [ctypes.c_int, _DP, _I32P, _DP, _DP, _I32P]),
     "psoci_subspace_eigen": (ctypes.c_int, [ctypes.c_int, _DP, ctypes.c_int, _DP, _DP, ctypes.c_int]),
     "psoci_write_vectors": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int, ctypes.c_int64, ctypes.c_int, _DP,
@@ -328,6 +331,26 @@ class Context:
         the context's stream."""
         self._check(self.lib.psoci_density1_device(self.ctx, k, ctypes.c_void_p(dV_ptr), ldv,
                                                    ctypes.c_void_p(dD_ptr)), "density1_device")
+
+    def energy_gradient(self, vecs, nonzero_only: bool = False, prec: int = PREC_FP64):
+        """dE_r/d(packed one-electron table) [k, nbf(nbf+1)/2] and dE_r/d(canonical two-electron
+        table) [k, NNDAF(NNDAF(nbf))] for CI vectors [k, N] (root-major): the 1-particle and
+        spin-orbit densities and the 8-fold packed 2-particle density of each root."""
+        v = np.ascontiguousarray(np.atleast_2d(vecs), np.float64)
+        if v.shape[1] != self.nsef:
+            raise ValueError(f"energy_gradient: vectors of length {v.shape[1]}, expected {self.nsef}")
+        n1 = self.nbf * (self.nbf + 1) // 2
+        g1 = np.zeros((v.shape[0], n1))
+        g2 = np.zeros((v.shape[0], n1 * (n1 + 1) // 2))
+        self._check(self.lib.psoci_energy_gradient(self.ctx, v.shape[0], _ptr(v, _DP), int(nonzero_only), prec,
+                                                   _ptr(g1, _DP), _ptr(g2, _DP)), "energy_gradient")
+        return g1, g2
+
+    def energy_gradient_device(self, dV_ptr: int, ldv: int, k: int, dG1_ptr: int, dG2_ptr: int,
+                               nonzero_only: bool = False, prec: int = PREC_FP64):
+        self._check(self.lib.psoci_energy_gradient_device(self.ctx, k, ctypes.c_void_p(dV_ptr), ldv, int(nonzero_only),
+                                                          prec, ctypes.c_void_p(dG1_ptr), ctypes.c_void_p(dG2_ptr)),
+                    "energy_gradient_device")
 
     def core_energy(self) -> float:
         return self.lib.psoci_core_energy(self.ctx)

@@ -341,6 +341,41 @@ psoci_status psoci_get_rows(const psoci_ctx *cc, int nrows, const int64_t *rows,
   return done(PSOCI_OK);
 }
 
+psoci_status psoci_energy_gradient_device(psoci_ctx *c, int k, const double *dV, int64_t ldv, int mode,
+                                          psoci_prec prec, double *dG1, double *dG2) {
+  if (!c) return PSOCI_ERR_INVALID_ARG;
+  psoci_status s;
+  if ((s = set_device(c))) return s;
+  return psoci_energy_grad_run(c, k, dV, ldv, mode, prec, dG1, dG2);
+}
+
+psoci_status psoci_energy_gradient(psoci_ctx *c, int k, const double *vecs, int mode, psoci_prec prec,
+                                   double *grad_one, double *grad_eri) {
+  if (!c) return PSOCI_ERR_INVALID_ARG;
+  if (k < 1 || !vecs || !grad_one || !grad_eri)
+    return psoci_fail(c, PSOCI_ERR_INVALID_ARG, "energy_gradient: bad arguments");
+  if (!c->have_dets) return psoci_fail(c, PSOCI_ERR_STATE, "energy_gradient: determinants not built");
+  psoci_status s;
+  if ((s = set_device(c))) return s;
+  const int64_t N = c->nsef_total, n1 = c->n1, n2 = c->n2;
+  double *dV = nullptr, *dG1 = nullptr, *dG2 = nullptr;
+  auto done = [&](psoci_status r) {
+    psoci_free(dV); psoci_free(dG1); psoci_free(dG2);
+    return r;
+  };
+  if ((s = psoci_alloc(c, &dV, (size_t)k * N)) || (s = psoci_alloc(c, &dG1, (size_t)k * n1)) ||
+      (s = psoci_alloc(c, &dG2, (size_t)k * n2)))
+    return done(s);
+  cudaError_t e = cudaMemcpyAsync(dV, vecs, sizeof(double) * k * N, cudaMemcpyHostToDevice, c->stream);
+  if (e != cudaSuccess) return done(psoci_cuda_fail(c, e, "energy_gradient"));
+  if ((s = psoci_energy_grad_run(c, k, dV, N, mode, prec, dG1, dG2))) return done(s);
+  e = cudaMemcpyAsync(grad_one, dG1, sizeof(double) * k * n1, cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(grad_eri, dG2, sizeof(double) * k * n2, cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return done(psoci_cuda_fail(c, e, "energy_gradient"));
+  return done(PSOCI_OK);
+}
+
 psoci_status psoci_get_diag(const psoci_ctx *cc, double *diag) {
   psoci_ctx *c = const_cast<psoci_ctx *>(cc);
   if (!c || !diag) return PSOCI_ERR_INVALID_ARG;

@@ -36,6 +36,7 @@
 // --fmad=false so products and sums round as the reference's do.
 #include <algorithm>
 #include <chrono>
+#include <climits>
 #include <cstdio>
 #include <functional>
 #include <queue>
@@ -1771,53 +1772,46 @@ psoci_status run_blocks(psoci_ctx *c, int npairs, const int32_t *hA, const int32
   return PSOCI_OK;
 }
 
+// Neighbour lists of every configuration: the configurations within two excitations (sorted),
+// less the pairs whose block the integral tables prune_one / prune_eri make zero (the build
+// passes the Hamiltonian's own tables; a table of ones keeps every pair).  Lookup screen for
+// MRCI-type spaces, all-pairs test otherwise.  d_nbroff [nconf+1] and d_nbr [npairs] are
+// allocated here and owned by the caller.
 template <int W>
-psoci_status run_build(psoci_ctx *c, psoci_hmode mode, int64_t *nnz_out) {
+psoci_status screen_pairs(psoci_ctx *c, const Params &P0, const double *prune_one, const double *prune_eri,
+                          int64_t *&d_nbroff, int32_t *&d_nbr, int64_t &ncand, int64_t &npairs, int &nsplit) {
   cudaStream_t st = c->stream;
   const int n = c->nconf;
-  Params P = {};
-  P.nconf = n; P.nbf = c->nbf; P.nelec = c->nelec; P.ksym = c->ksym;
-  P.e1 = c->d_e1; P.e2 = c->d_e2; P.jsym = c->d_jsym; P.nopen = c->d_nopen;
-  P.sefoff = c->d_sefoff; P.detoff = c->d_detoff;
-  P.alpha = c->d_alpha; P.beta = c->d_beta; P.phase = c->d_phase; P.nalpha = c->d_nalpha;
-  P.one = c->d_one; P.eri = c->d_eri;
-
+  Params P = P0;
+  P.one = prune_one;
+  P.eri = prune_eri;
   psoci_status s;
-  int64_t *d_cnt = nullptr, *d_nbroff = nullptr, *d_nseg = nullptr, *d_nrow = nullptr, *d_segoff = nullptr,
-          *d_rowslot = nullptr, *d_segk0 = nullptr, *d_segrow = nullptr, *d_segcnt = nullptr, *d_rownnz = nullptr;
-  int32_t *d_nbr = nullptr, *d_segcfg = nullptr, *d_segn = nullptr;
-  int64_t *d_soff = nullptr, *d_tot = nullptr, *d_segslot = nullptr, *d_candoff = nullptr;
-  int64_t *d_nlow = nullptr, *d_prrows = nullptr, *d_proff = nullptr;
-  int32_t *d_cand = nullptr, *d_mk = nullptr;
+  int64_t *d_cnt = nullptr, *d_soff = nullptr, *d_tot = nullptr, *d_candoff = nullptr;
+  int32_t *d_cand = nullptr;
   int64_t *d_gcnt = nullptr, *d_goff = nullptr;
   uint32_t *d_glist = nullptr;
-  uint32_t *d_prm = nullptr;
-  int *d_err = nullptr;
   unsigned long long *d_counter = nullptr;
-  double *d_slabval = nullptr;
   int32_t *d_jslab = nullptr;
   int64_t *d_jstart = nullptr;
   int2 *d_tpairs = nullptr;
   uint32_t *d_dkept = nullptr;
-  cudaEvent_t ev[6] = {};
+  ncand = npairs = 0;
+  nsplit = 0;
   auto cleanup = [&]() {
-    for (auto &e : ev)
-      if (e) cudaEventDestroy(e);
-    psoci_free(d_soff); psoci_free(d_tot); psoci_free(d_segslot); psoci_free(d_counter);
-    psoci_free(d_candoff); psoci_free(d_cand);
-    psoci_free(d_nlow); psoci_free(d_prrows); psoci_free(d_proff); psoci_free(d_mk); psoci_free(d_prm);
-    psoci_free(d_err); psoci_free(d_slabval); psoci_free(d_jslab); psoci_free(d_jstart);
-    psoci_free(d_tpairs); psoci_free(d_dkept);
-    psoci_free(d_gcnt); psoci_free(d_goff); psoci_free(d_glist);
-    psoci_free(d_cnt); psoci_free(d_nbroff); psoci_free(d_nseg); psoci_free(d_nrow); psoci_free(d_segoff);
-    psoci_free(d_rowslot); psoci_free(d_segk0); psoci_free(d_segrow); psoci_free(d_segcnt); psoci_free(d_rownnz);
-    psoci_free(d_nbr); psoci_free(d_segcfg); psoci_free(d_segn);
+    psoci_free(d_cnt); psoci_free(d_soff); psoci_free(d_tot); psoci_free(d_candoff); psoci_free(d_cand);
+    psoci_free(d_gcnt); psoci_free(d_goff); psoci_free(d_glist); psoci_free(d_counter); psoci_free(d_jslab);
+    psoci_free(d_jstart); psoci_free(d_tpairs); psoci_free(d_dkept);
+  };
+  auto fail = [&]() {
+    cleanup();
+    psoci_free(d_nbroff);
+    psoci_free(d_nbr);
   };
 #define TRY(x)                 \
   do {                         \
     s = (x);                   \
     if (s != PSOCI_OK) {       \
-      cleanup();               \
+      fail();                  \
       return s;                \
     }                          \
   } while (0)
@@ -1826,21 +1820,10 @@ psoci_status run_build(psoci_ctx *c, psoci_hmode mode, int64_t *nnz_out) {
     cudaError_t _e = (x);                       \
     if (_e != cudaSuccess) {                    \
       s = psoci_cuda_fail(c, _e, #x);           \
-      cleanup();                                \
+      fail();                                   \
       return s;                                 \
     }                                           \
   } while (0)
-
-  auto tnow = [&]() {
-    if (c->verbose) cudaStreamSynchronize(st);
-    return std::chrono::steady_clock::now();
-  };
-  for (auto &e : ev) TRYC(cudaEventCreate(&e));
-  TRYC(cudaEventRecord(ev[0], st));
-  auto t_a = tnow();
-  // 1. screen
-  int64_t ncand = 0, npairs = 0;
-  int nsplit = 0;
   if (c->join_ok) {
     // by lookup, with the integral pruning fused
     JoinTabs J = {c->join_s, c->join_G, c->join_L, c->d_jgid, c->d_jlid, c->d_jT, c->d_jlnoff, c->d_jln,
@@ -1851,14 +1834,14 @@ psoci_status run_build(psoci_ctx *c, psoci_hmode mode, int64_t *nnz_out) {
     TRY(psoci_alloc(c, &d_goff, G + 1));
     const int gblocks = (int)std::max<int64_t>(1, std::min<int64_t>(((int64_t)G * 32 + 255) / 256, 152 * 32));
     psoci_note_launch();
-    k_group_lists<W, 0><<<gblocks, 256, 0, st>>>(J, c->d_eri, d_gcnt, nullptr);
+    k_group_lists<W, 0><<<gblocks, 256, 0, st>>>(J, prune_eri, d_gcnt, nullptr);
     TRYC(cudaGetLastError());
     int64_t nglist = 0;
     TRY(psoci_scan_i64(c, d_gcnt, d_goff, G, &nglist));
     TRY(psoci_alloc(c, &d_glist, nglist));
     J.goff = d_goff;
     psoci_note_launch();
-    k_group_lists<W, 1><<<gblocks, 256, 0, st>>>(J, c->d_eri, nullptr, d_glist);
+    k_group_lists<W, 1><<<gblocks, 256, 0, st>>>(J, prune_eri, nullptr, d_glist);
     TRYC(cudaGetLastError());
     J.glist = d_glist;
     {
@@ -1871,7 +1854,7 @@ psoci_status run_build(psoci_ctx *c, psoci_hmode mode, int64_t *nnz_out) {
       TRY(psoci_alloc(c, &d_dkept, (nt * nt + 31) / 32));
       TRYC(cudaMemcpyAsync(d_tpairs, pairs.data(), sizeof(int2) * nt, cudaMemcpyHostToDevice, st));
       psoci_note_launch();
-      k_double_kept<<<152 * 8, 256, 0, st>>>(nt, d_tpairs, c->d_eri, d_dkept);
+      k_double_kept<<<152 * 8, 256, 0, st>>>(nt, d_tpairs, prune_eri, d_dkept);
       TRYC(cudaGetLastError());
       TRYC(cudaStreamSynchronize(st));  // pairs is a host buffer
       J.dkept = d_dkept;
@@ -1969,6 +1952,84 @@ psoci_status run_build(psoci_ctx *c, psoci_hmode mode, int64_t *nnz_out) {
   TRYC(cudaGetLastError());
   psoci_free(d_cand);
   }
+  cleanup();
+  return PSOCI_OK;
+#undef TRY
+#undef TRYC
+}
+
+template <int W>
+psoci_status run_build(psoci_ctx *c, psoci_hmode mode, int64_t *nnz_out) {
+  cudaStream_t st = c->stream;
+  const int n = c->nconf;
+  Params P = {};
+  P.nconf = n; P.nbf = c->nbf; P.nelec = c->nelec; P.ksym = c->ksym;
+  P.e1 = c->d_e1; P.e2 = c->d_e2; P.jsym = c->d_jsym; P.nopen = c->d_nopen;
+  P.sefoff = c->d_sefoff; P.detoff = c->d_detoff;
+  P.alpha = c->d_alpha; P.beta = c->d_beta; P.phase = c->d_phase; P.nalpha = c->d_nalpha;
+  P.one = c->d_one; P.eri = c->d_eri;
+
+  psoci_status s;
+  int64_t *d_cnt = nullptr, *d_nbroff = nullptr, *d_nseg = nullptr, *d_nrow = nullptr, *d_segoff = nullptr,
+          *d_rowslot = nullptr, *d_segk0 = nullptr, *d_segrow = nullptr, *d_segcnt = nullptr, *d_rownnz = nullptr;
+  int32_t *d_nbr = nullptr, *d_segcfg = nullptr, *d_segn = nullptr;
+  int64_t *d_soff = nullptr, *d_tot = nullptr, *d_segslot = nullptr, *d_candoff = nullptr;
+  int64_t *d_nlow = nullptr, *d_prrows = nullptr, *d_proff = nullptr;
+  int32_t *d_cand = nullptr, *d_mk = nullptr;
+  int64_t *d_gcnt = nullptr, *d_goff = nullptr;
+  uint32_t *d_glist = nullptr;
+  uint32_t *d_prm = nullptr;
+  int *d_err = nullptr;
+  unsigned long long *d_counter = nullptr;
+  double *d_slabval = nullptr;
+  int32_t *d_jslab = nullptr;
+  int64_t *d_jstart = nullptr;
+  int2 *d_tpairs = nullptr;
+  uint32_t *d_dkept = nullptr;
+  cudaEvent_t ev[6] = {};
+  auto cleanup = [&]() {
+    for (auto &e : ev)
+      if (e) cudaEventDestroy(e);
+    psoci_free(d_soff); psoci_free(d_tot); psoci_free(d_segslot); psoci_free(d_counter);
+    psoci_free(d_candoff); psoci_free(d_cand);
+    psoci_free(d_nlow); psoci_free(d_prrows); psoci_free(d_proff); psoci_free(d_mk); psoci_free(d_prm);
+    psoci_free(d_err); psoci_free(d_slabval); psoci_free(d_jslab); psoci_free(d_jstart);
+    psoci_free(d_tpairs); psoci_free(d_dkept);
+    psoci_free(d_gcnt); psoci_free(d_goff); psoci_free(d_glist);
+    psoci_free(d_cnt); psoci_free(d_nbroff); psoci_free(d_nseg); psoci_free(d_nrow); psoci_free(d_segoff);
+    psoci_free(d_rowslot); psoci_free(d_segk0); psoci_free(d_segrow); psoci_free(d_segcnt); psoci_free(d_rownnz);
+    psoci_free(d_nbr); psoci_free(d_segcfg); psoci_free(d_segn);
+  };
+#define TRY(x)                 \
+  do {                         \
+    s = (x);                   \
+    if (s != PSOCI_OK) {       \
+      cleanup();               \
+      return s;                \
+    }                          \
+  } while (0)
+#define TRYC(x)                                  \
+  do {                                          \
+    cudaError_t _e = (x);                       \
+    if (_e != cudaSuccess) {                    \
+      s = psoci_cuda_fail(c, _e, #x);           \
+      cleanup();                                \
+      return s;                                 \
+    }                                           \
+  } while (0)
+
+  auto tnow = [&]() {
+    if (c->verbose) cudaStreamSynchronize(st);
+    return std::chrono::steady_clock::now();
+  };
+  for (auto &e : ev) TRYC(cudaEventCreate(&e));
+  TRYC(cudaEventRecord(ev[0], st));
+  auto t_a = tnow();
+  // 1. screen
+  int64_t ncand = 0, npairs = 0;
+  int nsplit = 0;
+  TRY(screen_pairs<W>(c, P, c->d_one, c->d_eri, d_nbroff, d_nbr, ncand, npairs, nsplit));
+  P.nbroff = d_nbroff; P.nbr = d_nbr;
   c->ncand = ncand;
   c->npairs = npairs;
   TRYC(cudaEventRecord(ev[1], st));
@@ -2405,6 +2466,7 @@ psoci_status psoci_join_prepare(psoci_ctx *c) {
 }
 
 void psoci_h_release(psoci_ctx *c) {
+  psoci_grad_release(c);
   psoci_free(c->dir_nbroff);
   psoci_free(c->dir_nbr);
   psoci_free(c->dir_segcfg);
@@ -2448,4 +2510,607 @@ psoci_status psoci_h_build(psoci_ctx *c, psoci_hmode mode, int64_t *nnz) {
             (long long)c->nsef_total, (long long)c->nnz, (long long)c->ncand, (long long)c->npairs, (long long)c->nseg,
             c->build_seconds);
   return PSOCI_OK;
+}
+
+// ------------------------------------------------------------------------------------
+// Energy gradient with respect to the integral tables: the adjoint of the element
+// evaluation.  For a CI vector c, E = c^T H c and every element of H is a sum of entries of
+// the packed tables with fixed coefficients (once the reference's zero-prefactor skips are
+// left out), so dE / d table[t] is the transposed evaluation: every coupling of a
+// determinant pair (x of I, y of J) adds its weight w_xy = cd_I[x] cd_J[y] (cd = the vector in
+// the determinant basis, CDC^T's transpose) to the entries its element reads, with the
+// element's sign and coefficient.  dE/d one[pq] is the spin-free 1-RDM (equal irreps) or the
+// spin-orbit density (unequal irreps), dE/d eri[canon(pq,rs)] the 2-RDM in the reference's
+// 8-fold packed layout (Hellmann-Feynman).
+//
+// Work: one warp per row configuration I over its lower neighbours J <= I (pairs J < I
+// count twice, as H_JI = H_IJ^T), 32 pairs set up at a time (a lane each); lanes over the
+// determinant pairs of one configuration pair classify each coupling (det_adj mirrors
+// det_elem's branches) and add its weights to the pair's terms: v0, v1 (double, SO and
+// single prefactors, or the diagonal's Kd[0]) in registers, the exchange terms X[t] /
+// Kd[mm] in a per-warp shared array; the pair's terms are then scattered to the tables.
+// ------------------------------------------------------------------------------------
+namespace {
+
+constexpr int ADJ_WARPS = 4;
+constexpr int ADJ_MAXR = 8;                                        // roots per pass
+constexpr int ADJ_NT = 2 + PSOCI_MAX_OPEN * (PSOCI_MAX_OPEN - 1) / 2;  // v0, v1, X[t] or Kd[mm]
+
+enum { T_NONE = 0, T_V0, T_V1, T_V0MV1, T_SGL, T_X, T_DIAG, T_K, T_DIRECT };
+
+template <int W>
+struct AdjPair {
+  int64_t detA, detB;
+  int A, B, kind;
+  int iex0, iex1, jex0, jex1;
+  int jsA, jsB, nopenA, ndetA, ndetB;
+  uint64_t SA[W];
+  uint64_t bm[6][W];
+};
+
+// The structure of the pair (A, B) in the reference's roles, from the occupations and the
+// symmetries alone: diagonal, same-symmetry single, spin-orbit single, double or none
+// (more than two excitations).
+template <int W>
+__device__ void adj_pair_setup(const Params &P, int A, int B, AdjPair<W> &pi) {
+  pi.A = A; pi.B = B;
+  pi.detA = P.detoff[A]; pi.detB = P.detoff[B];
+  pi.ndetA = (int)(P.detoff[A + 1] - P.detoff[A]);
+  pi.ndetB = (int)(P.detoff[B + 1] - P.detoff[B]);
+  pi.jsA = P.jsym[A]; pi.jsB = P.jsym[B];
+  pi.nopenA = P.nopen[A];
+  uint64_t e1A[W], e2A[W], e1B[W], e2B[W], im1[W], im2[W], jm1[W], jm2[W];
+#pragma unroll
+  for (int w = 0; w < W; ++w) {
+    e1A[w] = P.e1[(int64_t)A * W + w]; e2A[w] = P.e2[(int64_t)A * W + w];
+    e1B[w] = P.e1[(int64_t)B * W + w]; e2B[w] = P.e2[(int64_t)B * W + w];
+    im1[w] = e1A[w] & ~e1B[w]; im2[w] = e2A[w] & ~e2B[w];
+    jm1[w] = e1B[w] & ~e1A[w]; jm2[w] = e2B[w] & ~e2A[w];
+    pi.SA[w] = e1A[w] & ~e2A[w];
+  }
+  pi.iex0 = pi.iex1 = pi.jex0 = pi.jex1 = -1;
+  const int ni = popc_w<W>(im1) + popc_w<W>(im2);
+  const int nj = popc_w<W>(jm1) + popc_w<W>(jm2);
+  if (A == B) { pi.kind = K_DIAG; return; }
+  if (ni == 1 && nj == 1) {
+    uint64_t im[W], jm[W];
+#pragma unroll
+    for (int w = 0; w < W; ++w) { im[w] = im1[w] | im2[w]; jm[w] = jm1[w] | jm2[w]; }
+    const int ie = lowest_bit<W>(im), je = lowest_bit<W>(jm);
+    pi.iex0 = ie; pi.jex0 = je;
+    between_mask<W>(ie, je, pi.bm[0]);
+    range_mask<W>(0, ie - 1, pi.bm[1]);
+    range_mask<W>(je + 1, 64 * W - 1, pi.bm[2]);
+    range_mask<W>(0, je - 1, pi.bm[3]);
+    range_mask<W>(ie + 1, 64 * W - 1, pi.bm[4]);
+    pi.kind = (pi.jsA != pi.jsB) ? K_SO : K_SINGLE;
+    return;
+  }
+  if (ni == 2 && nj == 2) {
+    int ex0 = -1, ex1 = -1, jy0 = -1, jy1 = -1;
+    two_positions<W>(im1, im2, ex0, ex1);
+    two_positions<W>(jm1, jm2, jy0, jy1);
+    pi.iex0 = ex0; pi.iex1 = ex1; pi.jex0 = jy0; pi.jex1 = jy1;
+    between_mask<W>(ex0, jy0, pi.bm[0]);
+    between_mask<W>(ex0, jy1, pi.bm[1]);
+    between_mask<W>(ex1, jy0, pi.bm[2]);
+    between_mask<W>(ex1, jy1, pi.bm[3]);
+    between_mask<W>(ex0, ex1, pi.bm[4]);
+    between_mask<W>(jy0, jy1, pi.bm[5]);
+    pi.kind = K_DOUBLE;
+    return;
+  }
+  pi.kind = K_NONE;
+}
+
+// rank of orbital p among the set bits of S (p must be set in S for a meaningful rank)
+template <int W>
+__device__ __forceinline__ int rank_in(const uint64_t (&S)[W], int p) {
+  int r = 0;
+#pragma unroll
+  for (int w = 0; w < W; ++w) {
+    if (64 * w + 63 < p) r += __popcll(S[w]);
+    else if (64 * w <= p) r += __popcll(S[w] & ((1ull << (p & 63)) - 1ull));
+  }
+  return r;
+}
+
+// det_elem's branches, returning what the element is made of instead of its value:
+// tag T_V0 / T_V1 / T_V0MV1 (+-v0, +-v1, +-(v0 - v1)); T_SGL: +-(v0 - sum of X[t] over the
+// bits of mask); T_X: +-X[term]; T_DIAG: Kd[0] - sum of Kd[mm] over the bits mm of mask;
+// T_K: +-Kd[term]; T_DIRECT: +-eri[direct]; T_NONE: zero.  sgn = +1 / -1.
+template <int W>
+__device__ __forceinline__ int det_adj(const AdjPair<W> &pi, const DetBits<W> &A, const DetBits<W> &B, int &sgn,
+                                       uint64_t &mask, int &term, int64_t &direct) {
+  const uint64_t(&aa)[W] = A.al;
+  const uint64_t(&ba)[W] = A.be;
+  const uint64_t(&ab)[W] = B.al;
+  const uint64_t(&bb)[W] = B.be;
+  const int pha = A.ph, phb = B.ph, naa = A.na, nab = B.na;
+  uint64_t ua[W], ub[W];
+#pragma unroll
+  for (int w = 0; w < W; ++w) { ua[w] = ab[w] & ~aa[w]; ub[w] = bb[w] & ~ba[w]; }
+  const int nmarka = popc_w<W>(ua);
+  const int nmarkb = nmarka + popc_w<W>(ub);
+  const int ie = pi.iex0, je = pi.jex0;
+  sgn = 1;
+  if (pi.kind == K_NONE) return T_NONE;
+  if (pi.kind == K_SO) {
+    if (nmarka > 1 || nmarkb > 1) return T_NONE;
+    int ncount = pha + phb;
+    if (naa < nab) {
+      ncount += popc_and<W>(ba, pi.bm[1]) + popc_and<W>(ab, pi.bm[2]);
+      if ((pi.jsA + pi.jsB) % 2 == 0) ++ncount;
+      else if (pi.jsA % 2 == 1) ++ncount;
+    } else if (naa > nab) {
+      ncount += popc_and<W>(aa, pi.bm[4]) + popc_and<W>(bb, pi.bm[3]);
+      if ((pi.jsA + pi.jsB) % 2 != 0 && (pi.jsA % 2) == 1) ++ncount;
+    } else {
+      if (nmarka == 0) ++ncount;
+      if (pi.jsA % 2 == 1) ++ncount;
+      uint64_t sp[W];
+      sel_w<W>(sp, nmarka != 0, aa, ba);
+      ncount += popc_and<W>(sp, pi.bm[0]);
+    }
+    sgn = (ncount & 1) ? -1 : 1;
+    return T_V0;
+  }
+  if (naa != nab) return T_NONE;
+  if (nmarka > 2 || nmarkb > 2) return T_NONE;
+  if (nmarkb == 0) {
+    if (pi.kind != K_DIAG) return T_NONE;
+    // diag_det_elem: Kd[0] minus Kd[mm] for every pair of open shells with equal spins
+    mask = 0ull;
+    int mm = 0, io = 0;
+#pragma unroll
+    for (int wi = 0; wi < W; ++wi) {
+      uint64_t si_bits = pi.SA[wi];
+      while (si_bits) {
+        const uint64_t lo_i = si_bits & (~si_bits + 1);
+        si_bits ^= lo_i;
+        const bool si = (aa[wi] & lo_i) != 0ull;
+        int jo = 0;
+#pragma unroll
+        for (int wj = 0; wj < W; ++wj) {
+          uint64_t sj = pi.SA[wj];
+          while (sj && jo < io) {
+            const uint64_t lo_j = sj & (~sj + 1);
+            sj ^= lo_j;
+            ++mm;
+            if (si == ((aa[wj] & lo_j) != 0ull)) mask |= 1ull << (mm - 1);
+            ++jo;
+          }
+        }
+        ++io;
+      }
+    }
+    return T_DIAG;
+  }
+  if (nmarkb == 1) {
+    if (pi.kind != K_SINGLE) return T_NONE;
+    uint64_t sp[W];
+    sel_w<W>(sp, nmarka != 0, aa, ba);
+    const int ncount = pha + phb + popc_and<W>(sp, pi.bm[0]);
+    mask = 0ull;
+    int t = 0;
+#pragma unroll
+    for (int w = 0; w < W; ++w) {
+      uint64_t m = sp[w] & ~(aa[w] & ba[w]);
+      if ((ie >> 6) == w) m &= ~(1ull << (ie & 63));
+      if ((je >> 6) == w) m &= ~(1ull << (je & 63));
+      uint64_t sa = pi.SA[w];
+      while (sa) {
+        const uint64_t low = sa & (~sa + 1);
+        if (m & low) mask |= 1ull << t;
+        ++t;
+        sa ^= low;
+      }
+    }
+    sgn = (ncount & 1) ? -1 : 1;
+    return T_SGL;
+  }
+  if (nmarka == 1) {
+    uint64_t xa[W], xb[W];
+#pragma unroll
+    for (int w = 0; w < W; ++w) { xa[w] = aa[w] & ~ab[w]; xb[w] = ba[w] & ~bb[w]; }
+    if (pi.kind == K_DOUBLE) {
+      const int ia = bit_w<W>(xa, pi.iex0) ? 0 : 1, ja = bit_w<W>(ua, pi.jex0) ? 0 : 1;
+      const int ncount = pha + phb + popc_and<W>(aa, pi.bm[2 * ia + ja]) + popc_and<W>(ba, pi.bm[3 - 2 * ia - ja]);
+      sgn = (ncount & 1) ? -1 : 1;
+      return (ia == ja) ? T_V0 : T_V1;
+    }
+    if (pi.kind != K_SINGLE && pi.kind != K_DIAG) return T_NONE;
+    const int iex2 = lowest_bit<W>(ua), jex2 = lowest_bit<W>(ub);
+    const int iex3 = lowest_bit<W>(xa), jex3 = lowest_bit<W>(xb);
+    int ncount = pha + phb;
+    if (abs(iex2 - iex3) > 1) ncount += popc_range<W>(aa, min(iex2, iex3) + 1, max(iex2, iex3) - 1);
+    if (abs(jex2 - jex3) > 1) ncount += popc_range<W>(ba, min(jex2, jex3) + 1, max(jex2, jex3) - 1);
+    sgn = (ncount & 1) ? -1 : 1;
+    direct = canon4(jex2, jex3, iex2, iex3);
+    if (pi.kind == K_SINGLE) {
+      // alpha and beta moves through an open shell p of A: the integral is X[rank of p]
+      const int p = (iex3 == ie || iex3 == je) ? iex2 : iex3;
+      if (bit_w<W>(pi.SA, p) && canon4(ie, p, p, je) == direct) {
+        term = rank_in<W>(pi.SA, p);
+        return T_X;
+      }
+      return T_DIRECT;
+    }
+    // diagonal: a spin exchange between two open shells p and q, the integral Kd[mm(p, q)]
+    const int p = iex3, q = iex2;
+    if (bit_w<W>(pi.SA, p) && bit_w<W>(pi.SA, q) && canon4(p, q, q, p) == direct) {
+      const int rp = rank_in<W>(pi.SA, p), rq = rank_in<W>(pi.SA, q);
+      const int a = max(rp, rq), b = min(rp, rq);
+      term = a * (a - 1) / 2 + b;  // Kd[1 + term] in diag_det_elem's order
+      return T_K;
+    }
+    return T_DIRECT;
+  }
+  if (pi.kind != K_DOUBLE) return T_NONE;
+  uint64_t spb[W], sa[W];
+  sel_w<W>(spb, nmarka == 2, ab, bb);
+  sel_w<W>(sa, nmarka != 0, aa, ba);
+  const int ncount = pha + phb + popc_and<W>(spb, pi.bm[5]) + popc_and<W>(sa, pi.bm[4]);
+  sgn = (ncount & 1) ? -1 : 1;
+  return T_V0MV1;
+}
+
+// vectors (k per pass, root-major with stride ldv, FP64) in the determinant basis:
+// CD[d * k + r], the transpose of ciout's transform (PsociHamiltonian.C:1457-1516)
+__global__ void k_sef_to_det(int nconf, int nelec, int ksym, const int64_t *__restrict__ sefoff,
+                             const int64_t *__restrict__ detoff, const int32_t *__restrict__ jsym,
+                             const int32_t *__restrict__ nopen, const double *__restrict__ V, int64_t ldv, int k,
+                             double *__restrict__ CD) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = (int)(t >> 5), lane = threadIdx.x & 31;
+  if (i >= nconf) return;
+  const int64_t s0 = sefoff[i], d0 = detoff[i];
+  const int nsef = (int)(sefoff[i + 1] - s0);
+  const bool odd = nelec & 1;
+  const bool open = !odd && nopen[i] != 0;
+  const double m = (jsym[i] % 2 != ksym % 2) ? -1.0 : 1.0;
+  const double r = sqrt(0.5);
+  for (int e = lane; e < nsef * k; e += 32) {
+    const int a = e / k, q = e - a * k;
+    const double c = V[(int64_t)q * ldv + s0 + a];
+    if (open) {
+      CD[(d0 + 2 * a) * k + q] = r * c;
+      CD[(d0 + 2 * a + 1) * k + q] = (m * r) * c;
+    } else {
+      CD[(d0 + a) * k + q] = c;
+    }
+  }
+}
+
+template <int W>
+struct AdjSmem {
+  AdjPair<W> pi[32];
+  double acc[ADJ_NT][ADJ_MAXR];
+};
+
+// scatter of one pair's terms into the gradient tables G1 [k][n1], G2 [k][n2] (FP64 atomics);
+// f = 2 for J < I, 1 on the diagonal.  Lanes split the roots and entries.
+template <int W>
+__device__ void adj_scatter(const Params &P, const AdjPair<W> &pi, const double (&acc)[ADJ_NT][ADJ_MAXR], int k,
+                            double f, double *G1, int64_t n1, double *G2, int64_t n2, int lane) {
+  const int A = pi.A;
+  if (pi.kind == K_DOUBLE) {
+    if (lane < k) {
+      atomicAdd(G2 + lane * n2 + canon4(pi.iex0, pi.jex0, pi.iex1, pi.jex1), f * acc[0][lane]);
+      atomicAdd(G2 + lane * n2 + canon4(pi.iex0, pi.jex1, pi.iex1, pi.jex0), f * acc[1][lane]);
+    }
+    return;
+  }
+  if (pi.kind == K_SO) {
+    // v = +-SO(ie, je) / 2, negated when je > ie (processSingleExcitation, PsociHamiltonian.C:223-237)
+    if (lane < k) atomicAdd(G1 + lane * n1 + tri64(pi.iex0, pi.jex0), f * (pi.jex0 > pi.iex0 ? -0.5 : 0.5) * acc[0][lane]);
+    return;
+  }
+  uint64_t e1A[W], e2A[W], e2B[W];
+#pragma unroll
+  for (int w = 0; w < W; ++w) {
+    e1A[w] = P.e1[(int64_t)A * W + w]; e2A[w] = P.e2[(int64_t)A * W + w];
+    e2B[w] = P.e2[(int64_t)pi.B * W + w];
+  }
+  if (pi.kind == K_SINGLE) {
+    const int ie = pi.iex0, je = pi.jex0;
+    // lanes over (root, entry): entry 0 one[ie, je], 1 (ie je|ie ie), 2.. the occupied p,
+    // then the X[t] terms
+    for (int r = 0; r < k; ++r) {
+      const double a0 = f * acc[0][r];
+      if (lane == 0) {
+        atomicAdd(G1 + r * n1 + tri64(ie, je), a0);
+        atomicAdd(G2 + r * n2 + canon4(ie, je, ie, ie), -a0);
+      }
+      // sum over the occupied orbitals p of A: (ie je|p p) x occ_A(p), and -(ie p|p je) where
+      // p is doubly occupied in both
+      int pidx = 0;
+#pragma unroll
+      for (int w = 0; w < W; ++w) {
+        uint64_t o = e1A[w];
+        while (o) {
+          const int p = 64 * w + __ffsll((long long)o) - 1;
+          o &= o - 1;
+          if ((pidx & 31) == lane) {
+            const bool dA = bit_w<W>(e2A, p);
+            atomicAdd(G2 + r * n2 + canon4(ie, je, p, p), dA ? 2.0 * a0 : a0);
+            if (dA && bit_w<W>(e2B, p)) atomicAdd(G2 + r * n2 + canon4(ie, p, p, je), -a0);
+          }
+          ++pidx;
+        }
+      }
+      int t = 0;
+#pragma unroll
+      for (int w = 0; w < W; ++w) {
+        uint64_t sa = pi.SA[w];
+        while (sa) {
+          const int p = 64 * w + __ffsll((long long)sa) - 1;
+          sa &= sa - 1;
+          if ((t & 31) == lane && acc[2 + t][r] != 0.0) atomicAdd(G2 + r * n2 + canon4(ie, p, p, je), f * acc[2 + t][r]);
+          ++t;
+        }
+      }
+    }
+    return;
+  }
+  if (pi.kind == K_DIAG) {
+    // Kd[0] = sum over occupied ib of occ h_ii (+ (ii|ii) if doubly) and over pairs jb < ib of
+    // Coulomb and exchange terms (processDiagExcitation, PsociHamiltonian.C:306-388); lanes
+    // over ib
+    for (int r = 0; r < k; ++r) {
+      const double a0 = f * acc[0][r];
+      int iidx = 0;
+#pragma unroll
+      for (int wi = 0; wi < W; ++wi) {
+        uint64_t oi = e1A[wi];
+        while (oi) {
+          const int ib = 64 * wi + __ffsll((long long)oi) - 1;
+          oi &= oi - 1;
+          if ((iidx & 31) == lane) {
+            const int occi = 1 + (int)bit_w<W>(e2A, ib);
+            if (occi == 1) atomicAdd(G1 + r * n1 + tri64(ib, ib), a0);
+            else {
+              atomicAdd(G1 + r * n1 + tri64(ib, ib), 2.0 * a0);
+              atomicAdd(G2 + r * n2 + canon4(ib, ib, ib, ib), a0);
+            }
+#pragma unroll
+            for (int wj = 0; wj < W; ++wj) {
+              uint64_t oj = e1A[wj];
+              while (oj) {
+                const int jb = 64 * wj + __ffsll((long long)oj) - 1;
+                oj &= oj - 1;
+                if (jb >= ib) break;
+                const int ninj = occi * (1 + (int)bit_w<W>(e2A, jb));
+                if (ninj == 1) atomicAdd(G2 + r * n2 + canon4(ib, ib, jb, jb), a0);
+                else {
+                  const double m = (ninj == 2) ? 1.0 : 2.0;
+                  atomicAdd(G2 + r * n2 + canon4(ib, ib, jb, jb), 2.0 * m * a0);
+                  atomicAdd(G2 + r * n2 + canon4(ib, jb, ib, jb), -m * a0);
+                }
+              }
+            }
+          }
+          ++iidx;
+        }
+      }
+      // Kd[mm] = (s_a s_b|s_b s_a) over the open shells a > b, in that order
+      int sing[PSOCI_MAX_OPEN], ns = 0;
+#pragma unroll
+      for (int w = 0; w < W; ++w) {
+        uint64_t sb = pi.SA[w];
+        while (sb && ns < PSOCI_MAX_OPEN) { sing[ns++] = 64 * w + __ffsll((long long)sb) - 1; sb &= sb - 1; }
+      }
+      int mm = 0;
+      for (int a = 1; a < ns; ++a)
+        for (int b = 0; b < a; ++b, ++mm)
+          if ((mm & 31) == lane && acc[2 + mm][r] != 0.0)
+            atomicAdd(G2 + r * n2 + canon4(sing[a], sing[b], sing[b], sing[a]), f * acc[2 + mm][r]);
+    }
+  }
+}
+
+// One warp per row configuration I (grid-stride); its lower neighbours J <= I in chunks of
+// 32 set up by the lanes, then each pair's determinant couplings spread over the lanes.
+template <int W, typename ACC>
+__global__ void __launch_bounds__(ADJ_WARPS * 32) k_energy_grad(Params P, const int64_t *__restrict__ nbroff,
+                                                                const int32_t *__restrict__ nbr,
+                                                                const double *__restrict__ CD, int k, double *G1,
+                                                                int64_t n1, double *G2, int64_t n2) {
+  __shared__ AdjSmem<W> sm[ADJ_WARPS];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  AdjSmem<W> &S = sm[wib];
+  const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int e = lane; e < ADJ_NT * ADJ_MAXR; e += 32) (&S.acc[0][0])[e] = 0.0;
+  __syncwarp();
+  for (int64_t I = warp; I < P.nconf; I += nwarps) {
+    const int64_t b0 = nbroff[I], b1 = nbroff[I + 1];
+    for (int64_t c0 = b0; c0 < b1; c0 += 32) {
+      // the chunk's pairs (lists are ascending: stop at the first J > I)
+      const int64_t q = c0 + lane;
+      const int J = (q < b1) ? nbr[q] : INT_MAX;
+      const bool lower = J <= (int)I;
+      if (lower) adj_pair_setup<W>(P, (int)I, J, S.pi[lane]);
+      const unsigned lm = __ballot_sync(0xffffffffu, lower);
+      __syncwarp();
+      const int np = __popc(lm);  // lower pairs come first within the chunk
+      for (int u = 0; u < np; ++u) {
+        const AdjPair<W> &pi = S.pi[u];
+        if (pi.kind == K_NONE) continue;
+        ACC a0[ADJ_MAXR], a1[ADJ_MAXR];
+#pragma unroll
+        for (int r = 0; r < ADJ_MAXR; ++r) { a0[r] = 0; a1[r] = 0; }
+        const int nd = pi.ndetA * pi.ndetB;
+        for (int e = lane; e < nd; e += 32) {
+          const int x = e / pi.ndetB, y = e - x * pi.ndetB;
+          DetBits<W> Ad, Bd;
+          load_det<W>(Ad, P.alpha, P.beta, P.phase, P.nalpha, pi.detA + x);
+          load_det<W>(Bd, P.alpha, P.beta, P.phase, P.nalpha, pi.detB + y);
+          int sgn = 1, term = 0;
+          uint64_t mask = 0ull;
+          int64_t direct = 0;
+          const int tag = det_adj<W>(pi, Ad, Bd, sgn, mask, term, direct);
+          if (tag == T_NONE) continue;
+          const double *ca = CD + (pi.detA + x) * k, *cb = CD + (pi.detB + y) * k;
+#pragma unroll
+          for (int r = 0; r < ADJ_MAXR; ++r) {
+            if (r >= k) break;
+            const ACC w = (ACC)(sgn * __ldg(ca + r) * __ldg(cb + r));
+            switch (tag) {
+              case T_V0: a0[r] += w; break;
+              case T_V1: a1[r] += w; break;
+              case T_V0MV1: a0[r] += w; a1[r] -= w; break;
+              case T_SGL:
+              case T_DIAG: {
+                a0[r] += w;
+                uint64_t m = mask;
+                while (m) {
+                  const int t = __ffsll((long long)m) - 1;
+                  m &= m - 1;
+                  atomicAdd(&S.acc[2 + t][r], -(double)w);
+                }
+                break;
+              }
+              case T_X:
+              case T_K: atomicAdd(&S.acc[2 + term][r], (double)w); break;
+              default: {
+                const double fd = (pi.A == pi.B) ? 1.0 : 2.0;
+                atomicAdd(G2 + (int64_t)r * n2 + direct, fd * (double)w);
+              }
+            }
+          }
+        }
+        // pair totals of v0 and v1 (lane 0) into the shared terms
+#pragma unroll
+        for (int r = 0; r < ADJ_MAXR; ++r) {
+          if (r >= k) break;
+          double s0 = (double)a0[r], s1 = (double)a1[r];
+#pragma unroll
+          for (int o = 16; o > 0; o >>= 1) {
+            s0 += __shfl_xor_sync(0xffffffffu, s0, o);
+            s1 += __shfl_xor_sync(0xffffffffu, s1, o);
+          }
+          if (lane == 0) { S.acc[0][r] += s0; S.acc[1][r] += s1; }
+        }
+        __syncwarp();
+        adj_scatter<W>(P, pi, S.acc, k, (pi.A == pi.B) ? 1.0 : 2.0, G1, n1, G2, n2, lane);
+        __syncwarp();
+        for (int e = lane; e < ADJ_NT * ADJ_MAXR; e += 32) (&S.acc[0][0])[e] = 0.0;
+        __syncwarp();
+      }
+      __syncwarp();
+      if (np < 32) break;  // past the diagonal
+    }
+  }
+}
+
+__global__ void k_fill(double *p, int64_t n, double v) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) p[i] = v;
+}
+__global__ void k_nonzero(const double *__restrict__ src, double *__restrict__ dst, int64_t n) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    dst[i] = (src[i] != 0.0) ? 1.0 : 0.0;
+}
+// entries of zero integrals reported as zero (mode: derivatives of the non-zero integrals)
+__global__ void k_mask_zero(const double *__restrict__ tab, int64_t n, int k, double *G) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    if (tab[i] == 0.0)
+      for (int r = 0; r < k; ++r) G[(int64_t)r * n + i] = 0.0;
+}
+
+template <int W>
+psoci_status run_energy_grad(psoci_ctx *c, int k, const double *dV, int64_t ldv, int mode, psoci_prec prec,
+                             double *dG1, double *dG2) {
+  cudaStream_t st = c->stream;
+  const int n = c->nconf;
+  Params P = {};
+  P.nconf = n; P.nbf = c->nbf; P.nelec = c->nelec; P.ksym = c->ksym;
+  P.e1 = c->d_e1; P.e2 = c->d_e2; P.jsym = c->d_jsym; P.nopen = c->d_nopen;
+  P.sefoff = c->d_sefoff; P.detoff = c->d_detoff;
+  P.alpha = c->d_alpha; P.beta = c->d_beta; P.phase = c->d_phase; P.nalpha = c->d_nalpha;
+  P.one = c->d_one; P.eri = c->d_eri;
+  psoci_status s;
+  const int64_t n1 = c->n1, n2 = c->n2;
+  // neighbour lists: every pair within two excitations (mode 0), or those whose integral
+  // prefactors are not all zero (mode 1); kept in the context for later calls
+  if (!c->grad_nbroff || c->grad_mode != mode) {
+    psoci_free(c->grad_nbroff);
+    psoci_free(c->grad_nbr);
+    double *t1 = nullptr, *t2 = nullptr;
+    if ((s = psoci_alloc(c, &t1, n1)) || (s = psoci_alloc(c, &t2, n2))) {
+      psoci_free(t1);
+      psoci_free(t2);
+      return s;
+    }
+    psoci_note_launch();
+    if (mode == 0) k_fill<<<152 * 4, 256, 0, st>>>(t1, n1, 1.0);
+    else k_nonzero<<<152 * 4, 256, 0, st>>>(c->d_one, t1, n1);
+    psoci_note_launch();
+    if (mode == 0) k_fill<<<152 * 8, 256, 0, st>>>(t2, n2, 1.0);
+    else k_nonzero<<<152 * 8, 256, 0, st>>>(c->d_eri, t2, n2);
+    int64_t ncand = 0, npairs = 0;
+    int nsplit = 0;
+    s = screen_pairs<W>(c, P, t1, t2, c->grad_nbroff, c->grad_nbr, ncand, npairs, nsplit);
+    cudaStreamSynchronize(st);
+    psoci_free(t1);
+    psoci_free(t2);
+    if (s) return s;
+    c->grad_mode = mode;
+    c->grad_npairs = npairs;
+  }
+  double *CD = nullptr;
+  if ((s = psoci_alloc(c, &CD, (size_t)c->ndet_total * std::min(k, ADJ_MAXR)))) return s;
+  PSOCI_CUDA(c, cudaMemsetAsync(dG1, 0, sizeof(double) * n1 * k, st));
+  PSOCI_CUDA(c, cudaMemsetAsync(dG2, 0, sizeof(double) * n2 * k, st));
+  const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>(((int64_t)n + ADJ_WARPS - 1) / ADJ_WARPS, 152 * 16));
+  for (int r0 = 0; r0 < k; r0 += ADJ_MAXR) {
+    const int kk = std::min(ADJ_MAXR, k - r0);
+    psoci_note_launch();
+    k_sef_to_det<<<(unsigned)(((int64_t)n * 32 + 255) / 256), 256, 0, st>>>(
+        n, c->nelec, c->ksym, c->d_sefoff, c->d_detoff, c->d_jsym, c->d_nopen, dV + (int64_t)r0 * ldv, ldv, kk, CD);
+    psoci_note_launch();
+    if (prec == PSOCI_PREC_MIXED)
+      k_energy_grad<W, float><<<blocks, ADJ_WARPS * 32, 0, st>>>(P, c->grad_nbroff, c->grad_nbr, CD, kk,
+                                                                 dG1 + r0 * n1, n1, dG2 + r0 * n2, n2);
+    else
+      k_energy_grad<W, double><<<blocks, ADJ_WARPS * 32, 0, st>>>(P, c->grad_nbroff, c->grad_nbr, CD, kk,
+                                                                  dG1 + r0 * n1, n1, dG2 + r0 * n2, n2);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+      psoci_free(CD);
+      return psoci_cuda_fail(c, e, "energy_gradient");
+    }
+  }
+  if (mode == 1) {
+    psoci_note_launch();
+    k_mask_zero<<<152 * 4, 256, 0, st>>>(c->d_one, n1, k, dG1);
+    psoci_note_launch();
+    k_mask_zero<<<152 * 8, 256, 0, st>>>(c->d_eri, n2, k, dG2);
+  }
+  cudaError_t e = cudaStreamSynchronize(st);
+  psoci_free(CD);
+  if (e != cudaSuccess) return psoci_cuda_fail(c, e, "energy_gradient");
+  return PSOCI_OK;
+}
+
+}  // namespace
+
+void psoci_grad_release(psoci_ctx *c) {
+  psoci_free(c->grad_nbroff);
+  psoci_free(c->grad_nbr);
+  c->grad_mode = -1;
+  c->grad_npairs = 0;
+}
+
+psoci_status psoci_energy_grad_run(psoci_ctx *c, int k, const double *dV, int64_t ldv, int mode, psoci_prec prec,
+                                   double *dG1, double *dG2) {
+  if (!c->have_ints) return psoci_fail(c, PSOCI_ERR_STATE, "energy_gradient: no integrals set");
+  if (!c->have_dets) return psoci_fail(c, PSOCI_ERR_STATE, "energy_gradient: determinants not built");
+  if (k < 1 || ldv < c->nsef_total || !dV || !dG1 || !dG2)
+    return psoci_fail(c, PSOCI_ERR_INVALID_ARG, "energy_gradient: bad arguments");
+  if (mode != 0 && mode != 1) return psoci_fail(c, PSOCI_ERR_INVALID_ARG, "energy_gradient: mode must be 0 or 1");
+  if (prec != PSOCI_PREC_FP64 && prec != PSOCI_PREC_MIXED)
+    return psoci_fail(c, PSOCI_ERR_INVALID_ARG, "energy_gradient: precision must be FP64 or MIXED");
+  return (c->words == 1) ? run_energy_grad<1>(c, k, dV, ldv, mode, prec, dG1, dG2)
+                         : run_energy_grad<2>(c, k, dV, ldv, mode, prec, dG1, dG2);
 }

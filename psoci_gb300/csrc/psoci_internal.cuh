@@ -111,6 +111,13 @@ struct psoci_ctx {
   float2 *den_vs = nullptr;      // float-float copy of the roots of one pass
   size_t den_vs_cap = 0;
 
+  // neighbour lists of the energy gradient (hbuild.cu): every pair within two excitations
+  // (grad_mode 0) or those with a non-zero integral prefactor (1)
+  int64_t *grad_nbroff = nullptr;
+  int32_t *grad_nbr = nullptr;
+  int grad_mode = -1;
+  int64_t grad_npairs = 0;
+
   // step-level Davidson basis (psoci_basis_*, davidson.cu)
   struct psoci_dav_basis *basis = nullptr;
 
@@ -205,6 +212,11 @@ void psoci_h_release(psoci_ctx *c);
 void psoci_dets_release(psoci_ctx *c);
 void psoci_density_release(psoci_ctx *c);
 void psoci_basis_release(psoci_ctx *c);
+void psoci_grad_release(psoci_ctx *c);
+// energy gradient with respect to the integral tables (hbuild.cu): device vectors k x ldv
+// root-major, gradients k x n1 and k x n2
+psoci_status psoci_energy_grad_run(psoci_ctx *c, int k, const double *dV, int64_t ldv, int mode, psoci_prec prec,
+                                   double *dG1, double *dG2);
 
 // ------------------------------------------------------------------------------------
 // device helpers

@@ -35,6 +35,11 @@ def tri(i, j):
     return a * (a + 1) // 2 + b
 
 
+def canon_index(i, j, k, l):
+    """0-based position of (ij|kl) in the canonical 8-fold packed two-electron table."""
+    return tri(tri(i, j), tri(k, l))
+
+
 def n_eri(nbf: int) -> int:
     n1 = nbf * (nbf + 1) // 2
     return n1 * (n1 + 1) // 2
