@@ -244,6 +244,14 @@ def run_ours(args):
     den_s = float(np.mean(ts))
     diag = [q * (q + 1) // 2 + q for q in range(p.nbf)]
     den_trace_err = float((Dd[:, diag].sum(1) - p.nelec).abs().max())
+    # energy gradient (1-, 2-particle and spin-orbit densities) of the 8 roots of the last
+    # mixed solve, outside the headline step: mode 1 (the non-zero integrals), FP64 and FP32
+    # pair sums, and mode 0 (every integral, every pair within two excitations) once
+    grad = None
+    if not args.no_grad:
+        rv = ctx.davidson(NROOTS, rtol=RTOL, mixed=True, refine=True, max_subspace=args.max_subspace,
+                          want_vectors=True)
+        grad = energy_gradient_timing(ctx, stream, torch, dev, p, rv, Dd, diag)
     del V, Dd
 
     hbm, peak_kind = peaks()
@@ -337,6 +345,7 @@ def run_ours(args):
                                                          "total_ms")},
             "h_build_counts": {k: int(bs[k]) for k in ("candidates", "pairs", "segments", "nnz", "nnz_lower",
                                                         "slab_slots", "evaluations")},
+            "energy_gradient": grad,
             "density1": {"s": round(den_s, 6), "first_call_s": round(den_first, 6), "roots": NROOTS,
                          "trace_err": den_trace_err, "cpu_estimate": cpu_den,
                          "note": "CIDEN 1-particle density of 8 unit vectors, device pointers, mean of 5 "
@@ -357,6 +366,51 @@ def run_ours(args):
 # Sigma vectors the FP64 block Davidson needed for 8 roots at rtol 1e-5 on GB300 (seed 1,
 # ksym 1); used by the CPU-only reference arm, which has no GPU solve to count them from.
 SIGMA_VECTORS = {"mrcisd_6e8o_v64": 121, "mrcis_6e8o_v40": 137}
+
+
+def energy_gradient_timing(ctx, stream, torch, dev, p, res, dens_unit, diag):
+    """Seconds of psoci_energy_gradient_device for the 8 roots of the solve (device pointers,
+    CUDA events on the library stream; the first call of a mode also forms its neighbour
+    lists), and the check of its spin-free diagonal against the CIDEN occupations."""
+    from psoci_gb300 import api
+
+    N = ctx.nsef
+    n1 = p.nbf * (p.nbf + 1) // 2
+    n2 = n1 * (n1 + 1) // 2
+    k = res.evecs.shape[0] if res.evecs is not None else 0
+    if k == 0:
+        return None
+    V = torch.from_numpy(res.evecs).to(dev)
+    G1 = torch.empty(k, n1, dtype=torch.float64, device=dev)
+    G2 = torch.empty(k, n2, dtype=torch.float64, device=dev)
+    D = torch.empty(k, n1, dtype=torch.float64, device=dev)
+    ctx.density1_device(V.data_ptr(), N, D.data_ptr(), k)
+    out = {"roots": k, "n_one": n1, "n_eri": n2}
+
+    def run(mode, prec):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize(dev)
+        a.record(stream)
+        ctx.energy_gradient_device(V.data_ptr(), N, k, G1.data_ptr(), G2.data_ptr(), nonzero_only=bool(mode),
+                                   prec=prec)
+        b.record(stream)
+        torch.cuda.synchronize(dev)
+        return a.elapsed_time(b) * 1e-3
+
+    first = run(1, api.PREC_FP64)
+    out["nonzero_fp64_s"] = round(run(1, api.PREC_FP64), 4)
+    out["nonzero_first_call_s"] = round(first, 4)
+    g1_64 = G1.clone()
+    out["nonzero_fp32_pairs_s"] = round(run(1, api.PREC_MIXED), 4)
+    out["fp32_pairs_max_rel_diff"] = float(((G1 - g1_64).abs().max() / g1_64.abs().max()).item())
+    out["diag_vs_ciden_occupations"] = float((g1_64[:, diag] - D[:, diag]).abs().max().item())
+    out["all_pairs_first_call_s"] = round(run(0, api.PREC_FP64), 4)
+    out["all_pairs_fp64_s"] = round(run(0, api.PREC_FP64), 4)
+    out["note"] = ("dE/d(one-electron table) and dE/d(8-fold packed two-electron table) of the 8 roots "
+                   "(1-RDM, spin-orbit density, 2-RDM); nonzero: pairs with a non-zero integral prefactor, "
+                   "derivatives of the non-zero integrals; all_pairs: every pair within two excitations")
+    del V, G1, G2, D
+    return out
 
 
 def check_rows(ctx, p, sample):
@@ -538,6 +592,7 @@ def main():
     ap.add_argument("--cpu-rows", type=int, default=8000, help="random row configurations in the CPU build sample")
     ap.add_argument("--cpu-density-rows", type=int, default=48, help="random rows in the CPU density sample")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-grad", action="store_true", help="skip the energy-gradient timing")
     ap.add_argument("--no-parity", action="store_true", help="skip the 8-root check of mrcis_6e8o_v40 vs the oracle")
     ap.add_argument("--verbose", type=int, default=0)
     args = ap.parse_args()

@@ -2909,24 +2909,53 @@ __device__ void adj_scatter(const Params &P, const AdjPair<W> &pi, const double 
   }
 }
 
+// Whether determinants A and B of the pair can couple (det_adj's early exits): a cheap
+// first pass, so that the classification runs on the coupled pairs only.
+template <int W>
+__device__ __forceinline__ bool det_coupled(const AdjPair<W> &pi, const DetBits<W> &A, const DetBits<W> &B) {
+  int na = 0, nb = 0;
+#pragma unroll
+  for (int w = 0; w < W; ++w) { na += __popcll(B.al[w] & ~A.al[w]); nb += __popcll(B.be[w] & ~A.be[w]); }
+  if (pi.kind == K_SO) return na <= 1 && na + nb <= 1;
+  if (A.na != B.na || na + nb > 2) return false;
+  if (na + nb == 0) return pi.kind == K_DIAG;
+  if (na + nb == 1) return pi.kind == K_SINGLE;
+  if (na == 1) return pi.kind != K_NONE;
+  return pi.kind == K_DOUBLE;
+}
+
+constexpr int ADJ_RT = 15;    // exchange terms held in registers (Kd[mm] of <= 6 open shells)
+constexpr int ADJ_CONN = 256; // coupled determinant pairs collected per round
+
 // One warp per row configuration I (grid-stride); its lower neighbours J <= I in chunks of
-// 32 set up by the lanes, then each pair's determinant couplings spread over the lanes.
+// 32 set up by the lanes.  Per pair: (1) lanes test the determinant pairs (x, y) for coupling
+// and collect the coupled ones in shared memory; (2) lanes = (slot, root) classify the
+// collected pairs, slots over the pairs and roots over the lanes of a slot, and add
+// s * cd_I[x] * cd_J[y] to register accumulators of the pair's terms (v0, v1, and the
+// exchange terms X[t] / Kd[mm]; terms beyond ADJ_RT, only on diagonals of 7+ open shells, go
+// to shared-memory atomics); (3) the slots' sums are reduced by shuffles and the root lanes
+// scatter the pair's terms to the tables.  ACC: the accumulator type (FP64, or FP32 sums
+// within a pair).
 template <int W, typename ACC>
 __global__ void __launch_bounds__(ADJ_WARPS * 32) k_energy_grad(Params P, const int64_t *__restrict__ nbroff,
                                                                 const int32_t *__restrict__ nbr,
                                                                 const double *__restrict__ CD, int k, double *G1,
                                                                 int64_t n1, double *G2, int64_t n2) {
   __shared__ AdjSmem<W> sm[ADJ_WARPS];
+  __shared__ uint32_t conn[ADJ_WARPS][ADJ_CONN];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   AdjSmem<W> &S = sm[wib];
   const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  // lanes of one slot hold consecutive roots: kp (a power of two >= k) roots per slot
+  const int kp = (k <= 1) ? 1 : (k <= 2) ? 2 : (k <= 4) ? 4 : 8;
+  const int nslot = 32 / kp, slot = lane / kp, r = lane % kp;
+  const bool rok = r < k;
   for (int e = lane; e < ADJ_NT * ADJ_MAXR; e += 32) (&S.acc[0][0])[e] = 0.0;
   __syncwarp();
   for (int64_t I = warp; I < P.nconf; I += nwarps) {
     const int64_t b0 = nbroff[I], b1 = nbroff[I + 1];
     for (int64_t c0 = b0; c0 < b1; c0 += 32) {
-      // the chunk's pairs (lists are ascending: stop at the first J > I)
       const int64_t q = c0 + lane;
       const int J = (q < b1) ? nbr[q] : INT_MAX;
       const bool lower = J <= (int)I;
@@ -2937,65 +2966,102 @@ __global__ void __launch_bounds__(ADJ_WARPS * 32) k_energy_grad(Params P, const 
       for (int u = 0; u < np; ++u) {
         const AdjPair<W> &pi = S.pi[u];
         if (pi.kind == K_NONE) continue;
-        ACC a0[ADJ_MAXR], a1[ADJ_MAXR];
+        ACC a0 = 0, a1 = 0, aT[ADJ_RT];
 #pragma unroll
-        for (int r = 0; r < ADJ_MAXR; ++r) { a0[r] = 0; a1[r] = 0; }
+        for (int t = 0; t < ADJ_RT; ++t) aT[t] = 0;
+        bool spill = false;  // terms beyond ADJ_RT went to shared memory
         const int nd = pi.ndetA * pi.ndetB;
-        for (int e = lane; e < nd; e += 32) {
-          const int x = e / pi.ndetB, y = e - x * pi.ndetB;
-          DetBits<W> Ad, Bd;
-          load_det<W>(Ad, P.alpha, P.beta, P.phase, P.nalpha, pi.detA + x);
-          load_det<W>(Bd, P.alpha, P.beta, P.phase, P.nalpha, pi.detB + y);
-          int sgn = 1, term = 0;
-          uint64_t mask = 0ull;
-          int64_t direct = 0;
-          const int tag = det_adj<W>(pi, Ad, Bd, sgn, mask, term, direct);
-          if (tag == T_NONE) continue;
-          const double *ca = CD + (pi.detA + x) * k, *cb = CD + (pi.detB + y) * k;
+        for (int e0 = 0; e0 < nd;) {
+          // (1) collect coupled determinant pairs (up to ADJ_CONN per round)
+          int nc = 0;
+          while (e0 < nd && nc + 32 <= ADJ_CONN) {
+            const int e = e0 + lane;
+            bool cp = false;
+            int x = 0, y = 0;
+            if (e < nd) {
+              x = e / pi.ndetB;
+              y = e - x * pi.ndetB;
+              DetBits<W> Ad, Bd;
+              load_det<W>(Ad, P.alpha, P.beta, P.phase, P.nalpha, pi.detA + x);
+              load_det<W>(Bd, P.alpha, P.beta, P.phase, P.nalpha, pi.detB + y);
+              cp = det_coupled<W>(pi, Ad, Bd);
+            }
+            const unsigned cb = __ballot_sync(0xffffffffu, cp);
+            if (cp) conn[wib][nc + __popc(cb & ((1u << lane) - 1u))] = ((uint32_t)x << 16) | (uint32_t)y;
+            nc += __popc(cb);
+            e0 += 32;
+          }
+          __syncwarp();
+          // (2) classify and accumulate, slots over the collected pairs
+          for (int cq = slot; cq < nc; cq += nslot) {
+            const uint32_t xy = conn[wib][cq];
+            const int x = (int)(xy >> 16), y = (int)(xy & 0xffffu);
+            DetBits<W> Ad, Bd;
+            load_det<W>(Ad, P.alpha, P.beta, P.phase, P.nalpha, pi.detA + x);
+            load_det<W>(Bd, P.alpha, P.beta, P.phase, P.nalpha, pi.detB + y);
+            int sgn = 1, term = 0;
+            uint64_t mask = 0ull;
+            int64_t direct = 0;
+            const int tag = det_adj<W>(pi, Ad, Bd, sgn, mask, term, direct);
+            if (tag == T_NONE || !rok) continue;
+            const ACC w = (ACC)(sgn * __ldg(CD + (pi.detA + x) * k + r) * __ldg(CD + (pi.detB + y) * k + r));
+            if (tag == T_V0) a0 += w;
+            else if (tag == T_V1) a1 += w;
+            else if (tag == T_V0MV1) { a0 += w; a1 -= w; }
+            else if (tag == T_SGL || tag == T_DIAG) {
+              a0 += w;
 #pragma unroll
-          for (int r = 0; r < ADJ_MAXR; ++r) {
-            if (r >= k) break;
-            const ACC w = (ACC)(sgn * __ldg(ca + r) * __ldg(cb + r));
-            switch (tag) {
-              case T_V0: a0[r] += w; break;
-              case T_V1: a1[r] += w; break;
-              case T_V0MV1: a0[r] += w; a1[r] -= w; break;
-              case T_SGL:
-              case T_DIAG: {
-                a0[r] += w;
-                uint64_t m = mask;
-                while (m) {
-                  const int t = __ffsll((long long)m) - 1;
-                  m &= m - 1;
-                  atomicAdd(&S.acc[2 + t][r], -(double)w);
-                }
-                break;
+              for (int t = 0; t < ADJ_RT; ++t)
+                if ((mask >> t) & 1ull) aT[t] -= w;
+              uint64_t m = mask >> ADJ_RT;
+              while (m) {
+                const int t = ADJ_RT + __ffsll((long long)m) - 1;
+                m &= m - 1;
+                atomicAdd(&S.acc[2 + t][r], -(double)w);
+                spill = true;
               }
-              case T_X:
-              case T_K: atomicAdd(&S.acc[2 + term][r], (double)w); break;
-              default: {
-                const double fd = (pi.A == pi.B) ? 1.0 : 2.0;
-                atomicAdd(G2 + (int64_t)r * n2 + direct, fd * (double)w);
+            } else if (tag == T_X || tag == T_K) {
+              if (term < ADJ_RT) {
+#pragma unroll
+                for (int t = 0; t < ADJ_RT; ++t)
+                  if (t == term) aT[t] += w;
+              } else {
+                atomicAdd(&S.acc[2 + term][r], (double)w);
+                spill = true;
               }
+            } else {
+              atomicAdd(G2 + (int64_t)r * n2 + direct, ((pi.A == pi.B) ? 1.0 : 2.0) * (double)w);
             }
           }
+          __syncwarp();
         }
-        // pair totals of v0 and v1 (lane 0) into the shared terms
+        // (3) sums over the slots (lanes r, r + kp, r + 2kp, ...): lanes of slot 0 hold them
+        const int nterm = (pi.kind == K_SINGLE) ? pi.nopenA
+                          : (pi.kind == K_DIAG) ? min(ADJ_RT, pi.nopenA * (pi.nopenA - 1) / 2) : 0;
+        double s0 = (double)a0, s1 = (double)a1, sT[ADJ_RT];
 #pragma unroll
-        for (int r = 0; r < ADJ_MAXR; ++r) {
-          if (r >= k) break;
-          double s0 = (double)a0[r], s1 = (double)a1[r];
+        for (int t = 0; t < ADJ_RT; ++t) sT[t] = (double)aT[t];
+        for (int o = kp; o < 32; o <<= 1) {
+          s0 += __shfl_xor_sync(0xffffffffu, s0, o);
+          s1 += __shfl_xor_sync(0xffffffffu, s1, o);
 #pragma unroll
-          for (int o = 16; o > 0; o >>= 1) {
-            s0 += __shfl_xor_sync(0xffffffffu, s0, o);
-            s1 += __shfl_xor_sync(0xffffffffu, s1, o);
-          }
-          if (lane == 0) { S.acc[0][r] += s0; S.acc[1][r] += s1; }
+          for (int t = 0; t < ADJ_RT; ++t)
+            if (t < nterm) sT[t] += __shfl_xor_sync(0xffffffffu, sT[t], o);
+        }
+        (void)spill;
+        __syncwarp();  // the shared-memory terms (spilled atomics) are complete
+        if (lane < k) {
+          S.acc[0][lane] = s0;
+          S.acc[1][lane] = s1;
+#pragma unroll
+          for (int t = 0; t < ADJ_RT; ++t)
+            if (t < nterm) S.acc[2 + t][lane] = sT[t];
         }
         __syncwarp();
         adj_scatter<W>(P, pi, S.acc, k, (pi.A == pi.B) ? 1.0 : 2.0, G1, n1, G2, n2, lane);
         __syncwarp();
-        for (int e = lane; e < ADJ_NT * ADJ_MAXR; e += 32) (&S.acc[0][0])[e] = 0.0;
+        const int used = 2 + ((pi.kind == K_DIAG) ? pi.nopenA * (pi.nopenA - 1) / 2 : pi.nopenA);
+        for (int e = lane; e < used * ADJ_MAXR; e += 32) (&S.acc[0][0])[e] = 0.0;
         __syncwarp();
       }
       __syncwarp();

@@ -96,7 +96,9 @@ def test_one_particle_part_is_ciden_density(oracle_mod, name, ksym):
 
 def test_gradcheck_fci_6e12o():
     """torch.autograd.gradcheck of the lowest 4 eigenvalues of the 33,814-SEF full-CI block
-    with respect to both tables (central differences, step 1e-5), plus central differences of
+    with respect to both tables (central differences, step 1e-5; the gradient's sums over
+    configuration pairs are FP64 atomics, so repeated backward passes may differ in the last
+    bits: nondet_tol 1e-10), plus central differences of
     single entries: a diagonal h, an off-diagonal h, a spin-orbit value, a Coulomb, an exchange
     and a symmetry-forbidden (zero) two-electron integral."""
     torch = pytest.importorskip("torch")
@@ -108,7 +110,7 @@ def test_gradcheck_fci_6e12o():
     one = torch.tensor(p.one_packed(), dtype=torch.float64, requires_grad=True)
     eri = torch.tensor(p.eri, dtype=torch.float64, requires_grad=True)
     assert torch.autograd.gradcheck(lambda a, b: EnergyFunction.apply(a, b, S), (one, eri), eps=1e-5, atol=1e-6,
-                                    rtol=1e-4, fast_mode=True)
+                                    rtol=1e-4, fast_mode=True, nondet_tol=1e-10)
     e0, v0 = S.solve(p.one_packed(), p.eri)
     g1, g2 = S.gradient(v0)
     irr = p.irreps
