@@ -202,6 +202,37 @@ class Oracle(_Base):
         return y
 
 
+def sigma_lower_rows(rp, ci, va, x, nthreads=0):
+    """y = H x for one vector from lower storage, rows over threads (the timed CPU sigma)."""
+    lib = ctypes.CDLL(ORACLE_SO)
+    f = lib.orc_sigma_lower_rows
+    f.restype = None
+    f.argtypes = [ctypes.c_long, _c_long_p, _c_int_p, _c_dbl_p, _c_dbl_p, _c_dbl_p, ctypes.c_int]
+    x = np.ascontiguousarray(x, np.float64)
+    y = np.zeros_like(x)
+    f(len(rp) - 1, _p(rp, _c_long_p), _p(ci, _c_int_p), _p(va, _c_dbl_p), _p(x, _c_dbl_p), _p(y, _c_dbl_p),
+      nthreads or os.cpu_count() or 1)
+    return y
+
+
+def davidson_ref(rp, ci, va, diag, nroots, rtol, maxsub=0, max_iter=1000, nthreads=0):
+    """The reference's Davidson loop on the CPU (see psoci_oracle.c): returns (evals, rnorms,
+    {"iterations", "sigma_vectors", "collapses"}, converged)."""
+    lib = ctypes.CDLL(ORACLE_SO)
+    f = lib.orc_davidson_ref
+    f.restype = ctypes.c_int
+    f.argtypes = [ctypes.c_long, _c_long_p, _c_int_p, _c_dbl_p, _c_dbl_p, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                  ctypes.c_int, ctypes.c_int, _c_dbl_p, _c_dbl_p, _c_long_p]
+    ev = np.zeros(nroots)
+    rn = np.zeros(nroots)
+    st = np.zeros(3, np.int64)
+    d = np.ascontiguousarray(diag, np.float64)
+    rc = f(len(rp) - 1, _p(rp, _c_long_p), _p(ci, _c_int_p), _p(va, _c_dbl_p), _p(d, _c_dbl_p), nroots,
+           maxsub or 4 * nroots, rtol, max_iter, nthreads or os.cpu_count() or 1, _p(ev, _c_dbl_p), _p(rn, _c_dbl_p),
+           _p(st, _c_long_p))
+    return ev, rn, {"iterations": int(st[0]), "sigma_vectors": int(st[1]), "collapses": int(st[2])}, rc == 0
+
+
 class Reference(_Base):
     """The reference's own compute sources (compiled unchanged), via oracle/ref_harness.cpp.
     Process-global state: one problem at a time."""

@@ -931,3 +931,249 @@ void orc_energy_gradient(const orc_ctx *c, int k, const double *vecs, int nonzer
   for (int t = 0; t < nthreads; ++t) pthread_join(th[t], NULL);
   free(th); free(args);
 }
+
+/* ---------------------------------------------------------------------------
+ * The reference's CPU Davidson, restated for the timed CPU baseline.
+ *
+ * sigma: y = H x for one vector from the lower triangle, rows split over threads as the
+ * reference splits them over MPI ranks (matrixVectorProductsSplitChunkMultipleJchunks,
+ * PsociGAhamiltonian.C:6921-7270): y_i += H_ij x_j and y_j += H_ij x_i (j < i) into a
+ * private y per thread, then summed (the reference's MPI_Allreduce).
+ *
+ * loop: driver.PSOCI.splittest.C:1050-1311 with the production flags (INCREMENTAL,
+ * NEWRNOMRS, DIAGGOP, MODIFIED_EXPAND): unit-vector guess on the first nroots SEFs
+ * (PsociGAvectors.C:687-726); per iteration the new column of G = V^T H V, the subspace
+ * eigen-solve, residual norms from root curroot on until one exceeds the tolerance, a
+ * preconditioned residual t_i = r_i / (D_i - lambda) where |D_i - lambda| > 1e-3
+ * (PsociGAbasis.C:1860-1919), one modified Gram-Schmidt pass and normalisation
+ * (:1371-1474), its H*v; tolerance 1e-3 first, then rtol; collapse to 2 nroots Ritz vectors
+ * (V and HV, no recompute, :483-583) when the basis exceeds maxsub.  The subspace solve is a
+ * cyclic Jacobi (the basis is orthonormal, so dsygv's metric is the identity).
+ * ------------------------------------------------------------------------- */
+typedef struct {
+  long n; const long *rp; const int *ci; const double *v; const double *x; double *y; long r0, r1;
+} sigr_arg;
+
+static void *sigr_worker(void *p) {
+  sigr_arg *a = (sigr_arg *)p;
+  memset(a->y, 0, sizeof(double) * a->n);
+  for (long i = a->r0; i < a->r1; ++i) {
+    double s = 0.0;
+    const double xi = a->x[i];
+    for (long e = a->rp[i]; e < a->rp[i + 1]; ++e) {
+      const int j = a->ci[e];
+      const double h = a->v[e];
+      s += h * a->x[j];
+      if (j != i) a->y[j] += h * xi;
+    }
+    a->y[i] += s;
+  }
+  return NULL;
+}
+
+typedef struct {
+  long n, nrows;
+  const long *rp; const int *ci; const double *v;
+  int nthreads;
+  double *ybuf;  /* nthreads x n */
+  long *cut;     /* nthreads + 1 row boundaries, balanced by stored elements */
+} sigr_plan;
+
+static void sigr_apply(const sigr_plan *P, const double *x, double *y) {
+  pthread_t th[256];
+  sigr_arg args[256];
+  for (int t = 0; t < P->nthreads; ++t) {
+    args[t].n = P->n; args[t].rp = P->rp; args[t].ci = P->ci; args[t].v = P->v; args[t].x = x;
+    args[t].y = P->ybuf + (size_t)t * P->n; args[t].r0 = P->cut[t]; args[t].r1 = P->cut[t + 1];
+    pthread_create(&th[t], NULL, sigr_worker, &args[t]);
+  }
+  for (int t = 0; t < P->nthreads; ++t) pthread_join(th[t], NULL);
+  for (long i = 0; i < P->n; ++i) {
+    double s = 0.0;
+    for (int t = 0; t < P->nthreads; ++t) s += P->ybuf[(size_t)t * P->n + i];
+    y[i] = s;
+  }
+}
+
+static void sigr_init(sigr_plan *P, long n, const long *rp, const int *ci, const double *v, int nthreads) {
+  if (nthreads < 1) nthreads = 1;
+  if (nthreads > 256) nthreads = 256;
+  P->n = n; P->rp = rp; P->ci = ci; P->v = v; P->nthreads = nthreads;
+  P->ybuf = (double *)malloc(sizeof(double) * (size_t)nthreads * n);
+  P->cut = (long *)malloc(sizeof(long) * (nthreads + 1));
+  long nnz = rp[n], r = 0;
+  P->cut[0] = 0;
+  for (int t = 1; t < nthreads; ++t) {
+    long target = nnz * t / nthreads;
+    while (r < n && rp[r] < target) ++r;
+    P->cut[t] = r;
+  }
+  P->cut[nthreads] = n;
+}
+
+/* y = H x for one vector, rows over threads (the timed CPU sigma) */
+void orc_sigma_lower_rows(long n, const long *rowptr, const int *cols, const double *vals, const double *x,
+                          double *y, int nthreads) {
+  sigr_plan P;
+  sigr_init(&P, n, rowptr, cols, vals, nthreads);
+  sigr_apply(&P, x, y);
+  free(P.ybuf); free(P.cut);
+}
+
+/* cyclic Jacobi eigen-solve of a symmetric m x m matrix (row-major, destroyed); w ascending,
+ * Y column c = eigenvector c (row-major m x m) */
+static void jacobi_eig(int m, double *A, double *w, double *Y) {
+  for (int i = 0; i < m; ++i)
+    for (int j = 0; j < m; ++j) Y[i * m + j] = (i == j) ? 1.0 : 0.0;
+  for (int sweep = 0; sweep < 100; ++sweep) {
+    double off = 0.0, tot = 0.0;
+    for (int i = 0; i < m; ++i)
+      for (int j = 0; j < m; ++j) { tot += A[i * m + j] * A[i * m + j]; if (i != j) off += A[i * m + j] * A[i * m + j]; }
+    if (off <= 1e-30 * tot) break;
+    for (int p = 0; p < m - 1; ++p)
+      for (int q = p + 1; q < m; ++q) {
+        double apq = A[p * m + q];
+        if (fabs(apq) < 1e-300) continue;
+        double app = A[p * m + p], aqq = A[q * m + q];
+        double th = (aqq - app) / (2.0 * apq);
+        double t = (th >= 0 ? 1.0 : -1.0) / (fabs(th) + sqrt(th * th + 1.0));
+        double cs = 1.0 / sqrt(t * t + 1.0), sn = t * cs;
+        for (int k = 0; k < m; ++k) {
+          double akp = A[k * m + p], akq = A[k * m + q];
+          A[k * m + p] = cs * akp - sn * akq;
+          A[k * m + q] = sn * akp + cs * akq;
+        }
+        for (int k = 0; k < m; ++k) {
+          double apk = A[p * m + k], aqk = A[q * m + k];
+          A[p * m + k] = cs * apk - sn * aqk;
+          A[q * m + k] = sn * apk + cs * aqk;
+        }
+        for (int k = 0; k < m; ++k) {
+          double ykp = Y[k * m + p], ykq = Y[k * m + q];
+          Y[k * m + p] = cs * ykp - sn * ykq;
+          Y[k * m + q] = sn * ykp + cs * ykq;
+        }
+      }
+  }
+  /* sort ascending */
+  int idx[128];
+  for (int i = 0; i < m; ++i) { idx[i] = i; w[i] = A[i * m + i]; }
+  for (int i = 1; i < m; ++i)
+    for (int j = i; j > 0 && w[idx[j]] < w[idx[j - 1]]; --j) { int t = idx[j]; idx[j] = idx[j - 1]; idx[j - 1] = t; }
+  double wt[128], Yt[128 * 128];
+  for (int i = 0; i < m; ++i) wt[i] = w[idx[i]];
+  for (int i = 0; i < m; ++i)
+    for (int c = 0; c < m; ++c) Yt[i * m + c] = Y[i * m + idx[c]];
+  memcpy(w, wt, sizeof(double) * m);
+  memcpy(Y, Yt, sizeof(double) * m * m);
+}
+
+/* Returns 0 when converged, 1 at the iteration limit.  stats[0] iterations, [1] sigma
+ * vectors, [2] collapses. */
+int orc_davidson_ref(long n, const long *rowptr, const int *cols, const double *vals, const double *diag,
+                     int nroots, int maxsub, double rtol, int max_iter, int nthreads, double *evals, double *rnorms,
+                     long *stats) {
+  if (maxsub > 127) maxsub = 127;
+  const int ld = maxsub + 1;
+  double *V = (double *)calloc((size_t)n * ld, sizeof(double));   /* vector c at c*n */
+  double *HV = (double *)calloc((size_t)n * ld, sizeof(double));
+  double *G = (double *)calloc((size_t)ld * ld, sizeof(double));
+  double *A = (double *)malloc(sizeof(double) * ld * ld), *Y = (double *)malloc(sizeof(double) * ld * ld);
+  double *w = (double *)malloc(sizeof(double) * ld);
+  double *r = (double *)malloc(sizeof(double) * n), *t = (double *)malloc(sizeof(double) * n);
+  double *xr = (double *)malloc(sizeof(double) * n), *tmp = (double *)malloc(sizeof(double) * (size_t)n * 2 * nroots);
+  sigr_plan P;
+  sigr_init(&P, n, rowptr, cols, vals, nthreads);
+  long nsig = 0, collapses = 0, total = 0;
+  int m = nroots;
+  for (int c = 0; c < nroots; ++c) V[(size_t)c * n + c] = 1.0;
+  for (int c = 0; c < nroots; ++c) { sigr_apply(&P, V + (size_t)c * n, HV + (size_t)c * n); ++nsig; }
+  int nupd = m, curroot = 1, converged = 0, count = 0, eig_m = 0;
+  const double coarse = 1e-3;
+  double cur_rtol = coarse;
+  for (int i = 0; i < nroots; ++i) rnorms[i] = -1.0;
+  while (count < max_iter && !converged) {
+    ++total; ++count;
+    /* generateIncrementalSubspace(nupd) */
+    for (int j = m - nupd; j < m; ++j)
+      for (int i = 0; i < m; ++i) {
+        double s = 0.0;
+        const double *vi = V + (size_t)i * n, *hj = HV + (size_t)j * n;
+        for (long q = 0; q < n; ++q) s += vi[q] * hj[q];
+        G[i * ld + j] = s;
+        G[j * ld + i] = s;
+      }
+    /* diagSubspaceGOP */
+    for (int i = 0; i < m; ++i)
+      for (int j = 0; j < m; ++j) A[i * m + j] = 0.5 * (G[i * ld + j] + G[j * ld + i]);
+    jacobi_eig(m, A, w, Y);
+    eig_m = m;
+    converged = 1;
+    for (int it = curroot; it <= nroots; ++it) {
+      /* computeRnormSingle */
+      const int c = it - 1;
+      double nr = 0.0;
+      for (long q = 0; q < n; ++q) {
+        double hx = 0.0, xx = 0.0;
+        for (int s = 0; s < m; ++s) { hx += HV[(size_t)s * n + q] * Y[s * m + c]; xx += V[(size_t)s * n + q] * Y[s * m + c]; }
+        r[q] = hx - w[c] * xx;
+        nr += r[q] * r[q];
+      }
+      nr = sqrt(nr);
+      rnorms[c] = nr;
+      if (nr > cur_rtol) { converged = 0; curroot = it; break; }
+    }
+    if (!converged) {
+      /* preconditionAndNewVectorIncore + appendScratchVector */
+      const double shift = w[curroot - 1];
+      for (long q = 0; q < n; ++q) {
+        double d = diag[q] - shift;
+        t[q] = (fabs(d) > 1e-3) ? r[q] / d : r[q];
+      }
+      for (int s = 0; s < m; ++s) {
+        const double *vs = V + (size_t)s * n;
+        double dot = 0.0;
+        for (long q = 0; q < n; ++q) dot += vs[q] * t[q];
+        for (long q = 0; q < n; ++q) t[q] -= dot * vs[q];
+      }
+      double nt = 0.0;
+      for (long q = 0; q < n; ++q) nt += t[q] * t[q];
+      nt = sqrt(nt);
+      if (nt > 0.0) {
+        for (long q = 0; q < n; ++q) V[(size_t)m * n + q] = t[q] / nt;
+        sigr_apply(&P, V + (size_t)m * n, HV + (size_t)m * n);
+        ++nsig;
+        ++m;
+      }
+      nupd = 1;
+    }
+    int collapse_to = 0;
+    if (converged && cur_rtol == coarse) {
+      converged = 0; count = 0; cur_rtol = rtol; curroot = 1;
+      if (m >= 2 * nroots) collapse_to = 2 * nroots;
+      nupd = m;
+    }
+    if (m > maxsub) collapse_to = 2 * nroots;
+    if (collapse_to) {
+      /* expandAndReplaceVectorsNew over the basis of the last eigen-solve */
+      for (int pass = 0; pass < 2; ++pass) {
+        double *B = pass == 0 ? V : HV;
+        for (int c = 0; c < collapse_to; ++c)
+          for (long q = 0; q < n; ++q) {
+            double s = 0.0;
+            for (int k2 = 0; k2 < eig_m; ++k2) s += B[(size_t)k2 * n + q] * Y[k2 * eig_m + c];
+            tmp[(size_t)c * n + q] = s;
+          }
+        memcpy(B, tmp, sizeof(double) * (size_t)n * collapse_to);
+      }
+      m = collapse_to;
+      nupd = m;
+      ++collapses;
+    }
+  }
+  for (int i = 0; i < nroots; ++i) evals[i] = w[i];
+  stats[0] = total; stats[1] = nsig; stats[2] = collapses;
+  free(V); free(HV); free(G); free(A); free(Y); free(w); free(r); free(t); free(xr); free(tmp);
+  free(P.ybuf); free(P.cut);
+  return converged ? 0 : 1;
+}

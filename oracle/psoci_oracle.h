@@ -36,6 +36,12 @@ void orc_sigma_lower(long n, const long *rowptr, const int *cols, const double *
  * (vecs: k x N root-major; dens: k x nbf(nbf+1)/2). */
 int orc_ciden_block(const orc_ctx *c, int i, int j, double *out);
 void orc_density1(const orc_ctx *c, int k, const double *vecs, double *dens);
+/* the reference's CPU sigma (one vector, rows over threads) and Davidson loop (see .c) */
+void orc_sigma_lower_rows(long n, const long *rowptr, const int *cols, const double *vals, const double *x,
+                          double *y, int nthreads);
+int orc_davidson_ref(long n, const long *rowptr, const int *cols, const double *vals, const double *diag,
+                     int nroots, int maxsub, double rtol, int max_iter, int nthreads, double *evals, double *rnorms,
+                     long *stats);
 /* energy gradients with respect to the packed tables (see psoci_oracle.c) */
 void orc_energy_gradient(const orc_ctx *c, int k, const double *vecs, int nonzero_only, double *grad_one,
                          double *grad_eri, int nthreads);

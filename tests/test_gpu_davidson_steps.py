@@ -42,7 +42,8 @@ def reference_loop(S, nroots, maxsub, rtol, max_iter=400):
     ev_p = evals.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
     r = ctypes.c_double()
     coarse, cur_rtol, curroot, count, converged, nupd = 1e-3, 1e-3, 1, 0, False, nroots
-    total = 0
+    total, nsig = 0, nroots
+    nap = ctypes.c_int()
     while count < max_iter and not converged:
         count += 1
         total += 1
@@ -57,7 +58,8 @@ def reference_loop(S, nroots, maxsub, rtol, max_iter=400):
             itest += 1
         if not converged:
             S.ok("basis_precondition_new", curroot, evals[curroot - 1], 1e-3)
-            S.ok("basis_append_scratch", 0, None)
+            S.ok("basis_append_scratch", 0, ctypes.byref(nap))
+            nsig += nap.value
             nupd = 1
         if converged and cur_rtol == coarse:
             converged, count, cur_rtol, curroot = False, 0, rtol, 1
@@ -73,7 +75,7 @@ def reference_loop(S, nroots, maxsub, rtol, max_iter=400):
     S.ok("basis_expand_replace", S.existing())
     vecs = np.zeros((nroots, S.c.nsef))
     S.ok("basis_vectors", nroots, vecs.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
-    return evals[:nroots].copy(), rn, vecs, total
+    return evals[:nroots].copy(), rn, vecs, total, nsig
 
 
 @pytest.mark.parametrize("name,ksym", [("fci_6e8o", 1), ("fci_5e6o", 2)])
@@ -86,7 +88,8 @@ def test_reference_loop_matches_solve(oracle_mod, name, ksym):
     c = gpu_context(p)
     c.build_hamiltonian(mixed=True)
     S = Steps(c)
-    ev, rn, vecs, iters = reference_loop(S, 4, 16, 1e-8)
+    ev, rn, vecs, iters, nsig = reference_loop(S, 4, 16, 1e-8)
+    assert nsig >= iters
     assert np.abs(ev - ref).max() <= 1e-10
     assert (rn <= 1e-8).all()
     fast = c.davidson(4, rtol=1e-8, mixed=False)
