@@ -293,17 +293,17 @@ def run_ours(args):
     cpu_den = None
     row_check = None
     parity_cfg1 = None
+    measured_cfg1 = None
     if rank == 0 and not args.no_cpu:
+        measured_cfg1 = measured_comparison("mrcis_6e8o_v40", args.seed, args.ksym, local)
         sample = {}
-        cpu = cpu_estimate(p, args.cpu_rows, args.cpu_sample, REF_LOOP_SIGMA_VECTORS.get(args.workload), keep=sample)
+        cpu = cpu_estimate(p, args.cpu_rows, args.cpu_sample, REF_LOOP.get(args.workload), keep=sample,
+                           calib=measured_cfg1["cpu"])
         cpu["nnz_full_measured"] = int(nnz)
         row_check = check_rows(ctx, p, sample)
         cpu_den = cpu_density_estimate(p, args.cpu_density_rows)
     if rank == 0 and not args.no_parity:
         parity_cfg1 = roots_vs_oracle("mrcis_6e8o_v40", NROOTS, args.seed, args.ksym, local)
-    measured_cfg1 = None
-    if rank == 0 and not args.no_cpu:
-        measured_cfg1 = measured_comparison("mrcis_6e8o_v40", args.seed, args.ksym, local)
 
     if rank == 0:
         clocks = clk.summary()
@@ -367,14 +367,15 @@ def run_ours(args):
     ctx.close()
 
 
-# Sigma vectors the reference's own Davidson loop needs for 8 roots of these blocks (seed 1,
-# ksym 1, residual 1e-5): one new vector per iteration for the first unconverged root, coarse
-# tolerance 1e-3 first, collapse from 32 to 16 vectors, unit-vector guess on the first 8 SEFs
-# (driver.PSOCI.splittest.C:1050-1311).  mrcis_6e8o_v40: counted by the oracle's CPU loop
-# (measured_reference_run); mrcisd_6e8o_v64: counted by the same loop run on the GPU through
-# the library's step-level Davidson entry points with FP64 products (a one-off run; too long
-# for the CPU).
-REF_LOOP_SIGMA_VECTORS = {"mrcisd_6e8o_v64": None, "mrcis_6e8o_v40": 173}
+# Iterations and sigma vectors of the reference's own Davidson loop for 8 roots of these
+# blocks (seed 1, ksym 1, residual 1e-5): one new vector per iteration for the first
+# unconverged root, coarse tolerance 1e-3 first, collapse from 32 to 16 vectors, unit-vector
+# guess on the first 8 SEFs (driver.PSOCI.splittest.C:1050-1311).  mrcis_6e8o_v40: counted
+# by the oracle's CPU loop (measured_reference_run); mrcisd_6e8o_v64: counted by the same loop
+# run on a GB300 through the library's step-level Davidson entry points with FP64 products
+# (4.9 s there; too long for the CPU).
+REF_LOOP = {"mrcisd_6e8o_v64": {"iterations": 133, "sigma_vectors": 139},
+            "mrcis_6e8o_v40": {"iterations": 167, "sigma_vectors": 173}}
 
 
 def energy_gradient_timing(ctx, stream, torch, dev, p, res, dens_unit, diag):
@@ -477,7 +478,7 @@ def roots_vs_oracle(workload, nroots, seed, ksym, device):
     return out
 
 
-def cpu_estimate(p, rows_sample, sigma_sample, sigma_vectors, seed=0, keep=None):
+def cpu_estimate(p, rows_sample, sigma_sample, loop, seed=0, keep=None, calib=None):
     """Seconds the oracle (C restatement of the reference's build, sigma and Davidson, all host
     threads) needs for the full solve, extrapolated from bounded samples:
 
@@ -487,8 +488,10 @@ def cpu_estimate(p, rows_sample, sigma_sample, sigma_vectors, seed=0, keep=None)
     * sigma: one vector through the reference's lower-triangle product with rows split over
       all host threads and the partial results summed (the reference's MPI_Allreduce), timed
       on the matrix of the first ``sigma_sample`` configurations and scaled by stored
-      elements, times ``sigma_vectors`` (the reference loop's count for this block).
-    The Davidson's vector operations are not counted, so the estimate favours the CPU.
+      elements, times the reference loop's sigma-vector count for this block (``loop``);
+    * the Davidson's vector operations (subspace columns, residuals, Gram-Schmidt, collapses):
+      their measured seconds per iteration and per SEF on a block run in full (``calib``, from
+      measured_reference_run) times this block's SEFs and the loop's iteration count.
     """
     import oracle
 
@@ -519,15 +522,22 @@ def cpu_estimate(p, rows_sample, sigma_sample, sigma_vectors, seed=0, keep=None)
         oracle.sigma_lower_rows(rp, ci, va, x, cores)
     t_sample = (time.perf_counter() - t0) / reps
     t_sigma = t_sample * nnz_lower / max(len(ci), 1)
-    sv = sigma_vectors if sigma_vectors else 20 * NROOTS
-    total = t_build + sv * t_sigma
+    loop = loop or {"iterations": 20 * NROOTS, "sigma_vectors": 20 * NROOTS}
+    sv, iters = loop["sigma_vectors"], loop["iterations"]
+    t_vec = 0.0
+    if calib:
+        per = max(calib["davidson_s"] - calib["sigma_vectors"] * calib["sigma_s_per_vector"], 0.0)
+        t_vec = per / (calib["iterations"] * calib["nsef"]) * p.num_sefs() * iters
+    total = t_build + sv * t_sigma + t_vec
     return {"value": round(total, 3), "unit": "s", "cores": cores, "kind": "port", "extrapolated": True,
             "sample": f"oracle H build of {ns} random row configurations of {p.nconf} ({ns / p.nconf:.2%}, {cores} "
                       f"threads, {t_rows:.2f} s, scaled x{scale:.1f}); one-vector lower-triangle sigma ({cores} threads) "
                       f"on the first {S.p.nconf} configurations ({len(ci)} stored elements, {t_sample * 1e3:.1f} ms), "
                       f"scaled to {nnz_lower:.3e} estimated stored elements, x {sv} sigma vectors of the reference "
-                      f"loop; vector operations not counted",
+                      f"loop; vector operations {t_vec:.1f} s ({iters} iterations, per SEF and iteration as measured "
+                      f"on the {calib['nsef'] if calib else 0}-SEF block run in full)",
             "h_build_s": round(t_build, 3), "sigma_s_per_vector": round(t_sigma, 4), "sigma_vectors": sv,
+            "davidson_vector_ops_s": round(t_vec, 3), "iterations": iters,
             "nnz_full_estimated": int(2 * nnz_lower - p.num_sefs()),
             "sample_seconds": round(t_rows + reps * t_sample, 3)}
 
@@ -547,10 +557,15 @@ def measured_reference_run(p, nroots, rtol):
     t1 = time.perf_counter()
     ev, rn, st, ok = oracle.davidson_ref(rp, ci, va, d, nroots, rtol, nthreads=cores)
     t2 = time.perf_counter()
+    x = np.random.default_rng(0).standard_normal(len(rp) - 1)
+    t3 = time.perf_counter()
+    for _ in range(5):
+        oracle.sigma_lower_rows(rp, ci, va, x, cores)
+    t_sig = (time.perf_counter() - t3) / 5
     return {"value": round(t2 - t0, 3), "unit": "s", "cores": cores, "kind": "port", "extrapolated": False,
             "nsef": int(len(rp) - 1), "nnz_lower": int(len(ci)), "h_build_s": round(t1 - t0, 3),
-            "davidson_s": round(t2 - t1, 3), "converged": bool(ok), "evals": [float(x) for x in ev],
-            "max_rnorm": float(rn.max()), **st}
+            "davidson_s": round(t2 - t1, 3), "sigma_s_per_vector": round(t_sig, 5), "converged": bool(ok),
+            "evals": [float(x) for x in ev], "max_rnorm": float(rn.max()), **st}
 
 
 def measured_comparison(workload, seed, ksym, device):
@@ -617,14 +632,15 @@ def run_reference(args):
 
     p = named_workload(args.workload, seed=args.seed, ksym=args.ksym)
     N = p.num_sefs()
-    sv = REF_LOOP_SIGMA_VECTORS.get(args.workload)
+    loop = REF_LOOP.get(args.workload)
+    measured = measured_reference_run(named_workload("mrcis_6e8o_v40", seed=args.seed, ksym=args.ksym), NROOTS, RTOL)
     for w in range(args.warmup):
-        cpu_estimate(p, args.cpu_rows // 4, args.cpu_sample // 4, sv, seed=1000 + w)
-    ests = [cpu_estimate(p, args.cpu_rows, args.cpu_sample, sv, seed=s) for s in range(max(1, args.steps))]
+        cpu_estimate(p, args.cpu_rows // 4, args.cpu_sample // 4, loop, seed=1000 + w, calib=measured)
+    ests = [cpu_estimate(p, args.cpu_rows, args.cpu_sample, loop, seed=s, calib=measured)
+            for s in range(max(1, args.steps))]
     v = float(np.mean([e["value"] for e in ests]))
     cb = dict(ests[-1])
     cb["value"] = round(v, 3)
-    measured = measured_reference_run(named_workload("mrcis_6e8o_v40", seed=args.seed, ksym=args.ksym), NROOTS, RTOL)
     out = {"impl": "reference",
            "metric": "s to 8 roots at |dE|<1e-7 Eh (mixed-precision block Davidson incl. H build), 1 GB300",
            "value": round(v, 3), "unit": "s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
