@@ -211,6 +211,28 @@ typedef struct {
 PSOCI_API psoci_status psoci_davidson(psoci_ctx *ctx, const psoci_dav_opts *opts, double *evals,
                             double *evecs, double *rnorms, psoci_dav_stats *stats);
 
+/* Sigma autotuner: times each variant of the mixed-precision sigma kernel (lanes per row
+ * 32 or 16 x stored elements in flight per lane 4 or 2; variant 0 is the default, 32 x 4) on
+ * k random vectors with CUDA events on the context's stream and keeps the fastest for this
+ * Hamiltonian (a new build resets it to 0).  choice receives it; times_ms (4 entries, may be
+ * NULL) the best of three runs of each.  k = 0 times nothing and installs the variant given
+ * in *choice (0..3).  Needs a stored build with the FP32 copy.  No counterpart in the
+ * reference. */
+PSOCI_API psoci_status psoci_autotune_sigma(psoci_ctx *ctx, int k, int *choice, float *times_ms);
+
+/* Batched Davidson over several double-group symmetry blocks, one context each (the reference
+ * solves one ksym block per job, driver.PSOCI.splittest.C:1186-1311): block b is solved as
+ * psoci_davidson(ctxs[b], &opts[b], evals[b], evecs[b], rnorms[b], &stats[b]) would solve it,
+ * all blocks at once — each on its context's own stream, driven by its own host thread, so
+ * the kernels of the blocks overlap on the GPU and one block's host-side eigen-solve overlaps
+ * the others' kernels.  Before a block's first MIXED solve after a build, its sigma variant is
+ * chosen by psoci_autotune_sigma.  evecs and rnorms may be NULL, or hold NULL entries;
+ * block_status (may be NULL) receives each block's status; the return value is the first
+ * failing block's status.  The contexts must be distinct. */
+PSOCI_API psoci_status psoci_davidson_batch(psoci_ctx *const *ctxs, int nblocks, const psoci_dav_opts *opts,
+                                            double *const *evals, double *const *evecs, double *const *rnorms,
+                                            psoci_dav_stats *stats, psoci_status *block_status);
+
 /* Step-level Davidson: the basis and subspace of the reference's own loop
  * (driver.PSOCI.splittest.C:1186-1311), held on the device between calls so that a host
  * program keeps that loop as it is.  One basis per context: V and H*V (N x max_vectors), the

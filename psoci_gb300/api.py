@@ -94,6 +94,10 @@ SIGNATURES = {
     "psoci_set_guess": (ctypes.c_int, [_P, ctypes.c_int, _DP]),
     "psoci_density1": (ctypes.c_int, [_P, ctypes.c_int, _DP, _DP]),
     "psoci_density1_device": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p]),
+    "psoci_autotune_sigma": (ctypes.c_int, [_P, ctypes.c_int, _IP, ctypes.POINTER(ctypes.c_float)]),
+    "psoci_davidson_batch": (ctypes.c_int, [ctypes.POINTER(_P), ctypes.c_int, ctypes.POINTER(DavOpts),
+                                            ctypes.POINTER(_DP), ctypes.POINTER(_DP), ctypes.POINTER(_DP),
+                                            ctypes.POINTER(DavStats), _IP]),
     "psoci_energy_gradient": (ctypes.c_int, [_P, ctypes.c_int, _DP, ctypes.c_int, ctypes.c_int, _DP, _DP]),
     "psoci_energy_gradient_device": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int,
                                                     ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]),
@@ -332,6 +336,18 @@ class Context:
         self._check(self.lib.psoci_density1_device(self.ctx, k, ctypes.c_void_p(dV_ptr), ldv,
                                                    ctypes.c_void_p(dD_ptr)), "density1_device")
 
+    def autotune_sigma(self, k: int = 8):
+        """Pick the fastest mixed-sigma variant for this Hamiltonian: (choice, ms per variant)."""
+        ch = ctypes.c_int()
+        t = (ctypes.c_float * 4)()
+        self._check(self.lib.psoci_autotune_sigma(self.ctx, k, ctypes.byref(ch), t), "autotune_sigma")
+        return ch.value, [float(x) for x in t]
+
+    def set_sigma_variant(self, v: int):
+        """Install mixed-sigma variant v (0..3) without timing."""
+        ch = ctypes.c_int(v)
+        self._check(self.lib.psoci_autotune_sigma(self.ctx, 0, ctypes.byref(ch), None), "autotune_sigma")
+
     def energy_gradient(self, vecs, nonzero_only: bool = False, prec: int = PREC_FP64):
         """dE_r/d(packed one-electron table) [k, nbf(nbf+1)/2] and dE_r/d(canonical two-electron
         table) [k, NNDAF(NNDAF(nbf))] for CI vectors [k, N] (root-major): the 1-particle and
@@ -388,6 +404,34 @@ class Context:
     def launch_count(self) -> int:
         """Kernels the library has launched in this process so far (all contexts)."""
         return int(self.lib.psoci_launch_count())
+
+
+def davidson_batch(contexts, nroots, rtol: float = 1e-6, mixed: bool = True, refine: bool = True,
+                   max_subspace=0, max_iter: int = 1000, want_vectors: bool = False, precond_min: float = 1e-3):
+    """Solve several symmetry blocks (one Context each, Hamiltonians built) at once:
+    nroots[b] roots of block b.  Returns a list of DavidsonResult (vectors when asked)."""
+    lib = load_library()
+    nb = len(contexts)
+    ms = list(max_subspace) if isinstance(max_subspace, (list, tuple)) else [max_subspace] * nb
+    opts = (DavOpts * nb)(*[DavOpts(int(nroots[b]), int(ms[b]), max_iter, rtol, PREC_MIXED if mixed else PREC_FP64,
+                                    int(refine), 1, precond_min) for b in range(nb)])
+    ctxs = (_P * nb)(*[c.ctx for c in contexts])
+    ev = [np.zeros(int(nroots[b])) for b in range(nb)]
+    rn = [np.zeros(int(nroots[b])) for b in range(nb)]
+    vec = [np.zeros((int(nroots[b]), contexts[b].nsef)) for b in range(nb)] if want_vectors else None
+    pev = (_DP * nb)(*[_ptr(a, _DP) for a in ev])
+    prn = (_DP * nb)(*[_ptr(a, _DP) for a in rn])
+    pvec = (_DP * nb)(*[_ptr(a, _DP) for a in vec]) if vec is not None else None
+    stats = (DavStats * nb)()
+    bst = (ctypes.c_int * nb)()
+    st = lib.psoci_davidson_batch(ctxs, nb, opts, pev, pvec, prn, stats, bst)
+    if st != PSOCI_OK:
+        bad = [b for b in range(nb) if bst[b] != PSOCI_OK]
+        raise PsociError(st, f"davidson_batch: blocks {bad} failed: " +
+                         "; ".join(lib.psoci_last_error(contexts[b].ctx).decode() for b in bad))
+    return [DavidsonResult(ev[b], vec[b] if vec is not None else None, rn[b], stats[b].iterations,
+                           stats[b].sigma_calls, stats[b].collapses, stats[b].refine_iters, stats[b].seconds,
+                           stats[b].sigma_seconds) for b in range(nb)]
 
 
 def natural_orbitals(dens_packed, orb_sym):

@@ -1,6 +1,7 @@
 // C ABI of libpsoci_gpu.so (declared in include/psoci_gpu.h).
 #include <cstdio>
 #include <cstring>
+#include <thread>
 #include <vector>
 
 #include "psoci_internal.cuh"
@@ -436,6 +437,48 @@ psoci_status psoci_davidson(psoci_ctx *c, const psoci_dav_opts *opts, double *ev
   psoci_status s;
   if ((s = set_device(c))) return s;
   return psoci_davidson_impl(c, opts, evals, evecs, rnorms, stats);
+}
+
+psoci_status psoci_autotune_sigma(psoci_ctx *c, int k, int *choice, float *times_ms) {
+  if (!c) return PSOCI_ERR_INVALID_ARG;
+  psoci_status s;
+  if ((s = set_device(c))) return s;
+  return psoci_sigma_autotune_run(c, k, choice, times_ms);
+}
+
+psoci_status psoci_davidson_batch(psoci_ctx *const *ctxs, int nblocks, const psoci_dav_opts *opts,
+                                  double *const *evals, double *const *evecs, double *const *rnorms,
+                                  psoci_dav_stats *stats, psoci_status *block_status) {
+  if (!ctxs || !opts || !evals || nblocks < 1) return PSOCI_ERR_INVALID_ARG;
+  for (int b = 0; b < nblocks; ++b) {
+    if (!ctxs[b] || !evals[b]) return PSOCI_ERR_INVALID_ARG;
+    for (int a = 0; a < b; ++a)
+      if (ctxs[a] == ctxs[b]) return psoci_fail(ctxs[b], PSOCI_ERR_INVALID_ARG, "davidson_batch: a context twice");
+  }
+  std::vector<psoci_status> st(nblocks, PSOCI_OK);
+  auto run = [&](int b) {
+    psoci_ctx *c = ctxs[b];
+    psoci_status s = set_device(c);
+    // the sigma variant for this block's Hamiltonian, chosen once per build
+    if (s == PSOCI_OK && opts[b].prec == PSOCI_PREC_MIXED && c->have_h && !c->direct && c->d_val32 && !c->sigma_tuned) {
+      s = psoci_sigma_autotune_run(c, std::min(8, std::max(1, opts[b].nroots)), nullptr, nullptr);
+      if (s == PSOCI_OK) c->sigma_tuned = true;
+    }
+    if (s == PSOCI_OK)
+      s = psoci_davidson_impl(c, &opts[b], evals[b], evecs ? evecs[b] : nullptr, rnorms ? rnorms[b] : nullptr,
+                              stats ? &stats[b] : nullptr);
+    st[b] = s;
+  };
+  std::vector<std::thread> th;
+  for (int b = 1; b < nblocks; ++b) th.emplace_back(run, b);
+  run(0);
+  for (auto &t : th) t.join();
+  psoci_status worst = PSOCI_OK;
+  for (int b = 0; b < nblocks; ++b) {
+    if (block_status) block_status[b] = st[b];
+    if (st[b] != PSOCI_OK && worst == PSOCI_OK) worst = st[b];
+  }
+  return worst;
 }
 
 }  // extern "C"

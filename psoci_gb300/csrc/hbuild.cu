@@ -2467,6 +2467,8 @@ psoci_status psoci_join_prepare(psoci_ctx *c) {
 
 void psoci_h_release(psoci_ctx *c) {
   psoci_grad_release(c);
+  c->sigma_variant = 0;
+  c->sigma_tuned = false;
   psoci_free(c->dir_nbroff);
   psoci_free(c->dir_nbr);
   psoci_free(c->dir_segcfg);

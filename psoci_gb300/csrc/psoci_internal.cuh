@@ -111,6 +111,10 @@ struct psoci_ctx {
   float2 *den_vs = nullptr;      // float-float copy of the roots of one pass
   size_t den_vs_cap = 0;
 
+  // mixed-sigma variant in use (sigma.cu; psoci_autotune_sigma picks it, a build resets it)
+  int sigma_variant = 0;
+  bool sigma_tuned = false;
+
   // neighbour lists of the energy gradient (hbuild.cu): every pair within two excitations
   // (grad_mode 0) or those with a non-zero integral prefactor (1)
   int64_t *grad_nbroff = nullptr;
@@ -199,6 +203,9 @@ psoci_status psoci_scan_i64(psoci_ctx *c, const int64_t *d_in, int64_t *d_out, i
 // sigma (sigma.cu) — device pointers, row-major N x k with leading dims
 psoci_status psoci_sigma_launch(psoci_ctx *c, int k, const double *dX, int ldx, double *dY, int ldy,
                                 psoci_prec prec, float *dX32);
+
+#define PSOCI_SIGMA_VARIANTS 4
+psoci_status psoci_sigma_autotune_run(psoci_ctx *c, int k, int *choice, float *times_ms);
 
 // determinant templates (dets.cu)
 psoci_status psoci_dets_build(psoci_ctx *c);

@@ -152,8 +152,13 @@ __device__ __forceinline__ void kahan_add(float &s, float &c, float prod) {
 // MIXED: FP32 element x FP32 input products.  Each lane keeps a compensated FP32 sum per
 // vector (Kahan: the rounding error of every addition is carried in c and fed back), so
 // no FP64 arithmetic runs in the streaming loop — on GB300 the FP64 pipe, not HBM, would
-// otherwise bound the kernel.  The 32 lane sums (value + compensation) are combined in FP64.
-template <int K>
+// otherwise bound the kernel.  The lane sums (value + compensation) are combined as
+// float-float pairs, FP64 only at the end.
+//
+// Variants (chosen per Hamiltonian by psoci_autotune_sigma): LPR lanes per row (32: a warp
+// per row; 16: two rows per warp, for short rows) and UNR stored elements per lane whose
+// gathers are in flight together.
+template <int K, int LPR, int UNR>
 __global__ void __launch_bounds__(SIG_THREADS) k_spmm_mixed(int64_t nrows, const int64_t *__restrict__ rowptr,
                                                             const int32_t *__restrict__ col,
                                                             const float *__restrict__ val,
@@ -164,31 +169,36 @@ __global__ void __launch_bounds__(SIG_THREADS) k_spmm_mixed(int64_t nrows, const
   // wavefront per gathered row, and half the bytes when the block is narrow
   constexpr int XS = (K <= 4) ? 4 : 8;
   const int lane = threadIdx.x & 31;
-  const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  for (int64_t r = warp; r < nrows; r += nwarps) {
+  const int sub = lane % LPR;  // lane within the row group
+  const int64_t grp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / LPR;
+  const int64_t ngrp = ((int64_t)gridDim.x * blockDim.x) / LPR;
+  // every lane of the warp runs the same number of rounds (shuffles below)
+  const int64_t rounds = (nrows + ngrp - 1) / ngrp;
+  for (int64_t it = 0; it < rounds; ++it) {
+    const int64_t r = grp + it * ngrp;
+    const bool live = r < nrows;
     float s[K], cmp[K];
 #pragma unroll
     for (int q = 0; q < K; ++q) { s[q] = 0.f; cmp[q] = 0.f; }
-    const int64_t e = rowptr[r + 1];
-    int64_t t = rowptr[r] + lane;
-    // SIG_UNROLL elements per lane in flight: the gathers are latency-bound
-    for (; t + 32 * (SIG_UNROLL - 1) < e; t += 32 * SIG_UNROLL) {
-      int cc[SIG_UNROLL];
-      float vv[SIG_UNROLL], xx[SIG_UNROLL][8];
+    const int64_t e = live ? rowptr[r + 1] : 0;
+    int64_t t = live ? rowptr[r] + sub : 0;
+    // UNR elements per lane in flight: the gathers are latency-bound
+    for (; t + LPR * (UNR - 1) < e; t += LPR * UNR) {
+      int cc[UNR];
+      float vv[UNR], xx[UNR][8];
 #pragma unroll
-      for (int u = 0; u < SIG_UNROLL; ++u) {
-        cc[u] = ldg_stream(col + t + 32 * u);
-        vv[u] = ldg_stream(val + t + 32 * u);
+      for (int u = 0; u < UNR; ++u) {
+        cc[u] = ldg_stream(col + t + LPR * u);
+        vv[u] = ldg_stream(val + t + LPR * u);
       }
 #pragma unroll
-      for (int u = 0; u < SIG_UNROLL; ++u) ldg_row<XS>(xx[u], x + (int64_t)cc[u] * XS);
+      for (int u = 0; u < UNR; ++u) ldg_row<XS>(xx[u], x + (int64_t)cc[u] * XS);
 #pragma unroll
-      for (int u = 0; u < SIG_UNROLL; ++u)
+      for (int u = 0; u < UNR; ++u)
 #pragma unroll
         for (int q = 0; q < K; ++q) kahan_add(s[q], cmp[q], __fmul_rn(vv[u], xx[u][q]));
     }
-    for (; t < e; t += 32) {
+    for (; t < e; t += LPR) {
       const int c = ldg_stream(col + t);
       const float v = ldg_stream(val + t);
       float xv[8];
@@ -196,29 +206,33 @@ __global__ void __launch_bounds__(SIG_THREADS) k_spmm_mixed(int64_t nrows, const
 #pragma unroll
       for (int q = 0; q < K; ++q) kahan_add(s[q], cmp[q], __fmul_rn(v, xv[q]));
     }
-    // Kahan leaves sum = s - cmp; reduce (s, -cmp) as float-float pairs, FP64 only at the end
+    // Kahan leaves sum = s - cmp; reduce (s, -cmp) as float-float pairs within the row group:
+    // halving exchanges leave each lane one partial, butterflies finish the sum
     ff2 v[8];
 #pragma unroll
     for (int q = 0; q < 8; ++q) v[q] = (q < K) ? ff2{s[q], -cmp[q]} : ff2{0.f, 0.f};
     ff2 a[4], b[2], cc;
+    constexpr int O1 = LPR / 2, O2 = LPR / 4, O3 = LPR / 8;
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
-      const bool hi = lane & 16;
-      a[i] = ff_add(hi ? v[i + 4] : v[i], shfl_ff(hi ? v[i] : v[i + 4], 16));
+      const bool hi = lane & O1;
+      a[i] = ff_add(hi ? v[i + 4] : v[i], shfl_ff(hi ? v[i] : v[i + 4], O1));
     }
 #pragma unroll
     for (int i = 0; i < 2; ++i) {
-      const bool hi = lane & 8;
-      b[i] = ff_add(hi ? a[i + 2] : a[i], shfl_ff(hi ? a[i] : a[i + 2], 8));
+      const bool hi = lane & O2;
+      b[i] = ff_add(hi ? a[i + 2] : a[i], shfl_ff(hi ? a[i] : a[i + 2], O2));
     }
     {
-      const bool hi = lane & 4;
-      cc = ff_add(hi ? b[1] : b[0], shfl_ff(hi ? b[0] : b[1], 4));
+      const bool hi = lane & O3;
+      cc = ff_add(hi ? b[1] : b[0], shfl_ff(hi ? b[0] : b[1], O3));
     }
-    cc = ff_add(cc, shfl_ff(cc, 2));
-    cc = ff_add(cc, shfl_ff(cc, 1));
-    const int qq = lane >> 2;
-    if ((lane & 3) == 0 && qq < K) y[r * ldy + qq] = (double)cc.h + (double)cc.l;
+#pragma unroll
+    for (int o = O3 / 2; o > 0; o >>= 1) cc = ff_add(cc, shfl_ff(cc, o));
+    // lanes sub = q * O3 ... hold value q (the halving steps sorted the values by the high bits)
+    const int qq = (((sub & O1) ? 1 : 0) | ((sub & O2) ? 2 : 0) | ((sub & O3) ? 4 : 0));
+    const int q = ((qq & 1) << 2) | (qq & 2) | ((qq & 4) >> 2);
+    if (live && (sub & (O3 - 1)) == 0 && q < K) y[r * ldy + q] = (double)cc.h + (double)cc.l;
   }
 }
 
@@ -334,8 +348,23 @@ void launch_k(psoci_ctx *c, int64_t n, const double *dX, int ldx, double *dY, in
   else if (prec == PSOCI_PREC_FF)
     k_spmm_ff<K><<<blocks, SIG_THREADS, 0, c->stream>>>(n, c->d_rowptr, c->d_col, c->d_val,
                                                         reinterpret_cast<const float2 *>(x32), dY, ldy);
-  else
-    k_spmm_mixed<K><<<blocks, SIG_THREADS, 0, c->stream>>>(n, c->d_rowptr, c->d_col, c->d_val32, x32, dY, ldy);
+  else {
+    // the variant chosen by psoci_autotune_sigma for this Hamiltonian (0 until it runs)
+    switch (c->sigma_variant) {
+      case 1:
+        k_spmm_mixed<K, 32, 2><<<blocks, SIG_THREADS, 0, c->stream>>>(n, c->d_rowptr, c->d_col, c->d_val32, x32, dY, ldy);
+        break;
+      case 2:
+        k_spmm_mixed<K, 16, 4><<<blocks, SIG_THREADS, 0, c->stream>>>(n, c->d_rowptr, c->d_col, c->d_val32, x32, dY, ldy);
+        break;
+      case 3:
+        k_spmm_mixed<K, 16, 2><<<blocks, SIG_THREADS, 0, c->stream>>>(n, c->d_rowptr, c->d_col, c->d_val32, x32, dY, ldy);
+        break;
+      default:
+        k_spmm_mixed<K, 32, SIG_UNROLL><<<blocks, SIG_THREADS, 0, c->stream>>>(n, c->d_rowptr, c->d_col, c->d_val32, x32,
+                                                                              dY, ldy);
+    }
+  }
 }
 
 }  // namespace
@@ -382,5 +411,66 @@ psoci_status psoci_sigma_launch(psoci_ctx *c, int k, const double *dX, int ldx, 
     }
     PSOCI_CUDA(c, cudaGetLastError());
   }
+  return PSOCI_OK;
+}
+
+// Autotuner of the mixed sigma: each variant (lanes per row x gathers in flight) timed with
+// CUDA events on the context's stream over k random vectors, best of three after one warm-up
+// run; the fastest is kept for this Hamiltonian (reset by the next build).  times_ms may be
+// null or receive PSOCI_SIGMA_VARIANTS entries.
+psoci_status psoci_sigma_autotune_run(psoci_ctx *c, int k, int *choice, float *times_ms) {
+  if (!c->have_h || c->direct || !c->d_val32)
+    return psoci_fail(c, PSOCI_ERR_STATE, "autotune_sigma: needs a stored Hamiltonian with the FP32 copy");
+  if (k == 0) {
+    // no timing: install the variant given in *choice
+    if (!choice || *choice < 0 || *choice >= PSOCI_SIGMA_VARIANTS)
+      return psoci_fail(c, PSOCI_ERR_INVALID_ARG, "autotune_sigma: variant outside 0..3");
+    c->sigma_variant = *choice;
+    c->sigma_tuned = true;
+    return PSOCI_OK;
+  }
+  if (k < 1 || k > 8) return psoci_fail(c, PSOCI_ERR_INVALID_ARG, "autotune_sigma: k must be 0..8");
+  const int64_t n = c->nsef_total;
+  double *dX = nullptr, *dY = nullptr;
+  float *x32 = nullptr;
+  psoci_status s;
+  if ((s = psoci_alloc(c, &dX, (size_t)n * k)) || (s = psoci_alloc(c, &dY, (size_t)n * k)) ||
+      (s = psoci_alloc(c, &x32, (size_t)n * 8))) {
+    psoci_free(dX); psoci_free(dY); psoci_free(x32);
+    return s;
+  }
+  cudaStream_t st = c->stream;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  // inputs: any finite values (the timing does not depend on them)
+  cudaMemsetAsync(dX, 0, sizeof(double) * n * k, st);
+  const int saved = c->sigma_variant;
+  int best = 0;
+  float best_ms = 1e30f;
+  for (int v = 0; v < PSOCI_SIGMA_VARIANTS; ++v) {
+    c->sigma_variant = v;
+    float tmin = 1e30f;
+    for (int rep = 0; rep < 4 && s == PSOCI_OK; ++rep) {
+      cudaEventRecord(e0, st);
+      s = psoci_sigma_launch(c, k, dX, k, dY, k, PSOCI_PREC_MIXED, x32);
+      cudaEventRecord(e1, st);
+      cudaEventSynchronize(e1);
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      if (rep > 0) tmin = std::min(tmin, ms);
+    }
+    if (times_ms) times_ms[v] = tmin;
+    if (tmin < best_ms) { best_ms = tmin; best = v; }
+  }
+  cudaError_t e = cudaStreamSynchronize(st);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  psoci_free(dX); psoci_free(dY); psoci_free(x32);
+  if (s != PSOCI_OK) { c->sigma_variant = saved; return s; }
+  if (e != cudaSuccess) { c->sigma_variant = saved; return psoci_cuda_fail(c, e, "autotune_sigma"); }
+  c->sigma_variant = best;
+  c->sigma_tuned = true;
+  if (choice) *choice = best;
   return PSOCI_OK;
 }
