@@ -211,13 +211,13 @@ typedef struct {
 PSOCI_API psoci_status psoci_davidson(psoci_ctx *ctx, const psoci_dav_opts *opts, double *evals,
                             double *evecs, double *rnorms, psoci_dav_stats *stats);
 
-/* Sigma autotuner: times each variant of the mixed-precision sigma kernel (lanes per row
- * 32 or 16 x stored elements in flight per lane 4 or 2; variant 0 is the default, 32 x 4) on
- * k random vectors with CUDA events on the context's stream and keeps the fastest for this
- * Hamiltonian (a new build resets it to 0).  choice receives it; times_ms (4 entries, may be
- * NULL) the best of three runs of each.  k = 0 times nothing and installs the variant given
- * in *choice (0..3).  Needs a stored build with the FP32 copy.  No counterpart in the
- * reference. */
+/* Sigma autotuner: times each of the 6 variants of the mixed-precision sigma kernel — lanes
+ * per row x stored elements in flight per lane: 0 (32 x 4), 1 (32 x 2), 2 (16 x 4), 3 (16 x 2),
+ * 4 (8 x 4), 5 (16 x 6) — on k random vectors with CUDA events on the context's stream and
+ * keeps the fastest for this Hamiltonian (a new build resets it to variant 2).  choice
+ * receives it; times_ms (6 entries, may be NULL) the best of three runs of each.  k = 0 times
+ * nothing and installs the variant given in *choice (0..5).  Needs a stored build with the
+ * FP32 copy.  No counterpart in the reference. */
 PSOCI_API psoci_status psoci_autotune_sigma(psoci_ctx *ctx, int k, int *choice, float *times_ms);
 
 /* Batched Davidson over several double-group symmetry blocks, one context each (the reference

@@ -339,12 +339,12 @@ class Context:
     def autotune_sigma(self, k: int = 8):
         """Pick the fastest mixed-sigma variant for this Hamiltonian: (choice, ms per variant)."""
         ch = ctypes.c_int()
-        t = (ctypes.c_float * 4)()
+        t = (ctypes.c_float * 6)()
         self._check(self.lib.psoci_autotune_sigma(self.ctx, k, ctypes.byref(ch), t), "autotune_sigma")
         return ch.value, [float(x) for x in t]
 
     def set_sigma_variant(self, v: int):
-        """Install mixed-sigma variant v (0..3) without timing."""
+        """Install mixed-sigma variant v (0..5) without timing."""
         ch = ctypes.c_int(v)
         self._check(self.lib.psoci_autotune_sigma(self.ctx, 0, ctypes.byref(ch), None), "autotune_sigma")
 

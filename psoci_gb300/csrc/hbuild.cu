@@ -109,7 +109,9 @@ struct Params {
   double *val;
   float *val32;
   double *diag;
-  // direct sigma (PASS 2): Y[:, 0:kvec] += H X[:, 0:kvec]
+  // direct sigma (PASS 2): Y[:, 0:kvec] += H X[:, 0:kvec]; with dx32 (the inputs in FP32,
+  // 8 per row) the products are FP32 element x FP32 input with compensated FP32 sums
+  const float *dx32;
   const double *dx;
   double *dy;
   int ldx, ldy, kvec;
@@ -1444,8 +1446,9 @@ __global__ void __launch_bounds__(WARPS_PER_CTA * 32) k_hbuild_fast(Params P) {
         chunk_end = cursor + len;
       }
       double acc[8];
+      float accs[8], accc[8];  // direct mode with FP32 inputs: compensated FP32 sums
 #pragma unroll
-      for (int q = 0; q < 8; ++q) acc[q] = 0.0;
+      for (int q = 0; q < 8; ++q) { acc[q] = 0.0; accs[q] = 0.f; accc[q] = 0.f; }
       const unsigned long long base = cursor;
       // chunks beyond the slab capacity are counted but not written; the host sees the
       // final counter, enlarges the slab and evaluates again
@@ -1478,7 +1481,20 @@ __global__ void __launch_bounds__(WARPS_PER_CTA * 32) k_hbuild_fast(Params P) {
           v = sef_elem<W>(P, pi, ws->K, flip ? t : r, flip ? r : t, conn, (DIRECT && pi.swap) ? nullptr : &rowA);
           keep = (fabs(v) >= PSOCI_MIN_VALUE) || (diag_blk && t == r);
           if (DIRECT) {
-            if (keep) {
+            if (keep && P.dx32) {
+              const float vf = (float)v;
+              const float4 *xr = reinterpret_cast<const float4 *>(P.dx32 + (pi.colbase + t) * 8);
+              const float4 xa = __ldg(xr), xb = __ldg(xr + 1);
+              const float xv[8] = {xa.x, xa.y, xa.z, xa.w, xb.x, xb.y, xb.z, xb.w};
+#pragma unroll
+              for (int q = 0; q < 8; ++q) {
+                // Kahan: the rounding error of each addition is carried in accc and fed back
+                const float yv = __fsub_rn(__fmul_rn(vf, xv[q]), accc[q]);
+                const float tt = __fadd_rn(accs[q], yv);
+                accc[q] = __fsub_rn(__fsub_rn(tt, accs[q]), yv);
+                accs[q] = tt;
+              }
+            } else if (keep) {
               const double *xr = P.dx + (pi.colbase + t) * P.ldx;
 #pragma unroll
               for (int q = 0; q < 8; ++q)
@@ -1495,6 +1511,10 @@ __global__ void __launch_bounds__(WARPS_PER_CTA * 32) k_hbuild_fast(Params P) {
         }
       }
       if (DIRECT) {
+        if (P.dx32) {
+#pragma unroll
+          for (int q = 0; q < 8; ++q) acc[q] = (double)accs[q] - (double)accc[q];
+        }
         const double tot = reduce_scatter8_f64(acc, lane);
         const int q = lane >> 2;
         if ((lane & 3) == 0 && q < P.kvec && tot != 0.0) atomicAdd(P.dy + (P.sefoff[I] + r) * P.ldy + q, tot);
@@ -2239,8 +2259,21 @@ psoci_status run_build(psoci_ctx *c, psoci_hmode mode, int64_t *nnz_out) {
 #undef TRYC
 }
 
+// X (FP64, leading dim ldx, k <= 8 columns) -> X32 (FP32, row stride 8, zero padded)
+__global__ void k_direct_x32(int64_t n, int k, const double *__restrict__ x, int ldx, float *__restrict__ x32) {
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+    float f[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) f[q] = (q < k) ? (float)x[r * ldx + q] : 0.f;
+    float4 *d = reinterpret_cast<float4 *>(x32 + r * 8);
+    d[0] = make_float4(f[0], f[1], f[2], f[3]);
+    d[1] = make_float4(f[4], f[5], f[6], f[7]);
+  }
+}
+
 template <int W>
-psoci_status run_direct_sigma(psoci_ctx *c, int k, const double *dX, int ldx, double *dY, int ldy) {
+psoci_status run_direct_sigma(psoci_ctx *c, int k, const double *dX, int ldx, double *dY, int ldy, psoci_prec prec,
+                              float *x32) {
   cudaStream_t st = c->stream;
   Params P = {};
   P.nconf = c->nconf; P.nbf = c->nbf; P.nelec = c->nelec; P.ksym = c->ksym;
@@ -2262,8 +2295,16 @@ psoci_status run_direct_sigma(psoci_ctx *c, int k, const double *dX, int ldx, do
   else
     PSOCI_CUDA(c, cudaFuncSetAttribute(k_hbuild<W, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>((P.nseg + WARPS_PER_CTA - 1) / WARPS_PER_CTA, 152 * 16));
+  // MIXED (connectivity-marking kernel only): FP32 element x FP32 input products
+  const bool mixed = fast && prec == PSOCI_PREC_MIXED && x32;
   for (int q0 = 0; q0 < k; q0 += 8) {
     P.dx = dX + q0; P.dy = dY + q0; P.ldx = ldx; P.ldy = ldy; P.kvec = std::min(8, k - q0);
+    P.dx32 = nullptr;
+    if (mixed) {
+      psoci_note_launch();
+      k_direct_x32<<<(unsigned)std::min<int64_t>((N + 255) / 256, 152 * 16), 256, 0, st>>>(N, P.kvec, P.dx, ldx, x32);
+      P.dx32 = x32;
+    }
     psoci_note_launch();
     if (fast)
       k_hbuild_fast<W, true><<<blocks, WARPS_PER_CTA * 32, smem, st>>>(P);
@@ -2276,9 +2317,11 @@ psoci_status run_direct_sigma(psoci_ctx *c, int k, const double *dX, int ldx, do
 
 }  // namespace
 
-psoci_status psoci_direct_sigma(psoci_ctx *c, int k, const double *dX, int ldx, double *dY, int ldy) {
+psoci_status psoci_direct_sigma(psoci_ctx *c, int k, const double *dX, int ldx, double *dY, int ldy, psoci_prec prec,
+                                float *x32) {
   if (!c->direct) return psoci_fail(c, PSOCI_ERR_STATE, "direct sigma: no direct-mode build");
-  return (c->words == 1) ? run_direct_sigma<1>(c, k, dX, ldx, dY, ldy) : run_direct_sigma<2>(c, k, dX, ldx, dY, ldy);
+  return (c->words == 1) ? run_direct_sigma<1>(c, k, dX, ldx, dY, ldy, prec, x32)
+                         : run_direct_sigma<2>(c, k, dX, ldx, dY, ldy, prec, x32);
 }
 
 void psoci_join_release(psoci_ctx *c) {
@@ -2467,7 +2510,7 @@ psoci_status psoci_join_prepare(psoci_ctx *c) {
 
 void psoci_h_release(psoci_ctx *c) {
   psoci_grad_release(c);
-  c->sigma_variant = 0;
+  c->sigma_variant = PSOCI_SIGMA_DEFAULT;
   c->sigma_tuned = false;
   psoci_free(c->dir_nbroff);
   psoci_free(c->dir_nbr);

@@ -15,6 +15,10 @@
 #define PSOCI_MAX_WORDS 2     // nbf <= 128
 #define PSOCI_SEG 32          // neighbours per warp segment in the H build
 #define PSOCI_MIN_VALUE 1.0e-8  // packSefsef threshold (PsociHamiltonian.hpp:37)
+// mixed-sigma kernel variants (sigma.cu) and the one used until psoci_autotune_sigma runs:
+// 16 lanes per row, 4 gathers in flight per lane (the fastest on the MRCISD blocks measured)
+#define PSOCI_SIGMA_VARIANTS 6
+#define PSOCI_SIGMA_DEFAULT 2
 
 // ------------------------------------------------------------------------------------
 // host-side context
@@ -112,7 +116,7 @@ struct psoci_ctx {
   size_t den_vs_cap = 0;
 
   // mixed-sigma variant in use (sigma.cu; psoci_autotune_sigma picks it, a build resets it)
-  int sigma_variant = 0;
+  int sigma_variant = PSOCI_SIGMA_DEFAULT;
   bool sigma_tuned = false;
 
   // neighbour lists of the energy gradient (hbuild.cu): every pair within two excitations
@@ -204,7 +208,6 @@ psoci_status psoci_scan_i64(psoci_ctx *c, const int64_t *d_in, int64_t *d_out, i
 psoci_status psoci_sigma_launch(psoci_ctx *c, int k, const double *dX, int ldx, double *dY, int ldy,
                                 psoci_prec prec, float *dX32);
 
-#define PSOCI_SIGMA_VARIANTS 4
 psoci_status psoci_sigma_autotune_run(psoci_ctx *c, int k, int *choice, float *times_ms);
 
 // determinant templates (dets.cu)
@@ -212,7 +215,8 @@ psoci_status psoci_dets_build(psoci_ctx *c);
 psoci_status psoci_h_build(psoci_ctx *c, psoci_hmode mode, int64_t *nnz);
 psoci_status psoci_h_blocks(psoci_ctx *c, int npairs, const int32_t *A, const int32_t *B, double *out);
 // sigma of a direct-mode build: every element evaluated again (hbuild.cu)
-psoci_status psoci_direct_sigma(psoci_ctx *c, int k, const double *dX, int ldx, double *dY, int ldy);
+psoci_status psoci_direct_sigma(psoci_ctx *c, int k, const double *dX, int ldx, double *dY, int ldy, psoci_prec prec,
+                                float *x32);
 psoci_status psoci_join_prepare(psoci_ctx *c);  // after h_occ is set
 void psoci_join_release(psoci_ctx *c);
 void psoci_h_release(psoci_ctx *c);

@@ -168,15 +168,16 @@ __global__ void __launch_bounds__(SIG_THREADS) k_spmm_mixed(int64_t nrows, const
   // K <= 4; aligned to the stride), so every gather is one 256- or 128-bit load — one L1
   // wavefront per gathered row, and half the bytes when the block is narrow
   constexpr int XS = (K <= 4) ? 4 : 8;
+  constexpr int RPW = 32 / LPR;  // rows per warp
   const int lane = threadIdx.x & 31;
   const int sub = lane % LPR;  // lane within the row group
-  const int64_t grp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / LPR;
-  const int64_t ngrp = ((int64_t)gridDim.x * blockDim.x) / LPR;
-  // every lane of the warp runs the same number of rounds (shuffles below)
-  const int64_t rounds = (nrows + ngrp - 1) / ngrp;
-  for (int64_t it = 0; it < rounds; ++it) {
-    const int64_t r = grp + it * ngrp;
-    const bool live = r < nrows;
+  const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  // the warp takes RPW consecutive rows at a time, so all its lanes run the same number of
+  // rounds (shuffles below)
+  for (int64_t base = warp * RPW; base < nrows; base += nwarps * RPW) {
+    const int64_t r = base + lane / LPR;
+    const bool live = (RPW == 1) || r < nrows;
     float s[K], cmp[K];
 #pragma unroll
     for (int q = 0; q < K; ++q) { s[q] = 0.f; cmp[q] = 0.f; }
@@ -349,7 +350,8 @@ void launch_k(psoci_ctx *c, int64_t n, const double *dX, int ldx, double *dY, in
     k_spmm_ff<K><<<blocks, SIG_THREADS, 0, c->stream>>>(n, c->d_rowptr, c->d_col, c->d_val,
                                                         reinterpret_cast<const float2 *>(x32), dY, ldy);
   else {
-    // the variant chosen by psoci_autotune_sigma for this Hamiltonian (0 until it runs)
+    // the variant chosen by psoci_autotune_sigma for this Hamiltonian (PSOCI_SIGMA_DEFAULT
+    // until it runs)
     switch (c->sigma_variant) {
       case 1:
         k_spmm_mixed<K, 32, 2><<<blocks, SIG_THREADS, 0, c->stream>>>(n, c->d_rowptr, c->d_col, c->d_val32, x32, dY, ldy);
@@ -359,6 +361,12 @@ void launch_k(psoci_ctx *c, int64_t n, const double *dX, int ldx, double *dY, in
         break;
       case 3:
         k_spmm_mixed<K, 16, 2><<<blocks, SIG_THREADS, 0, c->stream>>>(n, c->d_rowptr, c->d_col, c->d_val32, x32, dY, ldy);
+        break;
+      case 4:
+        k_spmm_mixed<K, 8, 4><<<blocks, SIG_THREADS, 0, c->stream>>>(n, c->d_rowptr, c->d_col, c->d_val32, x32, dY, ldy);
+        break;
+      case 5:
+        k_spmm_mixed<K, 16, 6><<<blocks, SIG_THREADS, 0, c->stream>>>(n, c->d_rowptr, c->d_col, c->d_val32, x32, dY, ldy);
         break;
       default:
         k_spmm_mixed<K, 32, SIG_UNROLL><<<blocks, SIG_THREADS, 0, c->stream>>>(n, c->d_rowptr, c->d_col, c->d_val32, x32,
@@ -376,7 +384,7 @@ psoci_status psoci_sigma_launch(psoci_ctx *c, int k, const double *dX, int ldx, 
     return psoci_fail(c, PSOCI_ERR_INVALID_ARG, "sigma: unknown precision");
   if (!c->have_h) return psoci_fail(c, PSOCI_ERR_STATE, "sigma: Hamiltonian not built");
   if (k < 1 || ldx < k || ldy < k) return psoci_fail(c, PSOCI_ERR_INVALID_ARG, "sigma: bad k / leading dimensions");
-  if (c->direct) return psoci_direct_sigma(c, k, dX, ldx, dY, ldy);
+  if (c->direct) return psoci_direct_sigma(c, k, dX, ldx, dY, ldy, prec, dX32);
   if (prec == PSOCI_PREC_MIXED && !c->d_val32)
     return psoci_fail(c, PSOCI_ERR_STATE, "sigma: MIXED needs the FP32 copy (PSOCI_HMODE_CSR_BOTH)");
   const int64_t n = c->nsef_total;
@@ -424,7 +432,7 @@ psoci_status psoci_sigma_autotune_run(psoci_ctx *c, int k, int *choice, float *t
   if (k == 0) {
     // no timing: install the variant given in *choice
     if (!choice || *choice < 0 || *choice >= PSOCI_SIGMA_VARIANTS)
-      return psoci_fail(c, PSOCI_ERR_INVALID_ARG, "autotune_sigma: variant outside 0..3");
+      return psoci_fail(c, PSOCI_ERR_INVALID_ARG, "autotune_sigma: variant outside 0..5");
     c->sigma_variant = *choice;
     c->sigma_tuned = true;
     return PSOCI_OK;

@@ -104,11 +104,14 @@ def test_mrcisd_4e6o_v30_direct(oracle_mod):
     X = np.random.default_rng(9).standard_normal((n, 8))
     Yref = O.sigma_lower(rp, ci, va, X.T.copy()).T
     scale = np.abs(Yref).max()
-    for prec in (api.PREC_FP64, api.PREC_MIXED):
+    # FP64 products, and FP32 element x FP32 input products with compensated sums
+    for prec, tol in ((api.PREC_FP64, SIGMA_RTOL * 10), (api.PREC_MIXED, 1e-5)):
         Y = c.sigma(X, prec=prec)
-        assert np.abs(Y - Yref).max() <= SIGMA_RTOL * scale * 10, prec
+        assert np.abs(Y - Yref).max() <= tol * scale, prec
     F = lower_to_full(rp, ci, va, n)
     ref = _arpack(F, 8)
     e = c.davidson(8, rtol=1e-8, mixed=False).evals
     assert np.abs(e - ref).max() <= EIG_TOL_FP64, (e, ref)
+    em = c.davidson(8, rtol=1e-8, mixed=True, refine=True).evals
+    assert np.abs(em - ref).max() <= EIG_TOL_MIXED, (em, ref)
     c.close()

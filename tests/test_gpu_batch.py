@@ -59,7 +59,7 @@ def test_sigma_variants():
     ref = c.sigma(X, prec=api.PREC_FP64)
     scale = np.abs(ref).max()
     outs = []
-    for v in range(4):
+    for v in range(6):
         c.set_sigma_variant(v)
         for k in (8, 3):
             Y = c.sigma(X[:, :k], prec=api.PREC_MIXED)
@@ -68,6 +68,6 @@ def test_sigma_variants():
     for o in outs[1:]:
         assert np.abs(o - outs[0]).max() <= 1e-6 * scale
     choice, times = c.autotune_sigma(8)
-    assert 0 <= choice < 4 and all(t > 0 for t in times)
+    assert 0 <= choice < 6 and all(t > 0 for t in times)
     assert times[choice] == min(times)
     c.close()
