@@ -307,6 +307,7 @@ def run_ours(args):
 
     ctx.close()
     batch = batch_config2(args.seed, local, torch) if (rank == 0 and not args.no_batch) else None
+    direct = direct_mode(p, nnz, local, torch, r_mixed.evals) if (rank == 0 and not args.no_direct) else None
 
     if rank == 0:
         clocks = clk.summary()
@@ -365,6 +366,7 @@ def run_ours(args):
             "row_check": row_check,
             "measured_mrcis_6e8o_v40": measured_cfg1,
             "batch_4_blocks": batch,
+            "direct_mode": direct,
             "parity_mrcis_6e8o_v40": parity_cfg1,
         }
         print(json.dumps(out))
@@ -436,6 +438,62 @@ def batch_config2(seed, device, torch):
             "dE_ok": bool(all(x["max_abs_dE_mixed_vs_fp64"] < DE_TOL for x in blocks)),
             "note": "4 MRCISD blocks solved together (a host thread and stream per block), mixed precision "
                     "with refinement, residual 1e-5; wall clock, median of 3"}
+
+
+def direct_mode(p, nnz_stored, device, torch, evals_stored):
+    """Direct mode (no stored elements; every product evaluates the elements again) on the
+    benchmark block: the build of the neighbour lists and diagonal, one 8-vector product in
+    FP64 and in mixed precision (CUDA events on the library stream), a mixed-precision solve of
+    the 8 roots with FP64 refinement, and the device memory the Davidson arrays take at this
+    block and at 30M SEFs.  'effective_bandwidth' is the stored-equivalent sigma bytes
+    (FP32 values + columns for nnz_stored elements, row pointers, inputs and outputs) over the
+    product's time: not a physical HBM figure."""
+    from psoci_gb300 import api
+
+    out = {}
+    with api.Context(device) as c:
+        stream = torch.cuda.ExternalStream(c.stream_handle(), device=torch.device("cuda", device))
+        c.load_problem(p)
+        c.build_determinants()
+        t0 = time.perf_counter()
+        c.build_hamiltonian(direct=True)
+        torch.cuda.synchronize()
+        out["build_s"] = round(time.perf_counter() - t0, 4)
+        out["pairs"] = int(c.build_stats()["pairs"])
+        N = c.nsef
+        X = torch.randn(N, 8, dtype=torch.float64, device=torch.device("cuda", device))
+        Y = torch.empty_like(X)
+        for prec, name in ((api.PREC_FP64, "fp64"), (api.PREC_MIXED, "mixed")):
+            c.sigma_device(X.data_ptr(), 8, Y.data_ptr(), 8, 8, prec)
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            a.record(stream)
+            c.sigma_device(X.data_ptr(), 8, Y.data_ptr(), 8, 8, prec)
+            b.record(stream)
+            torch.cuda.synchronize()
+            t = a.elapsed_time(b) * 1e-3
+            b_eq = nnz_stored * (4 + 4) + (N + 1) * 8 + N * 8 * (8 + 4 + 4 + 8)
+            out[f"sigma8_{name}_s"] = round(t, 4)
+            out[f"effective_bandwidth_{name}_gbs"] = round(b_eq / t / 1e9, 1)
+        del X, Y
+        t0 = time.perf_counter()
+        r = c.davidson(NROOTS, rtol=RTOL, mixed=True, refine=True)
+        out["davidson_s"] = round(time.perf_counter() - t0, 3)
+        out["iterations"] = r.iterations
+        out["sigma_vectors"] = r.sigma_calls
+        out["max_abs_dE_vs_stored_mixed"] = float(np.abs(r.evals - evals_stored).max())
+
+    def davidson_bytes(n, nroots=NROOTS, maxsub=40):
+        ld = (maxsub + 1) & ~1
+        # V and HV (n x ld), X, HX, R, T (n x nroots), tmp (n x 2 nroots), FP32/float-float staging
+        # (n x 16 floats), diagonal
+        return n * ld * 8 * 2 + n * nroots * 8 * 4 + n * 2 * nroots * 8 + n * 16 * 4 + n * 8
+
+    out["davidson_arrays_gb"] = {"this_block": round(davidson_bytes(N) / 1e9, 2),
+                                 "30M_sefs": round(davidson_bytes(30_000_000) / 1e9, 2)}
+    out["note"] = ("products: FP64, or FP32 element x FP32 input with compensated FP32 sums (mixed); "
+                   "effective bandwidth is stored-equivalent bytes / time, not a physical HBM figure")
+    return out
 
 
 def energy_gradient_timing(ctx, stream, torch, dev, p, res, dens_unit, diag):
@@ -732,6 +790,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-grad", action="store_true", help="skip the energy-gradient timing")
     ap.add_argument("--no-batch", action="store_true", help="skip the four-block batched solve")
+    ap.add_argument("--no-direct", action="store_true", help="skip the direct-mode measurement")
     ap.add_argument("--no-parity", action="store_true", help="skip the 8-root check of mrcis_6e8o_v40 vs the oracle")
     ap.add_argument("--verbose", type=int, default=0)
     args = ap.parse_args()
