@@ -214,7 +214,7 @@ PSOCI_API psoci_status psoci_davidson(psoci_ctx *ctx, const psoci_dav_opts *opts
 /* Sigma autotuner: times each of the 6 variants of the mixed-precision sigma kernel — lanes
  * per row x stored elements in flight per lane: 0 (32 x 4), 1 (32 x 2), 2 (16 x 4), 3 (16 x 2),
  * 4 (8 x 4), 5 (16 x 6) — on k random vectors with CUDA events on the context's stream and
- * keeps the fastest for this Hamiltonian (a new build resets it to variant 2).  choice
+ * keeps the fastest for this Hamiltonian (a new build resets it to variant 0).  choice
  * receives it; times_ms (6 entries, may be NULL) the best of three runs of each.  k = 0 times
  * nothing and installs the variant given in *choice (0..5).  Needs a stored build with the
  * FP32 copy.  No counterpart in the reference. */

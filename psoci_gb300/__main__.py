@@ -1,13 +1,15 @@
 """Solve one double-group symmetry block of a named synthetic workload on one GPU.
 
   python -m psoci_gb300 --workload mrcisd_6e8o_v24 [--roots 8] [--rtol 1e-5] [--fp64]
-                        [--no-davidson] [--sigma K] [--density] [--verbose 1]
+                        [--no-davidson] [--sigma K] [--density] [--gradient] [--verbose 1]
 
 Determinants -> Hamiltonian (CSR) -> block Davidson; prints the sizes and the total
 energies in the layout of the reference driver's "Eigenvalue" lines.  ``--sigma K`` also
 applies H to K random vectors once (the Davidson's inner product, on its own);
 ``--density`` forms the 1-particle densities of the converged roots and prints the
-natural-orbital occupations of the first root (diagonal blocks of one orbital label).
+natural-orbital occupations of the first root (diagonal blocks of one orbital label);
+``--gradient`` forms dE/d(integral tables) of the converged roots (1-, 2-particle and
+spin-orbit densities, derivatives of the non-zero integrals).
 """
 from __future__ import annotations
 
@@ -31,6 +33,7 @@ def main(argv=None):
     ap.add_argument("--no-davidson", action="store_true")
     ap.add_argument("--sigma", type=int, default=0, help="apply H to this many random vectors once")
     ap.add_argument("--density", action="store_true", help="1-particle densities of the roots")
+    ap.add_argument("--gradient", action="store_true", help="energy gradients of the roots")
     ap.add_argument("--max-subspace", type=int, default=48)
     ap.add_argument("--device", type=int, default=0)
     ap.add_argument("--verbose", type=int, default=0)
@@ -55,11 +58,18 @@ def main(argv=None):
             print(f"sigma on {a.sigma} vectors: |HX|_max {np.abs(Y).max():.6e}")
         if not a.no_davidson:
             r = c.davidson(a.roots, rtol=a.rtol, mixed=mixed, refine=True, max_subspace=a.max_subspace,
-                           want_vectors=a.density)
+                           want_vectors=a.density or a.gradient)
             ecore = c.core_energy()
             for i, e in enumerate(r.evals):
                 print(f"Eigenvalue {i + 1:4d} Total energy (au) {e + ecore:20.12f} Electronic (au) {e:20.12f}")
             print(f"iterations {r.iterations}, sigma vectors {r.sigma_calls}, {r.seconds:.3f} s")
+            if a.gradient:
+                t0 = time.perf_counter()
+                g1, g2 = c.energy_gradient(r.evecs, nonzero_only=True)
+                tg = time.perf_counter() - t0
+                diag = [q * (q + 1) // 2 + q for q in range(p.nbf)]
+                print(f"energy gradient of {len(r.evals)} roots: {tg:.3f} s; traces of dE/dh_pp "
+                      + np.array2string(g1[:, diag].sum(1), precision=10))
             if a.density:
                 for rep in range(2):  # the first call also forms the configuration groups
                     t0 = time.perf_counter()

@@ -1263,7 +1263,7 @@ __device__ __forceinline__ bool det_connected(bool so, const uint64_t *aA, const
 
 // DIRECT (direct mode): segments over the full neighbour lists; instead of storing the kept
 // elements, Y[row, 0:kvec] += element * X[column, 0:kvec], added atomically per row.
-template <int W, bool DIRECT = false>
+template <int W, int DIRECT = 0>
 __global__ void __launch_bounds__(WARPS_PER_CTA * 32) k_hbuild_fast(Params P) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   FastSmem<W> *ws = reinterpret_cast<FastSmem<W> *>(smem_raw) + (threadIdx.x >> 5);
@@ -1446,7 +1446,7 @@ __global__ void __launch_bounds__(WARPS_PER_CTA * 32) k_hbuild_fast(Params P) {
         chunk_end = cursor + len;
       }
       double acc[8];
-      float accs[8], accc[8];  // direct mode with FP32 inputs: compensated FP32 sums
+      float accs[8], accc[8];  // DIRECT == 2: compensated FP32 sums of FP32 products
 #pragma unroll
       for (int q = 0; q < 8; ++q) { acc[q] = 0.0; accs[q] = 0.f; accc[q] = 0.f; }
       const unsigned long long base = cursor;
@@ -1481,7 +1481,7 @@ __global__ void __launch_bounds__(WARPS_PER_CTA * 32) k_hbuild_fast(Params P) {
           v = sef_elem<W>(P, pi, ws->K, flip ? t : r, flip ? r : t, conn, (DIRECT && pi.swap) ? nullptr : &rowA);
           keep = (fabs(v) >= PSOCI_MIN_VALUE) || (diag_blk && t == r);
           if (DIRECT) {
-            if (keep && P.dx32) {
+            if (DIRECT == 2 && keep) {
               const float vf = (float)v;
               const float4 *xr = reinterpret_cast<const float4 *>(P.dx32 + (pi.colbase + t) * 8);
               const float4 xa = __ldg(xr), xb = __ldg(xr + 1);
@@ -1511,7 +1511,7 @@ __global__ void __launch_bounds__(WARPS_PER_CTA * 32) k_hbuild_fast(Params P) {
         }
       }
       if (DIRECT) {
-        if (P.dx32) {
+        if (DIRECT == 2) {
 #pragma unroll
           for (int q = 0; q < 8; ++q) acc[q] = (double)accs[q] - (double)accc[q];
         }
@@ -2290,9 +2290,10 @@ psoci_status run_direct_sigma(psoci_ctx *c, int k, const double *dX, int ldx, do
   // only the elements that can be non-zero; otherwise the generic one
   const bool fast = c->max_ndet <= FAST_MAXDET;
   const size_t smem = fast ? sizeof(FastSmem<W>) * WARPS_PER_CTA : sizeof(WarpSmem) * WARPS_PER_CTA;
-  if (fast)
-    PSOCI_CUDA(c, cudaFuncSetAttribute(k_hbuild_fast<W, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  else
+  if (fast) {
+    PSOCI_CUDA(c, cudaFuncSetAttribute(k_hbuild_fast<W, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    PSOCI_CUDA(c, cudaFuncSetAttribute(k_hbuild_fast<W, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  } else
     PSOCI_CUDA(c, cudaFuncSetAttribute(k_hbuild<W, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>((P.nseg + WARPS_PER_CTA - 1) / WARPS_PER_CTA, 152 * 16));
   // MIXED (connectivity-marking kernel only): FP32 element x FP32 input products
@@ -2306,8 +2307,10 @@ psoci_status run_direct_sigma(psoci_ctx *c, int k, const double *dX, int ldx, do
       P.dx32 = x32;
     }
     psoci_note_launch();
-    if (fast)
-      k_hbuild_fast<W, true><<<blocks, WARPS_PER_CTA * 32, smem, st>>>(P);
+    if (fast && mixed)
+      k_hbuild_fast<W, 2><<<blocks, WARPS_PER_CTA * 32, smem, st>>>(P);
+    else if (fast)
+      k_hbuild_fast<W, 1><<<blocks, WARPS_PER_CTA * 32, smem, st>>>(P);
     else
       k_hbuild<W, 2><<<blocks, WARPS_PER_CTA * 32, smem, st>>>(P);
     PSOCI_CUDA(c, cudaGetLastError());

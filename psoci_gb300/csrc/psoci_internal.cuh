@@ -16,9 +16,9 @@
 #define PSOCI_SEG 32          // neighbours per warp segment in the H build
 #define PSOCI_MIN_VALUE 1.0e-8  // packSefsef threshold (PsociHamiltonian.hpp:37)
 // mixed-sigma kernel variants (sigma.cu) and the one used until psoci_autotune_sigma runs:
-// 16 lanes per row, 4 gathers in flight per lane (the fastest on the MRCISD blocks measured)
+// a warp per row, 4 gathers in flight per lane (variant 1, 2 in flight, measured within 1%)
 #define PSOCI_SIGMA_VARIANTS 6
-#define PSOCI_SIGMA_DEFAULT 2
+#define PSOCI_SIGMA_DEFAULT 0
 
 // ------------------------------------------------------------------------------------
 // host-side context
