@@ -734,6 +734,130 @@ psoci_status orthonormalize(Work &w, int m, int b, int *bk) {
 
 namespace {
 
+// Radix select of the M lowest diagonal elements on the device: doubles as order-preserving
+// 64-bit keys, eight 8-bit digit passes (256-bin histograms of the elements whose higher
+// digits match the prefix found so far) fix the M-th smallest key; the indices of the elements
+// at or below it (M plus ties) are collected and ordered on the host by (value, index).
+__device__ __forceinline__ uint64_t order_key(double v) {
+  const uint64_t b = (uint64_t)__double_as_longlong(v);
+  return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+}
+
+__global__ void k_radix_hist(int64_t n, const double *__restrict__ d, uint64_t prefix, uint64_t pmask, int shift,
+                             unsigned *__restrict__ hist) {
+  __shared__ unsigned h[256];
+  for (int i = threadIdx.x; i < 256; i += blockDim.x) h[i] = 0u;
+  __syncthreads();
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const uint64_t k = order_key(d[i]);
+    if ((k & pmask) == prefix) atomicAdd(&h[(k >> shift) & 255u], 1u);
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < 256; i += blockDim.x)
+    if (h[i]) atomicAdd(&hist[i], h[i]);
+}
+
+__global__ void k_select_le(int64_t n, const double *__restrict__ d, uint64_t kth, int64_t *__restrict__ out,
+                            unsigned long long *cnt, int64_t cap) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    if (order_key(d[i]) <= kth) {
+      const unsigned long long p = atomicAdd(cnt, 1ull);
+      if ((int64_t)p < cap) out[p] = i;
+    }
+}
+
+__global__ void k_gather_vals(int64_t m, const int64_t *__restrict__ idx, const double *__restrict__ d,
+                              double *__restrict__ out) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = d[idx[i]];
+}
+
+// the M lowest elements of the device array d[N], ordered by (value, index)
+psoci_status lowest_elements(psoci_ctx *c, const double *d, int64_t N, int M, std::vector<int64_t> &low) {
+  cudaStream_t st = c->stream;
+  low.clear();
+  auto host_path = [&]() -> psoci_status {
+    std::vector<double> h(N);
+    PSOCI_CUDA(c, cudaMemcpyAsync(h.data(), d, sizeof(double) * N, cudaMemcpyDeviceToHost, st));
+    PSOCI_CUDA(c, cudaStreamSynchronize(st));
+    std::vector<int64_t> order(N);
+    std::iota(order.begin(), order.end(), 0);
+    std::partial_sort(order.begin(), order.begin() + M, order.end(),
+                      [&](int64_t a, int64_t b) { return h[a] < h[b] || (h[a] == h[b] && a < b); });
+    low.assign(order.begin(), order.begin() + M);
+    return PSOCI_OK;
+  };
+  if (N <= 65536 || M < 1) return host_path();
+  const int64_t cap = 4 * (int64_t)M + 1024;
+  unsigned *hist = nullptr;
+  int64_t *idx = nullptr;
+  double *vals = nullptr;
+  unsigned long long *cnt = nullptr;
+  psoci_status s;
+  auto done = [&](psoci_status r) {
+    psoci_free(hist); psoci_free(idx); psoci_free(vals); psoci_free(cnt);
+    return r;
+  };
+  if ((s = psoci_alloc(c, &hist, 256)) || (s = psoci_alloc(c, &idx, cap)) || (s = psoci_alloc(c, &vals, cap)) ||
+      (s = psoci_alloc(c, &cnt, 1)))
+    return done(s);
+  const int blocks = (int)std::min<int64_t>((N + 255) / 256, 152 * 8);
+  uint64_t prefix = 0, pmask = 0;
+  int64_t rem = M;  // rank of the wanted key among the elements matching the prefix
+  unsigned h[256];
+  for (int shift = 56; shift >= 0; shift -= 8) {
+    cudaError_t e = cudaMemsetAsync(hist, 0, sizeof(unsigned) * 256, st);
+    if (e == cudaSuccess) {
+      psoci_note_launch();
+      k_radix_hist<<<blocks, 256, 0, st>>>(N, d, prefix, pmask, shift, hist);
+      e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h, hist, sizeof(h), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return done(psoci_cuda_fail(c, e, "davidson: guess selection"));
+    int64_t cum = 0;
+    int dig = 255;
+    for (int b = 0; b < 256; ++b) {
+      if (cum + (int64_t)h[b] >= rem) { dig = b; break; }
+      cum += h[b];
+    }
+    rem -= cum;
+    prefix |= (uint64_t)dig << shift;
+    pmask |= (uint64_t)255 << shift;
+  }
+  unsigned long long found = 0;
+  cudaError_t e = cudaMemsetAsync(cnt, 0, sizeof(unsigned long long), st);
+  if (e == cudaSuccess) {
+    psoci_note_launch();
+    k_select_le<<<blocks, 256, 0, st>>>(N, d, prefix, idx, cnt, cap);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&found, cnt, sizeof(found), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return done(psoci_cuda_fail(c, e, "davidson: guess selection"));
+  if ((int64_t)found > cap || (int64_t)found < M) {  // many ties: the host orders them all
+    done(PSOCI_OK);
+    return host_path();
+  }
+  std::vector<int64_t> cand(found);
+  std::vector<double> hv(found);
+  psoci_note_launch();
+  k_gather_vals<<<(unsigned)((found + 255) / 256), 256, 0, st>>>((int64_t)found, idx, d, vals);
+  e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaMemcpyAsync(cand.data(), idx, sizeof(int64_t) * found, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(hv.data(), vals, sizeof(double) * found, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return done(psoci_cuda_fail(c, e, "davidson: guess selection"));
+  done(PSOCI_OK);
+  std::vector<size_t> ord(found);
+  std::iota(ord.begin(), ord.end(), 0);
+  std::sort(ord.begin(), ord.end(),
+            [&](size_t a, size_t b) { return hv[a] < hv[b] || (hv[a] == hv[b] && cand[a] < cand[b]); });
+  low.resize(M);
+  for (int q = 0; q < M; ++q) low[q] = cand[ord[q]];
+  return PSOCI_OK;
+}
+
 constexpr int GUESS_M = 3072;  // order of the initial guess's block of H (lowest diagonal elements)
 
 // The solver over an operator of order N with diagonal diag (device): the context's
@@ -788,14 +912,9 @@ psoci_status davidson_run(psoci_ctx *c, int64_t N, const double *diag, const dou
 
   // guess: the lowest eigenvectors of H restricted to the M lowest diagonal elements (a
   // stored matrix), else unit vectors on the nr lowest diagonal elements
-  std::vector<double> hdiag(N);
-  PSOCI_CUDA(c, cudaMemcpyAsync(hdiag.data(), diag, sizeof(double) * N, cudaMemcpyDeviceToHost, st));
-  PSOCI_CUDA(c, cudaStreamSynchronize(st));
   const int M = inner ? nr : (int)std::min<int64_t>(GUESS_M, N);
-  std::vector<int64_t> order(N);
-  std::iota(order.begin(), order.end(), 0);
-  std::partial_sort(order.begin(), order.begin() + M, order.end(),
-                    [&](int64_t a, int64_t b) { return hdiag[a] < hdiag[b] || (hdiag[a] == hdiag[b] && a < b); });
+  std::vector<int64_t> order;
+  if ((s = lowest_elements(c, diag, N, M, order))) return s;
   psoci_prec prec = o->prec;
   bool refine_phase = (prec != PSOCI_PREC_MIXED);  // FP64 and FF iterate to rtol directly
   w.lowp = (prec == PSOCI_PREC_MIXED);

@@ -2805,10 +2805,11 @@ __device__ __forceinline__ int det_adj(const AdjPair<W> &pi, const DetBits<W> &A
 
 // vectors (k per pass, root-major with stride ldv, FP64) in the determinant basis:
 // CD[d * k + r], the transpose of ciout's transform (PsociHamiltonian.C:1457-1516)
+template <typename CT>
 __global__ void k_sef_to_det(int nconf, int nelec, int ksym, const int64_t *__restrict__ sefoff,
                              const int64_t *__restrict__ detoff, const int32_t *__restrict__ jsym,
                              const int32_t *__restrict__ nopen, const double *__restrict__ V, int64_t ldv, int k,
-                             double *__restrict__ CD) {
+                             CT *__restrict__ CD) {
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int i = (int)(t >> 5), lane = threadIdx.x & 31;
   if (i >= nconf) return;
@@ -2822,10 +2823,10 @@ __global__ void k_sef_to_det(int nconf, int nelec, int ksym, const int64_t *__re
     const int a = e / k, q = e - a * k;
     const double c = V[(int64_t)q * ldv + s0 + a];
     if (open) {
-      CD[(d0 + 2 * a) * k + q] = r * c;
-      CD[(d0 + 2 * a + 1) * k + q] = (m * r) * c;
+      CD[(d0 + 2 * a) * k + q] = (CT)(r * c);
+      CD[(d0 + 2 * a + 1) * k + q] = (CT)((m * r) * c);
     } else {
-      CD[(d0 + a) * k + q] = c;
+      CD[(d0 + a) * k + q] = (CT)c;
     }
   }
 }
@@ -2973,26 +2974,35 @@ __device__ __forceinline__ bool det_coupled(const AdjPair<W> &pi, const DetBits<
 }
 
 constexpr int ADJ_RT = 15;    // exchange terms held in registers (Kd[mm] of <= 6 open shells)
-constexpr int ADJ_CONN = 256; // coupled determinant pairs collected per round
+constexpr int ADJ_CONN = 128; // coupled determinant pairs collected per round
+
+// A coupled determinant pair of the pair being processed, classified: its determinants
+// (x << 16 | y), the det_adj tag, sign and term, and the exchange-term mask.
+struct AdjRec {
+  uint64_t mask;
+  uint32_t xy;
+  int32_t info;  // tag | (sgn < 0) << 4 | term << 8
+};
 
 // One warp per row configuration I (grid-stride); its lower neighbours J <= I in chunks of
-// 32 set up by the lanes.  Per pair: (1) lanes test the determinant pairs (x, y) for coupling
-// and collect the coupled ones in shared memory; (2) lanes = (slot, root) classify the
-// collected pairs, slots over the pairs and roots over the lanes of a slot, and add
-// s * cd_I[x] * cd_J[y] to register accumulators of the pair's terms (v0, v1, and the
-// exchange terms X[t] / Kd[mm]; terms beyond ADJ_RT, only on diagonals of 7+ open shells, go
-// to shared-memory atomics); (3) the slots' sums are reduced by shuffles and the root lanes
-// scatter the pair's terms to the tables.  ACC: the accumulator type (FP64, or FP32 sums
-// within a pair).
-template <int W, typename ACC>
+// 32 set up by the lanes.  Per pair: (1) lanes over the determinant pairs (x, y) test them for
+// coupling and classify the coupled ones (det_adj), collecting the records in shared memory;
+// (2) lanes = (slot, root) take the records, slots over the records and roots over the lanes
+// of a slot, and add s * cd_I[x] * cd_J[y] to register accumulators of the pair's terms (v0,
+// v1, and the exchange terms X[t] / Kd[mm]; terms beyond ADJ_RT, only on diagonals of 7+ open
+// shells, go to shared-memory atomics); (3) the slots' sums are reduced by shuffles and the
+// root lanes scatter the pair's terms to the tables.  CT/ACC: the type of the determinant-
+// basis vectors and of the sums within a pair (FP64, or FP32 for the FP32-bulk variant).
+template <int W, typename CT, typename ACC>
 __global__ void __launch_bounds__(ADJ_WARPS * 32) k_energy_grad(Params P, const int64_t *__restrict__ nbroff,
                                                                 const int32_t *__restrict__ nbr,
-                                                                const double *__restrict__ CD, int k, double *G1,
+                                                                const CT *__restrict__ CD, int k, double *G1,
                                                                 int64_t n1, double *G2, int64_t n2) {
   __shared__ AdjSmem<W> sm[ADJ_WARPS];
-  __shared__ uint32_t conn[ADJ_WARPS][ADJ_CONN];
+  __shared__ AdjRec recs[ADJ_WARPS][ADJ_CONN];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   AdjSmem<W> &S = sm[wib];
+  AdjRec *rec = recs[wib];
   const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
   // lanes of one slot hold consecutive roots: kp (a power of two >= k) roots per slot
@@ -3014,78 +3024,90 @@ __global__ void __launch_bounds__(ADJ_WARPS * 32) k_energy_grad(Params P, const 
       for (int u = 0; u < np; ++u) {
         const AdjPair<W> &pi = S.pi[u];
         if (pi.kind == K_NONE) continue;
+        const double fpair = (pi.A == pi.B) ? 1.0 : 2.0;
+        const int nterm = (pi.kind == K_SINGLE) ? pi.nopenA
+                          : (pi.kind == K_DIAG) ? min(ADJ_RT, pi.nopenA * (pi.nopenA - 1) / 2) : 0;
         ACC a0 = 0, a1 = 0, aT[ADJ_RT];
 #pragma unroll
         for (int t = 0; t < ADJ_RT; ++t) aT[t] = 0;
-        bool spill = false;  // terms beyond ADJ_RT went to shared memory
         const int nd = pi.ndetA * pi.ndetB;
         for (int e0 = 0; e0 < nd;) {
-          // (1) collect coupled determinant pairs (up to ADJ_CONN per round)
+          // (1) classify the determinant pairs, one a lane; keep the coupled ones
           int nc = 0;
           while (e0 < nd && nc + 32 <= ADJ_CONN) {
             const int e = e0 + lane;
-            bool cp = false;
-            int x = 0, y = 0;
+            int tag = T_NONE, sgn = 1, term = 0, x = 0, y = 0;
+            uint64_t mask = 0ull;
             if (e < nd) {
               x = e / pi.ndetB;
               y = e - x * pi.ndetB;
               DetBits<W> Ad, Bd;
               load_det<W>(Ad, P.alpha, P.beta, P.phase, P.nalpha, pi.detA + x);
               load_det<W>(Bd, P.alpha, P.beta, P.phase, P.nalpha, pi.detB + y);
-              cp = det_coupled<W>(pi, Ad, Bd);
+              if (det_coupled<W>(pi, Ad, Bd)) {
+                int64_t direct = 0;
+                tag = det_adj<W>(pi, Ad, Bd, sgn, mask, term, direct);
+                if (tag == T_DIRECT) {
+                  // an integral outside the pair's terms (not met in practice): added here
+                  for (int rr = 0; rr < k; ++rr)
+                    atomicAdd(G2 + (int64_t)rr * n2 + direct,
+                              fpair * sgn * (double)CD[(pi.detA + x) * k + rr] * (double)CD[(pi.detB + y) * k + rr]);
+                  tag = T_NONE;
+                }
+              }
             }
-            const unsigned cb = __ballot_sync(0xffffffffu, cp);
-            if (cp) conn[wib][nc + __popc(cb & ((1u << lane) - 1u))] = ((uint32_t)x << 16) | (uint32_t)y;
+            const bool keep = tag != T_NONE;
+            const unsigned cb = __ballot_sync(0xffffffffu, keep);
+            if (keep) {
+              AdjRec &R = rec[nc + __popc(cb & ((1u << lane) - 1u))];
+              R.mask = mask;
+              R.xy = ((uint32_t)x << 16) | (uint32_t)y;
+              R.info = tag | ((sgn < 0) ? 16 : 0) | (term << 8);
+            }
             nc += __popc(cb);
             e0 += 32;
           }
           __syncwarp();
-          // (2) classify and accumulate, slots over the collected pairs
-          for (int cq = slot; cq < nc; cq += nslot) {
-            const uint32_t xy = conn[wib][cq];
-            const int x = (int)(xy >> 16), y = (int)(xy & 0xffffu);
-            DetBits<W> Ad, Bd;
-            load_det<W>(Ad, P.alpha, P.beta, P.phase, P.nalpha, pi.detA + x);
-            load_det<W>(Bd, P.alpha, P.beta, P.phase, P.nalpha, pi.detB + y);
-            int sgn = 1, term = 0;
-            uint64_t mask = 0ull;
-            int64_t direct = 0;
-            const int tag = det_adj<W>(pi, Ad, Bd, sgn, mask, term, direct);
-            if (tag == T_NONE || !rok) continue;
-            const ACC w = (ACC)(sgn * __ldg(CD + (pi.detA + x) * k + r) * __ldg(CD + (pi.detB + y) * k + r));
-            if (tag == T_V0) a0 += w;
-            else if (tag == T_V1) a1 += w;
-            else if (tag == T_V0MV1) { a0 += w; a1 -= w; }
-            else if (tag == T_SGL || tag == T_DIAG) {
-              a0 += w;
+          // (2) accumulate, slots over the records, roots over the lanes of a slot
+          if (rok) {
+            for (int cq = slot; cq < nc; cq += nslot) {
+              const AdjRec R = rec[cq];
+              const int x = (int)(R.xy >> 16), y = (int)(R.xy & 0xffffu);
+              const int tag = R.info & 15, term = R.info >> 8;
+              ACC w = (ACC)__ldg(CD + (pi.detA + x) * k + r) * (ACC)__ldg(CD + (pi.detB + y) * k + r);
+              if (R.info & 16) w = -w;
+              if (tag == T_V0) a0 += w;
+              else if (tag == T_V1) a1 += w;
+              else if (tag == T_V0MV1) { a0 += w; a1 -= w; }
+              else if (tag == T_SGL || tag == T_DIAG) {
+                a0 += w;
 #pragma unroll
-              for (int t = 0; t < ADJ_RT; ++t)
-                if ((mask >> t) & 1ull) aT[t] -= w;
-              uint64_t m = mask >> ADJ_RT;
-              while (m) {
-                const int t = ADJ_RT + __ffsll((long long)m) - 1;
-                m &= m - 1;
-                atomicAdd(&S.acc[2 + t][r], -(double)w);
-                spill = true;
-              }
-            } else if (tag == T_X || tag == T_K) {
-              if (term < ADJ_RT) {
+                for (int t = 0; t < ADJ_RT; ++t) {
+                  if (t >= nterm) break;  // uniform over the warp
+                  if ((R.mask >> t) & 1ull) aT[t] -= w;
+                }
+                uint64_t m = R.mask >> ADJ_RT;
+                while (m) {
+                  const int t = ADJ_RT + __ffsll((long long)m) - 1;
+                  m &= m - 1;
+                  atomicAdd(&S.acc[2 + t][r], -(double)w);
+                }
+              } else {  // T_X, T_K
+                if (term < ADJ_RT) {
 #pragma unroll
-                for (int t = 0; t < ADJ_RT; ++t)
-                  if (t == term) aT[t] += w;
-              } else {
-                atomicAdd(&S.acc[2 + term][r], (double)w);
-                spill = true;
+                  for (int t = 0; t < ADJ_RT; ++t) {
+                    if (t >= nterm) break;
+                    if (t == term) aT[t] += w;
+                  }
+                } else {
+                  atomicAdd(&S.acc[2 + term][r], (double)w);
+                }
               }
-            } else {
-              atomicAdd(G2 + (int64_t)r * n2 + direct, ((pi.A == pi.B) ? 1.0 : 2.0) * (double)w);
             }
           }
           __syncwarp();
         }
         // (3) sums over the slots (lanes r, r + kp, r + 2kp, ...): lanes of slot 0 hold them
-        const int nterm = (pi.kind == K_SINGLE) ? pi.nopenA
-                          : (pi.kind == K_DIAG) ? min(ADJ_RT, pi.nopenA * (pi.nopenA - 1) / 2) : 0;
         double s0 = (double)a0, s1 = (double)a1, sT[ADJ_RT];
 #pragma unroll
         for (int t = 0; t < ADJ_RT; ++t) sT[t] = (double)aT[t];
@@ -3096,7 +3118,6 @@ __global__ void __launch_bounds__(ADJ_WARPS * 32) k_energy_grad(Params P, const 
           for (int t = 0; t < ADJ_RT; ++t)
             if (t < nterm) sT[t] += __shfl_xor_sync(0xffffffffu, sT[t], o);
         }
-        (void)spill;
         __syncwarp();  // the shared-memory terms (spilled atomics) are complete
         if (lane < k) {
           S.acc[0][lane] = s0;
@@ -3106,7 +3127,7 @@ __global__ void __launch_bounds__(ADJ_WARPS * 32) k_energy_grad(Params P, const 
             if (t < nterm) S.acc[2 + t][lane] = sT[t];
         }
         __syncwarp();
-        adj_scatter<W>(P, pi, S.acc, k, (pi.A == pi.B) ? 1.0 : 2.0, G1, n1, G2, n2, lane);
+        adj_scatter<W>(P, pi, S.acc, k, fpair, G1, n1, G2, n2, lane);
         __syncwarp();
         const int used = 2 + ((pi.kind == K_DIAG) ? pi.nopenA * (pi.nopenA - 1) / 2 : pi.nopenA);
         for (int e = lane; e < used * ADJ_MAXR; e += 32) (&S.acc[0][0])[e] = 0.0;
@@ -3172,23 +3193,29 @@ psoci_status run_energy_grad(psoci_ctx *c, int k, const double *dV, int64_t ldv,
     c->grad_mode = mode;
     c->grad_npairs = npairs;
   }
-  double *CD = nullptr;
+  double *CD = nullptr;  // determinant-basis vectors (FP64, or FP32 for the FP32-bulk variant)
   if ((s = psoci_alloc(c, &CD, (size_t)c->ndet_total * std::min(k, ADJ_MAXR)))) return s;
+  float *CD32 = reinterpret_cast<float *>(CD);
   PSOCI_CUDA(c, cudaMemsetAsync(dG1, 0, sizeof(double) * n1 * k, st));
   PSOCI_CUDA(c, cudaMemsetAsync(dG2, 0, sizeof(double) * n2 * k, st));
   const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>(((int64_t)n + ADJ_WARPS - 1) / ADJ_WARPS, 152 * 16));
   for (int r0 = 0; r0 < k; r0 += ADJ_MAXR) {
     const int kk = std::min(ADJ_MAXR, k - r0);
-    psoci_note_launch();
-    k_sef_to_det<<<(unsigned)(((int64_t)n * 32 + 255) / 256), 256, 0, st>>>(
-        n, c->nelec, c->ksym, c->d_sefoff, c->d_detoff, c->d_jsym, c->d_nopen, dV + (int64_t)r0 * ldv, ldv, kk, CD);
+    const unsigned sb = (unsigned)(((int64_t)n * 32 + 255) / 256);
     psoci_note_launch();
     if (prec == PSOCI_PREC_MIXED)
-      k_energy_grad<W, float><<<blocks, ADJ_WARPS * 32, 0, st>>>(P, c->grad_nbroff, c->grad_nbr, CD, kk,
-                                                                 dG1 + r0 * n1, n1, dG2 + r0 * n2, n2);
+      k_sef_to_det<float><<<sb, 256, 0, st>>>(n, c->nelec, c->ksym, c->d_sefoff, c->d_detoff, c->d_jsym, c->d_nopen,
+                                              dV + (int64_t)r0 * ldv, ldv, kk, CD32);
     else
-      k_energy_grad<W, double><<<blocks, ADJ_WARPS * 32, 0, st>>>(P, c->grad_nbroff, c->grad_nbr, CD, kk,
-                                                                  dG1 + r0 * n1, n1, dG2 + r0 * n2, n2);
+      k_sef_to_det<double><<<sb, 256, 0, st>>>(n, c->nelec, c->ksym, c->d_sefoff, c->d_detoff, c->d_jsym, c->d_nopen,
+                                               dV + (int64_t)r0 * ldv, ldv, kk, CD);
+    psoci_note_launch();
+    if (prec == PSOCI_PREC_MIXED)
+      k_energy_grad<W, float, float><<<blocks, ADJ_WARPS * 32, 0, st>>>(P, c->grad_nbroff, c->grad_nbr, CD32, kk,
+                                                                        dG1 + r0 * n1, n1, dG2 + r0 * n2, n2);
+    else
+      k_energy_grad<W, double, double><<<blocks, ADJ_WARPS * 32, 0, st>>>(P, c->grad_nbroff, c->grad_nbr, CD, kk,
+                                                                          dG1 + r0 * n1, n1, dG2 + r0 * n2, n2);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) {
       psoci_free(CD);
