@@ -34,6 +34,12 @@ sys.path.insert(0, ROOT)
 # a smaller case of the same space, scaled to the full launch by the units processed; the
 # captures and the scaling are summarised under profiles/.
 TRAFFIC = {("k_hbuild_fast", "mrcisd_6e8o_v64"): 1.76e10, ("k_spmm_mixed", "mrcisd_6e8o_v64"): 1.91e10}
+# Warp instructions one launch of the element kernel issues (smsp__inst_executed.sum, a
+# one-pass ncu capture of that launch at the benchmark block; profiles/).  The kernel is bound
+# by instruction issue, so its roofline is issued instructions per second against the SMs'
+# issue peak: 152 SMs x 4 schedulers x 1 warp instruction per clock at the sampled SM clock.
+INST_PER_LAUNCH = {("k_hbuild_fast", "mrcisd_6e8o_v64"): 151807793810}
+SM_COUNT, ISSUE_PER_SM_CLK = 152, 4
 
 NROOTS = 8
 RTOL = 1e-5          # residual norm; |dE| ~ r^2/gap, well inside 1e-7 Eh (checked below)
@@ -255,6 +261,8 @@ def run_ours(args):
     del V, Dd
 
     hbm, peak_kind = peaks()
+    clocks_now = clk.summary()
+    sm_hz = (clocks_now["sm_mhz"] or 2070.0) * 1e6
     # dominant kernel: the element evaluation of the H build (k_hbuild_fast), timed by the
     # library's CUDA events on its stream in every timed mixed step.  Algorithmic bytes: the
     # reference's stored lower triangle (values 8 + columns 4 per element, row pointers 8
@@ -264,6 +272,16 @@ def run_ours(args):
     eval_s = float(np.mean([b["evaluate_ms"] for b in bstats])) * 1e-3
     b_eval = bs["nnz_lower"] * (8 + 4) + (N + 1) * 8 + p.nconf * (2 * 8 + 8) + one.nbytes + p.eri.nbytes
     ach_e = b_eval / eval_s / 1e9
+    inst = INST_PER_LAUNCH.get(("k_hbuild_fast", args.workload))
+    issue_peak = SM_COUNT * ISSUE_PER_SM_CLK * sm_hz
+    roofline_issue = {"kernel": "k_hbuild_fast (H build element evaluation, lower blocks)", "bound": "issue",
+                      "achieved": round(inst / eval_s / 1e9, 1) if inst else None, "peak": round(issue_peak / 1e9, 1),
+                      "unit": "G warp-instructions/s", "frac": round(inst / eval_s / issue_peak, 4) if inst else None,
+                      "traffic": TRAFFIC.get(("k_hbuild_fast", args.workload)), "peak_kind": "152 SMs x 4 issue/clk x "
+                      "sampled SM clock", "instructions_per_launch": inst, "launch_s": round(eval_s, 6),
+                      "instructions_per_lower_element": round(inst / bs["nnz_lower"], 1) if inst else None,
+                      "elements_per_s": round(bs["nnz_lower"] / eval_s, 1),
+                      "note": "issued warp instructions (ncu, one pass, this launch) over the CUDA-event launch time"}
     # sigma: values + column indices + row pointers + x gathered once per row of the block +
     # y written (mixed: FP32 x staged from FP64, conversion kernel included)
     b_mixed = nnz * (4 + 4) + (N + 1) * 8 + N * k * (8 + 4 + 4 + 8)
@@ -336,16 +354,22 @@ def run_ours(args):
                                "iterations": rr.iterations, "sigma_vectors": rr.sigma_calls,
                                "refine_iters": rr.refine_iters, "sigma_s": round(rr.sigma_seconds, 6)},
             "evals": [float(x) for x in r_mixed.evals],
-            "roofline": {"kernel": "k_hbuild_fast (H build element evaluation, lower blocks)", "bound": "hbm",
-                         "achieved": round(ach_e, 2), "peak": hbm, "unit": "GB/s", "frac": round(ach_e / hbm, 5),
-                         "traffic": TRAFFIC.get(("k_hbuild_fast", args.workload)), "peak_kind": peak_kind,
-                         "bytes_per_launch": int(b_eval), "launch_s": round(eval_s, 6),
-                         "elements_per_s": round(bs["nnz_lower"] / eval_s, 1),
-                         "note": "issue-bound (integer ALU, FP64 pipe, L2 gathers), not HBM-bound"},
+            "roofline": roofline_issue,
+            "roofline_hbm_element": {"kernel": "k_hbuild_fast", "bound": "hbm", "achieved": round(ach_e, 2),
+                                     "peak": hbm, "unit": "GB/s", "frac": round(ach_e / hbm, 5),
+                                     "traffic": TRAFFIC.get(("k_hbuild_fast", args.workload)), "peak_kind": peak_kind,
+                                     "bytes_per_launch": int(b_eval), "launch_s": round(eval_s, 6),
+                                     "note": "the element kernel's algorithmic bytes against HBM: not its bound"},
             "roofline_sigma": {"kernel": "k_spmm_mixed<8> (sigma, 8 vectors, timed alone)", "bound": "hbm",
                                "achieved": round(ach_m, 1), "peak": hbm, "unit": "GB/s", "frac": round(ach_m / hbm, 4),
                                "traffic": TRAFFIC.get(("k_spmm_mixed", args.workload)), "peak_kind": peak_kind,
-                               "bytes_per_launch": int(b_mixed), "launch_s": sig["mixed"]},
+                               "bytes_per_launch": int(b_mixed), "launch_s": sig["mixed"],
+                               "l2_gather_bytes_per_launch": int(nnz * 32),
+                               "l2_gather_gbs": round(nnz * 32 / sig["mixed"] / 1e9, 1),
+                               "note": "bound by L2 gathers, not HBM: one 32-byte input row (8 FP32 vectors) per "
+                                       "stored element, about one element per column of a configuration-pair block, so "
+                                       "rows are rarely reused; ncu lts__throughput 79% of peak at mrcisd_6e8o_v24 "
+                                       "(profiles/)"},
             "roofline_fp64_sigma": {"achieved": round(ach_d, 1), "frac": round(ach_d / hbm, 4),
                                     "bytes_per_launch": int(b_fp64), "launch_s": sig["fp64"]},
             "h_build_ms": {k: round(bs[k], 3) for k in ("screen_ms", "evaluate_ms", "rows_ms", "assemble_ms",
