@@ -1,7 +1,7 @@
 """Solve one double-group symmetry block of a named synthetic workload on one GPU.
 
   python -m psoci_gb300 --workload mrcisd_6e8o_v24 [--roots 8] [--rtol 1e-5] [--fp64]
-                        [--no-davidson] [--sigma K] [--density] [--gradient] [--verbose 1]
+                        [--no-davidson] [--sigma K] [--density] [--gradient] [--direct] [--verbose 1]
 
 Determinants -> Hamiltonian (CSR) -> block Davidson; prints the sizes and the total
 energies in the layout of the reference driver's "Eigenvalue" lines.  ``--sigma K`` also
@@ -9,7 +9,8 @@ applies H to K random vectors once (the Davidson's inner product, on its own);
 ``--density`` forms the 1-particle densities of the converged roots and prints the
 natural-orbital occupations of the first root (diagonal blocks of one orbital label);
 ``--gradient`` forms dE/d(integral tables) of the converged roots (1-, 2-particle and
-spin-orbit densities, derivatives of the non-zero integrals).
+spin-orbit densities, derivatives of the non-zero integrals); ``--direct`` stores no matrix
+elements (every product evaluates them again).
 """
 from __future__ import annotations
 
@@ -34,6 +35,7 @@ def main(argv=None):
     ap.add_argument("--sigma", type=int, default=0, help="apply H to this many random vectors once")
     ap.add_argument("--density", action="store_true", help="1-particle densities of the roots")
     ap.add_argument("--gradient", action="store_true", help="energy gradients of the roots")
+    ap.add_argument("--direct", action="store_true", help="direct mode: no stored elements")
     ap.add_argument("--max-subspace", type=int, default=48)
     ap.add_argument("--device", type=int, default=0)
     ap.add_argument("--verbose", type=int, default=0)
@@ -44,7 +46,7 @@ def main(argv=None):
         c.load_problem(p)
         t0 = time.perf_counter()
         c.build_determinants()
-        nnz = c.build_hamiltonian(mixed=mixed)
+        nnz = c.build_hamiltonian(mixed=mixed, direct=a.direct)
         tb = time.perf_counter() - t0
         print(f"workload {a.workload}: configurations {p.nconf}, SEFs {c.nsef}, stored elements {nnz}, "
               f"build {tb:.3f} s")

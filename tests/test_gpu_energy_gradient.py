@@ -129,3 +129,30 @@ def test_gradcheck_fci_6e12o():
         fd = (ev[0] - ev[1]) / (2 * h)
         an = (g1 if tab == "one" else g2)[:, t]
         assert np.abs(fd - an).max() <= 1e-6, (tab, t, fd, an)
+
+
+def test_gradient_feeds_natural_orbitals(oracle_mod):
+    """The spin-free part of dE/dh (diagonal as it is, equal-irrep off-diagonal halved) is the
+    CIDEN density, so its natural orbitals are those of psoci_density1."""
+    from psoci_gb300 import api
+    from psoci_gb300.inputs import tri
+
+    p = small_problem("fci_6e8o", 1)
+    O = oracle_mod.Oracle(p)
+    _, v = _eigvecs(O, 2)
+    c = gpu_context(p)
+    g1, _ = c.energy_gradient(v)
+    D = c.density1(v)
+    n = p.nbf
+    for r in range(2):
+        d = np.zeros_like(g1[r])
+        for a in range(n):
+            d[tri(a, a)] = g1[r, tri(a, a)]
+            for b in range(a):
+                if p.irreps[a] == p.irreps[b]:
+                    d[tri(a, b)] = 0.5 * g1[r, tri(a, b)]
+        occ_g, _ = api.natural_orbitals(d, p.irreps)
+        occ_d, _ = api.natural_orbitals(D[r], p.irreps)
+        assert np.abs(np.sort(occ_g) - np.sort(occ_d)).max() <= 1e-10
+        assert abs(occ_g.sum() - p.nelec) <= 1e-10
+    c.close()
