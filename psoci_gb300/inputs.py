@@ -317,8 +317,8 @@ def named_workload(name: str, seed: int = 0, ksym: int = 1) -> Problem:
         "mrcisd_4e6o_v60": ("mrcisd", dict(nact=6, nelec=4, nvirt=60)),
         # scaled MRCISD: CAS(6e,8o) + singles and doubles into 64 virtuals (~3.8M SEFs)
         "mrcisd_6e8o_v64": ("mrcisd", dict(nact=8, nelec=6, nvirt=64)),
-        # the same into 112 virtuals (11.6M SEFs, 120 orbitals): its stored matrix and the
-        # build's working set exceed one GPU's memory, the direct-mode case
+        # the same into 112 virtuals (11.6M SEFs, 120 orbitals): about 8.4e9 stored elements
+        # (135 GB with the FP32 copy, plus the build's working set); the direct-mode case
         "mrcisd_6e8o_v112": ("mrcisd", dict(nact=8, nelec=6, nvirt=112)),
         # small cases for tests
         "fci_4e6o": ("fci", dict(nbf=6, nelec=4)),
