@@ -224,6 +224,7 @@ def run_ours(args):
             torch.cuda.synchronize(dev)
             ts.append(a.elapsed_time(b) * 1e-3)
         sig[name] = float(np.mean(ts))
+    tsprod = tsprod_timing(ctx, stream, torch, dev, N)
     # 1-particle density (the reference's CIDEN path) of 8 unit vectors: outside the
     # headline step; the first call also forms the configuration groups
     ntri = p.nbf * (p.nbf + 1) // 2
@@ -377,6 +378,7 @@ def run_ours(args):
             "h_build_counts": {k: int(bs[k]) for k in ("candidates", "pairs", "segments", "nnz", "nnz_lower",
                                                         "slab_slots", "evaluations")},
             "energy_gradient": grad,
+            "projection_methods": tsprod,
             "density1": {"s": round(den_s, 6), "first_call_s": round(den_first, 6), "roots": NROOTS,
                          "trace_err": den_trace_err, "cpu_estimate": cpu_den,
                          "note": "CIDEN 1-particle density of 8 unit vectors, device pointers, mean of 5 "
@@ -517,6 +519,36 @@ def direct_mode(p, nnz_stored, device, torch, evals_stored):
                                  "30M_sefs": round(davidson_bytes(30_000_000) / 1e9, 2)}
     out["note"] = ("products: FP64, or FP32 element x FP32 input with compensated FP32 sums (mixed); "
                    "effective bandwidth is stored-equivalent bytes / time, not a physical HBM figure")
+    return out
+
+
+def tsprod_timing(ctx, stream, torch, dev, N, m=40, k=8):
+    """The Davidson's projection C = V^T W (N x 40 against N x 8, FP64 inputs) by the three
+    methods of psoci_tsprod — float-float on the FP32 pipe (the solver's), FP64 FMA, FP64
+    tensor-core MMA — CUDA events on the library stream, mean of 5 after 2 warm-up runs; and
+    each result's largest difference from the FP64 FMA one."""
+    A = torch.randn(N, m, dtype=torch.float64, device=dev)
+    B = torch.randn(N, k, dtype=torch.float64, device=dev)
+    C = [torch.empty(m, k, dtype=torch.float64, device=dev) for _ in range(3)]
+    out = {"n": N, "m": m, "k": k, "flops": 2 * N * m * k, "bytes": N * (m + k) * 8}
+    for method, name in ((0, "float_float"), (1, "fp64_fma"), (2, "fp64_mma")):
+        for _ in range(2):
+            ctx.tsprod_device(method, N, A.data_ptr(), m, m, B.data_ptr(), k, k, C[method].data_ptr())
+        ts = []
+        for _ in range(5):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize(dev)
+            a.record(stream)
+            ctx.tsprod_device(method, N, A.data_ptr(), m, m, B.data_ptr(), k, k, C[method].data_ptr())
+            b.record(stream)
+            torch.cuda.synchronize(dev)
+            ts.append(a.elapsed_time(b) * 1e-3)
+        t = float(np.mean(ts))
+        out[name] = {"ms": round(t * 1e3, 4), "tflops": round(out["flops"] / t / 1e12, 3),
+                     "gbs": round(out["bytes"] / t / 1e9, 1)}
+    for method, name in ((0, "float_float"), (2, "fp64_mma")):
+        out[name]["max_abs_diff_vs_fp64_fma"] = float((C[method] - C[1]).abs().max().item())
+    del A, B, C
     return out
 
 

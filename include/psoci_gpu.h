@@ -233,6 +233,15 @@ PSOCI_API psoci_status psoci_davidson_batch(psoci_ctx *const *ctxs, int nblocks,
                                             double *const *evals, double *const *evecs, double *const *rnorms,
                                             psoci_dav_stats *stats, psoci_status *block_status);
 
+/* Tall-skinny projection C = A^T B on device memory — the product behind
+ * PsociGAsubspace::generateIncrementalSubspace (PsociGAsubspace.C:273-366) — by one of three
+ * methods: 0 float-float sums on the FP32 pipe (what psoci_davidson runs), 1 FP64 FMA, 2 FP64
+ * tensor-core MMA (mma.sync m8n8k4 .f64).  A: n x m (row stride lda), B: n x k (row stride ldb),
+ * C: m x k row-major; 1 <= m <= 40, 1 <= k <= 8.  Runs on the context's stream and returns
+ * when C is written.  For measuring the methods against one another. */
+PSOCI_API psoci_status psoci_tsprod(psoci_ctx *ctx, int method, int64_t n, const double *dA, int lda, int m,
+                                    const double *dB, int ldb, int k, double *dC);
+
 /* Step-level Davidson: the basis and subspace of the reference's own loop
  * (driver.PSOCI.splittest.C:1186-1311), held on the device between calls so that a host
  * program keeps that loop as it is.  One basis per context: V and H*V (N x max_vectors), the

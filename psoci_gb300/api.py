@@ -94,6 +94,8 @@ SIGNATURES = {
     "psoci_set_guess": (ctypes.c_int, [_P, ctypes.c_int, _DP]),
     "psoci_density1": (ctypes.c_int, [_P, ctypes.c_int, _DP, _DP]),
     "psoci_density1_device": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p]),
+    "psoci_tsprod": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int64, ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
+                                    ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p]),
     "psoci_autotune_sigma": (ctypes.c_int, [_P, ctypes.c_int, _IP, ctypes.POINTER(ctypes.c_float)]),
     "psoci_davidson_batch": (ctypes.c_int, [ctypes.POINTER(_P), ctypes.c_int, ctypes.POINTER(DavOpts),
                                             ctypes.POINTER(_DP), ctypes.POINTER(_DP), ctypes.POINTER(_DP),
@@ -335,6 +337,12 @@ class Context:
         the context's stream."""
         self._check(self.lib.psoci_density1_device(self.ctx, k, ctypes.c_void_p(dV_ptr), ldv,
                                                    ctypes.c_void_p(dD_ptr)), "density1_device")
+
+    def tsprod_device(self, method: int, n: int, dA: int, lda: int, m: int, dB: int, ldb: int, k: int, dC: int):
+        """C (m x k) = A^T B on device pointers by method 0 (float-float), 1 (FP64 FMA) or 2
+        (FP64 tensor-core MMA)."""
+        self._check(self.lib.psoci_tsprod(self.ctx, method, n, ctypes.c_void_p(dA), lda, m, ctypes.c_void_p(dB), ldb,
+                                          k, ctypes.c_void_p(dC)), "tsprod")
 
     def autotune_sigma(self, k: int = 8):
         """Pick the fastest mixed-sigma variant for this Hamiltonian: (choice, ms per variant)."""

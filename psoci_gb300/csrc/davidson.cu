@@ -1616,3 +1616,144 @@ psoci_status psoci_basis_vectors(psoci_ctx *c, int k, double *vecs) {
 }
 
 }  // extern "C"
+
+// ------------------------------------------------------------------------------------
+// Tall-skinny projection C = A^T B three ways, for measuring the choice the Davidson makes
+// (generateIncrementalSubspace, PsociGAsubspace.C:273-366): float-float on the FP32 pipe (the
+// solver's k_tn), plain FP64 FMA, and FP64 tensor-core MMA (mma.sync m8n8k4 .f64 — the FP64
+// matrix instruction sm_103a offers; tcgen05 has no FP64 kind).
+// ------------------------------------------------------------------------------------
+namespace {
+
+constexpr int TP_THREADS = 256;
+
+// FP64 FMA: thread (i, sub) accumulates row i of C (k <= 8 outputs) over the rows sub,
+// sub + S, ... of its block's range; B's rows are read from global memory (8 consecutive
+// doubles, broadcast within the warp), the sub shares added in FP64 in shared memory.
+__global__ void __launch_bounds__(TP_THREADS) k_tn_f64(int64_t n, const double *__restrict__ A, int lda, int m,
+                                                       const double *__restrict__ B, int ldb, int k,
+                                                       double *__restrict__ partial, int64_t rows_per_blk) {
+  __shared__ double red[TP_THREADS][8];
+  const int tid = threadIdx.x;
+  const int S = TP_THREADS / m;
+  const int i = tid % m, sub = tid / m;
+  double acc[8];
+#pragma unroll
+  for (int j = 0; j < 8; ++j) acc[j] = 0.0;
+  const int64_t r0 = (int64_t)blockIdx.x * rows_per_blk, r1 = min(n, r0 + rows_per_blk);
+  if (sub < S)
+    for (int64_t r = r0 + sub; r < r1; r += S) {
+      const double a = __ldg(A + r * lda + i);
+      const double *br = B + r * ldb;
+#pragma unroll
+      for (int j = 0; j < 8; ++j)
+        if (j < k) acc[j] = fma(a, __ldg(br + j), acc[j]);
+    }
+#pragma unroll
+  for (int j = 0; j < 8; ++j) red[tid][j] = (sub < S) ? acc[j] : 0.0;
+  __syncthreads();
+  for (int e = tid; e < m * k; e += TP_THREADS) {
+    const int ii = e / k, j = e - ii * k;
+    double s = 0.0;
+    for (int q = 0; q < S; ++q) s += red[q * m + ii][j];
+    partial[(int64_t)blockIdx.x * m * k + e] = s;
+  }
+}
+
+// FP64 MMA: each warp sums C over its rows in steps of 4 with mma.sync.m8n8k4 (A^T's 8 x 4
+// fragment: lane (i = lane / 4, kk = lane % 4) holds A[r + kk, 8t + i]; B's 4 x 8 fragment:
+// lane (kk = lane % 4, j = lane / 4) holds B[r + kk, j]; the accumulator: lane holds C[8t +
+// lane / 4, 2 (lane % 4) + {0, 1}]), one accumulator pair per 8-row tile of C (m <= 40: 5).
+__global__ void __launch_bounds__(TP_THREADS) k_tn_dmma(int64_t n, const double *__restrict__ A, int lda, int m,
+                                                        const double *__restrict__ B, int ldb, int k,
+                                                        double *__restrict__ partial, int64_t rows_per_warp,
+                                                        int64_t nwarps) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (warp >= nwarps) return;  // whole warps: the last block's spare warps
+  const int mt = (m + 7) / 8;
+  double c[5][2];
+#pragma unroll
+  for (int t = 0; t < 5; ++t) { c[t][0] = 0.0; c[t][1] = 0.0; }
+  const int64_t r0 = warp * rows_per_warp, r1 = min(n, r0 + rows_per_warp);
+  const int kk = lane & 3, hi = lane >> 2;
+  for (int64_t r = r0; r < r1; r += 4) {
+    const int64_t row = r + kk;
+    const bool rv = row < r1;
+    const double b = (rv && hi < k) ? __ldg(B + row * ldb + hi) : 0.0;
+#pragma unroll
+    for (int t = 0; t < 5; ++t) {
+      if (t >= mt) break;
+      const int col = 8 * t + hi;
+      const double a = (rv && col < m) ? __ldg(A + row * lda + col) : 0.0;
+      asm volatile("mma.sync.aligned.m8n8k4.row.col.f64.f64.f64.f64 {%0,%1}, {%2}, {%3}, {%0,%1};"
+                   : "+d"(c[t][0]), "+d"(c[t][1])
+                   : "d"(a), "d"(b));
+    }
+  }
+  double *pw = partial + warp * (int64_t)m * k;
+#pragma unroll
+  for (int t = 0; t < 5; ++t) {
+    if (t >= mt) break;
+    const int i = 8 * t + hi;
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      const int j = 2 * kk + q;
+      if (i < m && j < k) pw[i * k + j] = c[t][q];
+    }
+  }
+}
+
+}  // namespace
+
+extern "C" psoci_status psoci_tsprod(psoci_ctx *c, int method, int64_t n, const double *dA, int lda, int m,
+                                     const double *dB, int ldb, int k, double *dC) {
+  if (!c) return PSOCI_ERR_INVALID_ARG;
+  if (!dA || !dB || !dC || n < 1 || m < 1 || m > 40 || k < 1 || k > 8 || lda < m || ldb < k)
+    return psoci_fail(c, PSOCI_ERR_INVALID_ARG, "tsprod: sizes outside n >= 1, 1 <= m <= 40, 1 <= k <= 8");
+  if (method < 0 || method > 2) return psoci_fail(c, PSOCI_ERR_INVALID_ARG, "tsprod: method must be 0, 1 or 2");
+  PSOCI_CUDA(c, cudaSetDevice(c->device));
+  cudaStream_t st = c->stream;
+  psoci_status s;
+  if (method == 0) {
+    // the solver's own path (float-float k_tn + reduction)
+    Work w;
+    w.c = c;
+    w.N = n;
+    w.nblk = (int)std::min<int64_t>(std::max<int64_t>(1, (n + 255) / 256), 152 * 4);
+    w.rows_per_blk = (n + w.nblk - 1) / w.nblk;
+    if ((s = psoci_alloc(c, &w.partial, (size_t)w.nblk * MAX_SUB * TN_MAXK))) return s;
+    s = tn(w, dA, lda, 0, m, dB, ldb, 0, k, dC, k, 0);
+    if (s) return s;
+    PSOCI_CUDA(c, cudaStreamSynchronize(st));
+    return PSOCI_OK;
+  }
+  int nblk = 0;
+  int64_t per = 0;
+  if (method == 1) {
+    nblk = (int)std::min<int64_t>(std::max<int64_t>(1, (n + 255) / 256), 152 * 8);
+    per = (n + nblk - 1) / nblk;
+  } else {
+    const int64_t warps = std::min<int64_t>(std::max<int64_t>(1, (n + 255) / 256), 152 * 8 * (TP_THREADS / 32));
+    nblk = (int)warps;  // partial sums per warp
+    per = ((n + warps - 1) / warps + 3) / 4 * 4;
+  }
+  double *partial = nullptr;
+  if ((s = psoci_alloc(c, &partial, (size_t)nblk * m * k))) return s;
+  psoci_note_launch();
+  if (method == 1) {
+    k_tn_f64<<<nblk, TP_THREADS, 0, st>>>(n, dA, lda, m, dB, ldb, k, partial, per);
+  } else {
+    PSOCI_CUDA(c, cudaMemsetAsync(partial, 0, sizeof(double) * nblk * m * k, st));
+    k_tn_dmma<<<(unsigned)((nblk + TP_THREADS / 32 - 1) / (TP_THREADS / 32)), TP_THREADS, 0, st>>>(n, dA, lda, m, dB,
+                                                                                                  ldb, k, partial, per,
+                                                                                                  (int64_t)nblk);
+  }
+  psoci_note_launch();
+  k_reduce_partials<<<(m * k + 31) / 32, 256, 0, st>>>(partial, nblk, m, k, dC, k, 0);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  psoci_free(partial);
+  if (e != cudaSuccess) return psoci_cuda_fail(c, e, "tsprod");
+  return PSOCI_OK;
+}
