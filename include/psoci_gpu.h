@@ -181,7 +181,8 @@ PSOCI_API psoci_status psoci_sigma_mixed_noalloc(psoci_ctx *ctx, int k, const do
 
 typedef struct {
   int nroots;          /* roots wanted                                                  */
-  int max_subspace;    /* basis size that triggers a collapse (reference: 4*nroots)      */
+  int max_subspace;    /* basis size that triggers a collapse; 0: 8*nroots, at most 96  */
+                       /* (the reference collapses at 4*nroots)                          */
   int max_iter;        /* iteration limit (reference: 1000 per tolerance)                */
   double rtol;         /* residual-norm tolerance for convergence                        */
   psoci_prec prec;     /* sigma precision during the iterations                          */
