@@ -449,6 +449,9 @@ __device__ __forceinline__ void hi_bits(int code, int s, uint64_t (&e1)[W], uint
   if (kind == 2) set_bit_w<W>(e1, s + b);
 }
 
+// electrons of hi pattern code: 0, 1, 2, 2 for kinds 0-3
+__device__ __forceinline__ int hi_electrons(int code) { return min(code & 3, 2); }
+
 // Hi-pattern lists.  For d_hi(g, h) = 4 the lo patterns must be equal, so the pair is a
 // double excitation between the hi orbitals alone and whether its block survives the
 // integral test (double_block_kept) depends on (g, h) only — it is decided here once
@@ -515,15 +518,17 @@ __global__ void __launch_bounds__(256) k_join(Params P, JoinTabs J, int64_t *cnt
     uint64_t a1[W], a2[W];
 #pragma unroll
     for (int w = 0; w < W; ++w) { a1[w] = P.e1[i * W + w]; a2[w] = P.e2[i * W + w]; }
-    const int li = J.lid[i], js_i = P.jsym[i];
+    const int li = J.lid[i], js_i = P.jsym[i], gi = J.gid[i];
+    const int ne_i = hi_electrons(J.hdec[gi]);
     int64_t nk = 0, nc = 0;
     int64_t base = (MODE == 1) ? off[i] : 0;
     unsigned long long lstart = cursor;  // MODE 2: where this configuration's list begins
-    const int64_t gl0 = J.goff[J.gid[i]], gl1 = J.goff[J.gid[i] + 1];
+    const int64_t gl0 = J.goff[gi], gl1 = J.goff[gi + 1];
     for (int64_t h0 = gl0; h0 < gl1; h0 += 32) {
-      // this lane's hi pattern h: the lo patterns l' with d_lo <= 4 - d_hi, as a range of
-      // the neighbour list of l_i (or l_i alone when the hi patterns are disjoint: those
-      // blocks passed the integral test when the list was built)
+      // this lane's hi pattern h: the lo patterns l' with d_lo <= 4 - d_hi and the electron
+      // count that h leaves, as a range of the neighbour list of l_i (or l_i alone when the
+      // hi patterns are disjoint: those blocks passed the integral test when the list was
+      // built)
       int h = 0;
       int len = 0, q0 = 0, lp0 = li;
       if (h0 + lane < gl1) {
@@ -531,10 +536,12 @@ __global__ void __launch_bounds__(256) k_join(Params P, JoinTabs J, int64_t *cnt
         h = (int)(ent & 0x0fffffffu);
         const int d = (int)(ent >> 28);
         const int tau = 4 - d;
-        if (tau <= 0) { len = 1; q0 = -1; }
+        const int k = ne_i - hi_electrons(J.hdec[h]) + 2;  // lo electrons of l' minus l_i's, + 2
+        if (tau <= 0) { len = (k == 2); q0 = -1; }
         else {
-          q0 = J.lnoff[(tau - 1) * (J.L + 1) + li];
-          len = J.lnoff[(tau - 1) * (J.L + 1) + li + 1] - q0;
+          const int64_t at = (int64_t)(tau - 1) * (5 * (int64_t)J.L + 1) + 5 * (int64_t)li + k;
+          q0 = J.lnoff[at];
+          len = J.lnoff[at + 1] - q0;
         }
       }
       int incl = len;
@@ -2454,34 +2461,47 @@ psoci_status psoci_join_prepare(psoci_ctx *c) {
   for (int b = 0; b < nh; ++b)
     for (int a = 0; a <= b; ++a)
       hdec[1 + nh + (size_t)b * (b + 1) / 2 + a] = (a == b) ? (3 | (a << 8)) : (2 | (a << 8) | (b << 20));
-  // lo patterns within tau = 1..4 of each lo pattern (itself included), ascending; lists
-  // tau-major, then by pattern.  One distance per pair, counted then written in parallel.
-  std::vector<int32_t> lnoff(4 * (L + 1)), ln, lcnt((size_t)4 * L, 0);
+  // lo patterns within tau = 1..4 of each lo pattern (itself included), ascending inside
+  // each of five groups: the lo electron count minus l's, -2..2 (a hi pattern holds 0-2
+  // electrons, so a partner lo pattern differs by at most 2; the others never make a
+  // configuration and are left out).  Lists tau-major, then by pattern, then by group; one
+  // distance per pair, counted then written in parallel.
+  constexpr int NGRP = 5;
+  std::vector<int32_t> lnoff(4 * (NGRP * L + 1)), ln, lcnt((size_t)4 * NGRP * L, 0);
   psoci_parallel_ranges(L, [&](int64_t lo, int64_t hi, int) {
-    for (int64_t l = lo; l < hi; ++l)
+    for (int64_t l = lo; l < hi; ++l) {
+      const int nel = __builtin_popcount(lokey[l]);
       for (int64_t m = 0; m < L; ++m) {
+        const int k = __builtin_popcount(lokey[m]) - nel + 2;
+        if (k < 0 || k >= NGRP) continue;
         const int d = __builtin_popcount(lokey[l] ^ lokey[m]);
-        for (int tau = std::max(d, 1); tau <= 4; ++tau) ++lcnt[(size_t)(tau - 1) * L + l];
+        for (int tau = std::max(d, 1); tau <= 4; ++tau) ++lcnt[((size_t)(tau - 1) * L + l) * NGRP + k];
       }
+    }
   }, 64);
   {
     int64_t run = 0;
     for (int tau = 1; tau <= 4; ++tau) {
-      for (int64_t l = 0; l < L; ++l) {
-        lnoff[(tau - 1) * (L + 1) + l] = (int32_t)run;
-        run += lcnt[(size_t)(tau - 1) * L + l];
+      for (int64_t g = 0; g < NGRP * L; ++g) {
+        lnoff[(tau - 1) * (NGRP * L + 1) + g] = (int32_t)run;
+        run += lcnt[(size_t)(tau - 1) * NGRP * L + g];
       }
-      lnoff[(tau - 1) * (L + 1) + L] = (int32_t)run;
+      lnoff[(tau - 1) * (NGRP * L + 1) + NGRP * L] = (int32_t)run;
     }
+    if (run > INT32_MAX) return PSOCI_OK;
     ln.resize((size_t)run);
   }
   psoci_parallel_ranges(L, [&](int64_t lo, int64_t hi, int) {
     for (int64_t l = lo; l < hi; ++l) {
-      int32_t pos[4];
-      for (int tau = 1; tau <= 4; ++tau) pos[tau - 1] = lnoff[(tau - 1) * (L + 1) + l];
+      const int nel = __builtin_popcount(lokey[l]);
+      int32_t pos[4][NGRP];
+      for (int tau = 1; tau <= 4; ++tau)
+        for (int k = 0; k < NGRP; ++k) pos[tau - 1][k] = lnoff[(tau - 1) * (NGRP * L + 1) + NGRP * l + k];
       for (int64_t m = 0; m < L; ++m) {
+        const int k = __builtin_popcount(lokey[m]) - nel + 2;
+        if (k < 0 || k >= NGRP) continue;
         const int d = __builtin_popcount(lokey[l] ^ lokey[m]);
-        for (int tau = std::max(d, 1); tau <= 4; ++tau) ln[pos[tau - 1]++] = (int32_t)m;
+        for (int tau = std::max(d, 1); tau <= 4; ++tau) ln[pos[tau - 1][k]++] = (int32_t)m;
       }
     }
   }, 64);

@@ -62,7 +62,7 @@ struct psoci_ctx {
   int32_t *d_jgid = nullptr;    // [nconf] pattern id of the orbitals >= s
   int32_t *d_jlid = nullptr;    // [nconf] pattern id of the orbitals < s
   int32_t *d_jT = nullptr;      // [L*G] configuration of (lo pattern, hi pattern), or -1
-  int32_t *d_jlnoff = nullptr;  // [4*(L+1)] per distance tau = 1..4: offsets into d_jln
+  int32_t *d_jlnoff = nullptr;  // [4*(5L+1)] per distance tau = 1..4, lo pattern, electron difference -2..2: offsets into d_jln
   int32_t *d_jln = nullptr;     // lo patterns within tau of each lo pattern, ascending
   int32_t *d_jhdec = nullptr;   // [G] hi pattern: kind | a << 8 | b << 20
   uint32_t *d_jlokey = nullptr; // [L] lo pattern: e1 bits | e2 bits << s
