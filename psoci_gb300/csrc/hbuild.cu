@@ -104,6 +104,7 @@ struct Params {
   unsigned long long *slab_counter;
   int64_t slab_cap;
   double *slab_val;
+  uint64_t *cg;            // connectivity masks C[r] per (pair, row SEF), as prm (two-launch evaluation)
   const int64_t *rowptr;
   int32_t *col;
   double *val;
@@ -1270,7 +1271,9 @@ __device__ __forceinline__ bool det_connected(bool so, const uint64_t *aA, const
 
 // DIRECT (direct mode): segments over the full neighbour lists; instead of storing the kept
 // elements, Y[row, 0:kvec] += element * X[column, 0:kvec], added atomically per row.
-template <int W, int DIRECT = 0>
+// PH: 0 both phases in one launch; 2 phase 2 alone, from the connectivity masks that
+// k_hbuild_masks stored in P.cg (each launch then runs a smaller body).
+template <int W, int DIRECT = 0, int PH = 0>
 __global__ void __launch_bounds__(WARPS_PER_CTA * 32) k_hbuild_fast(Params P) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   FastSmem<W> *ws = reinterpret_cast<FastSmem<W> *>(smem_raw) + (threadIdx.x >> 5);
@@ -1310,7 +1313,7 @@ __global__ void __launch_bounds__(WARPS_PER_CTA * 32) k_hbuild_fast(Params P) {
     uint32_t Ap[FAST_MAXOPEN], Nk[FAST_MAXOPEN + 1];
     int sI[FAST_MAXOPEN];
     uint64_t occI[W];
-    {
+    if (PH != 2) {
       uint64_t SI[W];
 #pragma unroll
       for (int w = 0; w < W; ++w) {
@@ -1341,7 +1344,7 @@ __global__ void __launch_bounds__(WARPS_PER_CTA * 32) k_hbuild_fast(Params P) {
     // of SEF r and determinant y of SEF t can couple; the SEF element is marked when any can.
     uint64_t C[FAST_MAXSEF];
     for (int r = 0; r < FAST_MAXSEF; ++r) C[r] = 0ull;
-    if (lane < n) {
+    if (PH != 2 && lane < n) {
       const PairInfo &pi = ws->pi[lane];
       if (pi.kind != K_NONE) {
         const bool so = (pi.kind == K_SO);
@@ -1404,12 +1407,12 @@ __global__ void __launch_bounds__(WARPS_PER_CTA * 32) k_hbuild_fast(Params P) {
         }
       }
     }
+    const int64_t prbase = DIRECT ? 0 : P.pr_off[I] + (k0 - P.nbroff[I]) * nsefI;
     // phase 2, row by row: the marked elements of the row, in (neighbour, column) order, are
     // numbered e = 0..T-1 and lane e % 32 evaluates element e, so the lanes share the work
     // whatever the spread of marks over the neighbours.  Kept values are compacted in the
     // same order, so each row stays in ascending column order.  Each warp takes slab space
     // in chunks and advances through a chunk by the kept count of each row.
-    const int64_t prbase = DIRECT ? 0 : P.pr_off[I] + (k0 - P.nbroff[I]) * nsefI;
     const RowDets rowA = {ws->ra, ws->rb, ws->rph, ws->rna};  // I's determinants (A = I)
     // evaluation order of the neighbours: grouped by pair kind (doubles, singles, spin-orbit,
     // diagonal), ascending within a kind, so that neighbouring lanes mostly run the same
@@ -1431,7 +1434,8 @@ __global__ void __launch_bounds__(WARPS_PER_CTA * 32) k_hbuild_fast(Params P) {
     }
     const int src = ws->perm[lane];  // the neighbour lane at evaluation slot `lane`
     for (int r = 0; r < nsefI; ++r) {
-      const uint64_t cr = __shfl_sync(0xffffffffu, (lane < n) ? C[r] : 0ull, src);
+      const uint64_t cr = (PH == 2) ? ((src < n) ? __ldg(P.cg + prbase + (int64_t)src * nsefI + r) : 0ull)
+                                    : __shfl_sync(0xffffffffu, (lane < n) ? C[r] : 0ull, src);
       const uint32_t mr = (uint32_t)((cr | (cr >> 16) | (cr >> 32) | (cr >> 48)) & 0xffffull);
       const int cm = __popc(mr);
       int inclm = cm;
@@ -1548,6 +1552,186 @@ __global__ void __launch_bounds__(WARPS_PER_CTA * 32) k_hbuild_fast(Params P) {
       cursor += (unsigned long long)kc;
       __syncwarp();
     }
+    __syncwarp();
+  }
+}
+
+// Connectivity masks of the lower pairs for the two-launch evaluation: for every (pair, row
+// SEF r) the word C[r] of k_hbuild_fast's phase 1 (bit t + 16 (x << 1 | y): determinant x of
+// row SEF r and determinant y of column SEF t can couple), stored in P.cg at the pair's prm
+// index.  Pair kinds come from the excitation level and the symmetries alone, without the
+// integrals: a pair whose integrals vanish is marked all the same, and its elements then
+// evaluate to exactly zero and are not kept.  The work items, (neighbour, column SEF t), are
+// spread evenly over the lanes; an item tests t's one or two column determinants against all
+// row determinants at once (the bit-sliced counter of k_hbuild_fast) and ors the result into
+// the neighbour's words in shared memory.
+constexpr int MASK_WARPS = 8;
+struct MaskSmem {
+  uint64_t C[PSOCI_SEG][FAST_MAXSEF];
+  int64_t d0J[PSOCI_SEG];
+  int8_t nopJ[PSOCI_SEG], so[PSOCI_SEG];
+  int16_t ipre[PSOCI_SEG];
+};
+
+template <int W>
+__global__ void __launch_bounds__(MASK_WARPS * 32) k_hbuild_masks(Params P) {
+  __shared__ MaskSmem smem_masks[MASK_WARPS];
+  MaskSmem &ws = smem_masks[threadIdx.x >> 5];
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  const bool odd = P.nelec & 1;
+  for (int64_t s = warp; s < P.nseg; s += nwarps) {
+    const int I = P.seg_cfg[s];
+    const int64_t k0 = P.seg_k0[s];
+    const int n = P.seg_n[s];
+    const int nsefI = (int)(P.sefoff[I + 1] - P.sefoff[I]);
+    const int64_t d0I = P.detoff[I];
+    const int ndI = (int)(P.detoff[I + 1] - d0I);
+    const int nopI = P.nopen[I];
+    uint64_t occI[W], dblI[W];
+#pragma unroll
+    for (int w = 0; w < W; ++w) { occI[w] = P.e1[(int64_t)I * W + w]; dblI[w] = P.e2[(int64_t)I * W + w]; }
+    // this lane's neighbour J <= I: diagonal, single (spin-orbit when the symmetries differ)
+    // or double by the excitation level I -> J
+    int nit = 0;
+    if (lane < n) {
+      const int J = P.nbr[k0 + lane];
+      int ni = 0;
+#pragma unroll
+      for (int w = 0; w < W; ++w)
+        ni += __popcll(occI[w] & ~P.e1[(int64_t)J * W + w]) + __popcll(dblI[w] & ~P.e2[(int64_t)J * W + w]);
+      const bool diag = (J == I);
+      ws.so[lane] = (int8_t)(!diag && ni == 1 && P.jsym[I] != P.jsym[J]);
+      ws.d0J[lane] = P.detoff[J];
+      ws.nopJ[lane] = (int8_t)P.nopen[J];
+      nit = (diag || ni == 1 || ni == 2) ? (int)(P.sefoff[J + 1] - P.sefoff[J]) : 0;
+    }
+    for (int q = lane; q < PSOCI_SEG * FAST_MAXSEF; q += 32) (&ws.C[0][0])[q] = 0ull;
+    int incl = nit;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int v = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += v;
+    }
+    ws.ipre[lane] = (int16_t)(incl - nit);
+    const int NIT = __shfl_sync(0xffffffffu, incl, 31);
+    // I's open shells and, over the row determinants, the ballots of the counter
+    uint32_t Ap[FAST_MAXOPEN], Nk[FAST_MAXOPEN + 1];
+    int sI[FAST_MAXOPEN];
+    {
+      uint64_t SI[W];
+#pragma unroll
+      for (int w = 0; w < W; ++w) SI[w] = occI[w] & ~dblI[w];
+#pragma unroll
+      for (int p = 0; p < FAST_MAXOPEN; ++p) {
+        sI[p] = lowest_bit<W>(SI);
+        bool done = false;
+#pragma unroll
+        for (int w = 0; w < W; ++w)
+          if (!done && SI[w]) { SI[w] &= SI[w] - 1; done = true; }
+      }
+      uint32_t ma = 0u;
+      if (lane < ndI) {
+        uint64_t ra[W];
+#pragma unroll
+        for (int w = 0; w < W; ++w) ra[w] = P.alpha[(d0I + lane) * W + w];
+#pragma unroll
+        for (int p = 0; p < FAST_MAXOPEN; ++p)
+          if (p < nopI) ma |= (uint32_t)bit_w<W>(ra, sI[p]) << p;
+      }
+#pragma unroll
+      for (int p = 0; p < FAST_MAXOPEN; ++p) Ap[p] = __ballot_sync(0xffffffffu, (lane < ndI) && ((ma >> p) & 1u));
+#pragma unroll
+      for (int k = 0; k <= FAST_MAXOPEN; ++k) Nk[k] = __ballot_sync(0xffffffffu, (lane < ndI) && __popc(ma) == k);
+    }
+    const int ndblI = P.nelec - nopI;
+    const uint32_t rows_valid = (ndI >= 32) ? 0xffffffffu : ((1u << ndI) - 1u);
+    __syncwarp();
+    for (int i0 = 0; i0 < NIT; i0 += 32) {
+      const int it = i0 + lane;
+      if (it >= NIT) break;
+      int p = 0;  // the neighbour owning item it: last lane whose first item is <= it
+#pragma unroll
+      for (int step = 16; step > 0; step >>= 1)
+        if (ws.ipre[p + step] <= it) p += step;
+      const int t = it - ws.ipre[p];
+      const bool so = ws.so[p] != 0;
+      const int nopJ = ws.nopJ[p];
+      const int thr = so ? 1 : 2;
+      // column SEF t: determinant t (odd electron count), 2t and 2t + 1 (even, open shells)
+      // or the configuration's one determinant
+      const bool two = !odd && nopJ;
+      const int64_t b0 = ws.d0J[p] + (two ? 2 * t : t);
+      uint32_t okv[2] = {0u, 0u};
+#pragma unroll
+      for (int y = 0; y < 2; ++y) {
+        if (y == 1 && !two) break;
+        uint64_t ja[W], jb[W];
+#pragma unroll
+        for (int w = 0; w < W; ++w) { ja[w] = __ldg(P.alpha + (b0 + y) * W + w); jb[w] = __ldg(P.beta + (b0 + y) * W + w); }
+        int F = 0;
+#pragma unroll
+        for (int w = 0; w < W; ++w) F += __popcll(ja[w] & ~occI[w]) + __popcll(jb[w] & ~occI[w]);
+        if (F > thr) continue;
+        // saturating counter over the row dets: S0 (c'=0), S1, S2, S3 (>= 3)
+        uint32_t S0 = 0xffffffffu, S1 = 0u, S2 = 0u;
+#pragma unroll
+        for (int q = 0; q < FAST_MAXOPEN; ++q) {
+          if (q >= nopI) break;
+          const bool xa = bit_w<W>(ja, sI[q]), yb = bit_w<W>(jb, sI[q]);
+          if (xa) {  // mismatch where row det has beta on q
+            const uint32_t T = ~Ap[q];
+            S2 = (S2 & ~T) | (S1 & T);
+            S1 = (S1 & ~T) | (S0 & T);
+            S0 &= ~T;
+          }
+          if (yb) {  // mismatch where row det has alpha on q
+            const uint32_t T = Ap[q];
+            S2 = (S2 & ~T) | (S1 & T);
+            S1 = (S1 & ~T) | (S0 & T);
+            S0 &= ~T;
+          }
+        }
+        uint32_t ok = (thr - F >= 2) ? (S0 | S1 | S2) : (thr - F == 1) ? (S0 | S1) : S0;
+        ok &= rows_valid;
+        if (!so) {
+          int na = 0;
+#pragma unroll
+          for (int w = 0; w < W; ++w) na += __popcll(ja[w]);
+          const int need = na - (ndblI / 2);  // alpha open shells a row det needs for equal counts
+          uint32_t nk = 0u;
+#pragma unroll
+          for (int k = 0; k <= FAST_MAXOPEN; ++k)
+            if (k == need) nk = Nk[k];
+          ok &= (need >= 0 && need <= nopI) ? nk : 0u;
+        }
+        okv[y] = ok;
+      }
+      if (odd) {  // row SEF r = row det r, column SEF t = column det t
+        uint32_t rows = okv[0];
+        while (rows) {
+          const int r = __ffs(rows) - 1;
+          rows &= rows - 1;
+          atomicOr(reinterpret_cast<unsigned long long *>(&ws.C[p][r]), 1ull << t);
+        }
+      } else {  // row SEF r holds row dets 2r (x = 0) and 2r + 1 (x = 1)
+        uint32_t rows = (okv[0] | okv[1]);
+        rows = (rows | (rows >> 1)) & 0x55555555u;
+        while (rows) {
+          const int a = __ffs(rows) - 1;  // 2r
+          rows &= rows - 1;
+          const uint64_t wd = ((uint64_t)((okv[0] >> a) & 1u) << t) | ((uint64_t)((okv[1] >> a) & 1u) << (t + 16)) |
+                              ((uint64_t)((okv[0] >> (a + 1)) & 1u) << (t + 32)) |
+                              ((uint64_t)((okv[1] >> (a + 1)) & 1u) << (t + 48));
+          atomicOr(reinterpret_cast<unsigned long long *>(&ws.C[p][a >> 1]), (unsigned long long)wd);
+        }
+      }
+    }
+    __syncwarp();
+    // the words at the pairs' prm positions (pair-major, then row)
+    const int64_t prbase = P.pr_off[I] + (k0 - P.nbroff[I]) * nsefI;
+    for (int q = lane; q < n * nsefI; q += 32) P.cg[prbase + q] = ws.C[q / nsefI][q % nsefI];
     __syncwarp();
   }
 }
@@ -2006,6 +2190,7 @@ psoci_status run_build(psoci_ctx *c, psoci_hmode mode, int64_t *nnz_out) {
   int64_t *d_gcnt = nullptr, *d_goff = nullptr;
   uint32_t *d_glist = nullptr;
   uint32_t *d_prm = nullptr;
+  uint64_t *d_cg = nullptr;
   int *d_err = nullptr;
   unsigned long long *d_counter = nullptr;
   double *d_slabval = nullptr;
@@ -2019,7 +2204,7 @@ psoci_status run_build(psoci_ctx *c, psoci_hmode mode, int64_t *nnz_out) {
       if (e) cudaEventDestroy(e);
     psoci_free(d_soff); psoci_free(d_tot); psoci_free(d_segslot); psoci_free(d_counter);
     psoci_free(d_candoff); psoci_free(d_cand);
-    psoci_free(d_nlow); psoci_free(d_prrows); psoci_free(d_proff); psoci_free(d_mk); psoci_free(d_prm);
+    psoci_free(d_nlow); psoci_free(d_prrows); psoci_free(d_proff); psoci_free(d_mk); psoci_free(d_prm); psoci_free(d_cg);
     psoci_free(d_err); psoci_free(d_slabval); psoci_free(d_jslab); psoci_free(d_jstart);
     psoci_free(d_tpairs); psoci_free(d_dkept);
     psoci_free(d_gcnt); psoci_free(d_goff); psoci_free(d_glist);
@@ -2066,6 +2251,7 @@ psoci_status run_build(psoci_ctx *c, psoci_hmode mode, int64_t *nnz_out) {
   const bool direct = (mode == PSOCI_HMODE_DIRECT);
   const bool fast = !direct && c->max_ndet <= FAST_MAXDET;
   int64_t nprm = 0;
+  bool split = false;  // fast path: masks and elements in two launches
   if (fast) {
     TRY(psoci_alloc(c, &d_nlow, n + 1));
     TRY(psoci_alloc(c, &d_prrows, n + 1));
@@ -2134,9 +2320,19 @@ psoci_status run_build(psoci_ctx *c, psoci_hmode mode, int64_t *nnz_out) {
     // 3. evaluate the lower pairs once: kept values go to slab slots, masks to prm
     const size_t smem = sizeof(FastSmem<W>) * WARPS_PER_CTA;
     TRYC(cudaFuncSetAttribute(k_hbuild_fast<W>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    // two launches when the masks fit (8 bytes per (pair, row SEF), a quarter of the free
+    // memory at most): the connectivity masks (k_hbuild_masks), then the elements from them;
+    // otherwise both phases in one launch
+    size_t freeb = 0, totb = 0;
+    TRYC(cudaMemGetInfo(&freeb, &totb));
+    split = (double)nprm * 8.0 <= 0.25 * (double)freeb;
+    if (split) {
+      TRYC(cudaFuncSetAttribute(k_hbuild_fast<W, 0, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      TRY(psoci_alloc(c, &d_cg, nprm));
+      P.cg = d_cg;
+    }
     TRY(psoci_alloc(c, &d_segslot, nslots));
     TRY(psoci_alloc(c, &d_counter, 1));
-    size_t freeb = 0, totb = 0;
     TRYC(cudaMemGetInfo(&freeb, &totb));
     // slots hold the kept elements of the lower pairs plus the unused tails of the warps'
     // chunks; first guess from the pair count (observed up to 7 kept elements per lower
@@ -2156,8 +2352,15 @@ psoci_status run_build(psoci_ctx *c, psoci_hmode mode, int64_t *nnz_out) {
       TRYC(cudaMemsetAsync(d_counter, 0, sizeof(unsigned long long), st));
       P.seg_slot = d_segslot; P.slab_counter = d_counter; P.slab_cap = cap; P.slab_val = d_slabval;
       TRYC(cudaEventRecord(ev[2], st));
+      if (split && attempt == 0) {
+        const int mblocks = (int)std::max<int64_t>(1, std::min<int64_t>((nseg + MASK_WARPS - 1) / MASK_WARPS, 152 * 8));
+        psoci_note_launch();
+        k_hbuild_masks<W><<<mblocks, MASK_WARPS * 32, 0, st>>>(P);
+        TRYC(cudaGetLastError());
+      }
       psoci_note_launch();
-      k_hbuild_fast<W><<<hb_blocks, WARPS_PER_CTA * 32, smem, st>>>(P);
+      if (split) k_hbuild_fast<W, 0, 2><<<hb_blocks, WARPS_PER_CTA * 32, smem, st>>>(P);
+      else k_hbuild_fast<W><<<hb_blocks, WARPS_PER_CTA * 32, smem, st>>>(P);
       TRYC(cudaGetLastError());
       TRYC(cudaEventRecord(ev[3], st));
       ++evaluations;
@@ -2172,6 +2375,7 @@ psoci_status run_build(psoci_ctx *c, psoci_hmode mode, int64_t *nnz_out) {
       cap = nlower + tails;  // chunk tails differ from run to run
       if (attempt == 1) TRY(psoci_fail(c, PSOCI_ERR_NOMEM, "H build: element slab overflow"));
     }
+    psoci_free(d_cg);  // the masks are done with
     t_d = tnow();
     // 4. full row lengths (lower counts + mirrored columns) and offsets
     TRY(psoci_alloc(c, &d_rownnz, N + 1));
@@ -2240,9 +2444,10 @@ psoci_status run_build(psoci_ctx *c, psoci_hmode mode, int64_t *nnz_out) {
   if (c->verbose) {
     auto d = [](auto a, auto b) { return std::chrono::duration<double>(b - a).count(); };
     fprintf(stderr,
-            "psoci: H build phases (%s kernel, %s screen): screen %.4f s, segments %.4f s, evaluate %.4f s, "
+            "psoci: H build phases (%s kernel%s, %s screen): screen %.4f s, segments %.4f s, evaluate %.4f s, "
             "offsets %.4f s, fill/copy %.4f s\n",
-            fast ? "fast" : "generic", nsplit ? "all-pairs" : "lookup", d(t_a, t_b), d(t_b, t_c), d(t_c, t_d),
+            fast ? "fast" : "generic", split ? ", masks launched apart" : "", nsplit ? "all-pairs" : "lookup",
+            d(t_a, t_b), d(t_b, t_c), d(t_c, t_d),
             d(t_d, t_e), d(t_e, t_f));
   }
   {
