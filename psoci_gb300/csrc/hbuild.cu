@@ -54,14 +54,12 @@ constexpr int MAXK = 1 + PSOCI_MAX_OPEN * (PSOCI_MAX_OPEN - 1) / 2;  // diagonal
 struct PairInfo {
   int64_t detA, detB;   // first determinant of A, B
   int64_t colbase;      // first SEF of the neighbour J
-  int A, B;             // configurations in the reference's roles (A = "iconf")
   int kind, swap;       // swap: J > I, element (t, r) of block (J, I)
-  int iex0, iex1, jex0, jex1; // excitation orbitals of A -> B (ascending, with multiplicity)
+  int iex0, jex0;       // single excitations: the orbital A -> B
   int nopenA, nopenB, jsA, jsB, nsefJ;
   double v0, v1;
   double X[PSOCI_MAX_OPEN];  // single: (iex0 s|s jex0) over the open shells s of A
-  uint64_t SA[PSOCI_MAX_WORDS];
-  uint64_t SB[PSOCI_MAX_WORDS];  // open shells of B
+  uint64_t SA[PSOCI_MAX_WORDS];  // open shells of A
   // orbital ranges the determinant phases count electrons over, fixed for the pair:
   //   K_DOUBLE: 0-3 strictly between ex_i and jy_j (index 2i + j), 4 between ex0 and ex1,
   //             5 between jy0 and jy1;
@@ -742,7 +740,7 @@ __device__ __forceinline__ void two_positions(const uint64_t (&m1)[W], const uin
 // J is the configuration whose SEFs are the CSR columns.
 template <int W>
 __device__ void pair_setup_ab(const Params &P, int A, int B, int J, int swap, PairInfo &pi, double *Kd) {
-  pi.A = A; pi.B = B; pi.swap = swap;
+  pi.swap = swap;
   pi.detA = P.detoff[A]; pi.detB = P.detoff[B];
   pi.colbase = P.sefoff[J];
   pi.nsefJ = (int)(P.sefoff[J + 1] - P.sefoff[J]);
@@ -756,10 +754,9 @@ __device__ void pair_setup_ab(const Params &P, int A, int B, int J, int swap, Pa
     im1[w] = e1A[w] & ~e1B[w]; im2[w] = e2A[w] & ~e2B[w];
     jm1[w] = e1B[w] & ~e1A[w]; jm2[w] = e2B[w] & ~e2A[w];
     pi.SA[w] = e1A[w] & ~e2A[w];
-    pi.SB[w] = e1B[w] & ~e2B[w];
   }
   pi.v0 = 0.0; pi.v1 = 0.0;
-  pi.iex0 = pi.iex1 = pi.jex0 = pi.jex1 = -1;
+  pi.iex0 = pi.jex0 = -1;
   int ni = popc_w<W>(im1) + popc_w<W>(im2);
   if (A == B) {
     pi.kind = K_DIAG;
@@ -865,7 +862,7 @@ __device__ void pair_setup_ab(const Params &P, int A, int B, int J, int swap, Pa
     two_positions<W>(im1, im2, ex0, ex1);
     two_positions<W>(jm1, jm2, jy0, jy1);
     const int ex[2] = {ex0, ex1}, jy[2] = {jy0, jy1};
-    pi.iex0 = ex0; pi.iex1 = ex1; pi.jex0 = jy0; pi.jex1 = jy1;
+    pi.iex0 = ex0; pi.jex0 = jy0;
     between_mask<W>(ex0, jy0, pi.bm[0]);
     between_mask<W>(ex0, jy1, pi.bm[1]);
     between_mask<W>(ex1, jy0, pi.bm[2]);
@@ -1241,20 +1238,23 @@ constexpr int FAST_MAXDET = 32;
 constexpr int FAST_MAXSEF = 16;
 constexpr int FAST_MAXOPEN = 6;  // 2^(6-1) = 32 determinants
 constexpr int SLAB_CHUNK = 4096; // slab slots a warp takes at a time
+constexpr int FAST_ROWS = 4;     // rows of a configuration evaluated together
+constexpr int FAST_MAXK = 1 + FAST_MAXOPEN * (FAST_MAXOPEN - 1) / 2;  // diagonal list, <= 6 open shells
 
 __device__ __forceinline__ bool tbit(const uint64_t *x, int p) { return (x[p >> 6] >> (p & 63)) & 1ull; }
 
 template <int W>
 struct FastSmem {
   PairInfo pi[PSOCI_SEG];
-  double K[MAXK];
+  double K[FAST_MAXK];
   uint64_t ra[FAST_MAXDET * W], rb[FAST_MAXDET * W];
   uint8_t rna[FAST_MAXDET], rph[FAST_MAXDET];
-  // phase 2, per row: marked columns of each neighbour, their exclusive prefix, kept columns
-  uint32_t mrow[PSOCI_SEG];
-  int pre[PSOCI_SEG];
-  uint32_t keep[PSOCI_SEG];
-  uint64_t cm[PSOCI_SEG];  // connectivity of the row's marked elements (see below)
+  // phase 2, per row of a group: connectivity of the marked elements of each slot (see
+  // below; the marked columns are its four 16-bit quarters or-ed), their exclusive prefix,
+  // kept columns of each neighbour
+  uint64_t cm[FAST_ROWS][PSOCI_SEG];
+  int16_t pre[FAST_ROWS][PSOCI_SEG];
+  uint32_t keep[FAST_ROWS][PSOCI_SEG];
   int8_t perm[PSOCI_SEG];  // evaluation order: slot -> neighbour lane, grouped by pair kind
 };
 
@@ -1408,11 +1408,14 @@ __global__ void __launch_bounds__(WARPS_PER_CTA * 32) k_hbuild_fast(Params P) {
       }
     }
     const int64_t prbase = DIRECT ? 0 : P.pr_off[I] + (k0 - P.nbroff[I]) * nsefI;
-    // phase 2, row by row: the marked elements of the row, in (neighbour, column) order, are
+    // phase 2, FAST_ROWS rows at a time (one row in the direct modes, whose sums are per
+    // row): the marked elements of the group's rows, in (row, neighbour, column) order, are
     // numbered e = 0..T-1 and lane e % 32 evaluates element e, so the lanes share the work
-    // whatever the spread of marks over the neighbours.  Kept values are compacted in the
-    // same order, so each row stays in ascending column order.  Each warp takes slab space
-    // in chunks and advances through a chunk by the kept count of each row.
+    // whatever the spread of marks over the neighbours and rows (a row holds about one
+    // warp's worth of marks: taken alone, its last pass would run on few lanes).  Kept values
+    // are compacted in the same order, so each row's values form one run in ascending column
+    // order and the runs of a group follow one another.  Each warp takes slab space in chunks
+    // and advances through a chunk by the kept count of each group.
     const RowDets rowA = {ws->ra, ws->rb, ws->rph, ws->rna};  // I's determinants (A = I)
     // evaluation order of the neighbours: grouped by pair kind (doubles, singles, spin-orbit,
     // diagonal), ascending within a kind, so that neighbouring lanes mostly run the same
@@ -1433,23 +1436,33 @@ __global__ void __launch_bounds__(WARPS_PER_CTA * 32) k_hbuild_fast(Params P) {
       __syncwarp();
     }
     const int src = ws->perm[lane];  // the neighbour lane at evaluation slot `lane`
-    for (int r = 0; r < nsefI; ++r) {
-      const uint64_t cr = (PH == 2) ? ((src < n) ? __ldg(P.cg + prbase + (int64_t)src * nsefI + r) : 0ull)
-                                    : __shfl_sync(0xffffffffu, (lane < n) ? C[r] : 0ull, src);
-      const uint32_t mr = (uint32_t)((cr | (cr >> 16) | (cr >> 32) | (cr >> 48)) & 0xffffull);
-      const int cm = __popc(mr);
-      int inclm = cm;
+    constexpr int R = DIRECT ? 1 : FAST_ROWS;
+    for (int r0 = 0; r0 < nsefI; r0 += R) {
+      const int nr = min(R, nsefI - r0);
+      // per row g of the group: marked columns of each slot, their exclusive prefix counted
+      // from the group's first element, and rs[g], the row's first element
+      int T = 0, rs[R];
 #pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        const int v = __shfl_up_sync(0xffffffffu, inclm, o);
-        if (lane >= o) inclm += v;
+      for (int g = 0; g < R; ++g) {
+        rs[g] = T;
+        if (g < nr) {
+          const uint64_t cr = (PH == 2) ? ((src < n) ? __ldg(P.cg + prbase + (int64_t)src * nsefI + r0 + g) : 0ull)
+                                        : __shfl_sync(0xffffffffu, (lane < n) ? C[r0 + g] : 0ull, src);
+          const uint32_t mr = (uint32_t)((cr | (cr >> 16) | (cr >> 32) | (cr >> 48)) & 0xffffull);
+          const int cm = __popc(mr);
+          int inclm = cm;
+#pragma unroll
+          for (int o = 1; o < 32; o <<= 1) {
+            const int v = __shfl_up_sync(0xffffffffu, inclm, o);
+            if (lane >= o) inclm += v;
+          }
+          ws->pre[g][lane] = (int16_t)(T + inclm - cm);
+          ws->cm[g][lane] = cr;
+          ws->keep[g][lane] = 0u;
+          T += __shfl_sync(0xffffffffu, inclm, 31);
+        }
       }
-      const int T = __shfl_sync(0xffffffffu, inclm, 31);
-      ws->pre[lane] = inclm - cm;
-      ws->mrow[lane] = mr;
-      ws->cm[lane] = cr;
-      ws->keep[lane] = 0u;
-      if (!DIRECT && cursor + T > chunk_end) {  // room for every marked element of the row
+      if (!DIRECT && cursor + T > chunk_end) {  // room for every marked element of the group
         const unsigned long long len = (unsigned long long)max(T, SLAB_CHUNK);
         unsigned long long b = 0;
         if (lane == 0) b = atomicAdd(P.slab_counter, len);
@@ -1471,19 +1484,24 @@ __global__ void __launch_bounds__(WARPS_PER_CTA * 32) k_hbuild_fast(Params P) {
         bool keep = false;
         double v = 0.0;
         if (e < T) {
+          int g = 0;  // the row of element e: last row whose first element is <= e
+#pragma unroll
+          for (int k = 1; k < R; ++k) g += (rs[k] <= e);
+          const int r = r0 + g;
           int o = 0;  // the slot owning element e: last slot whose prefix is <= e
 #pragma unroll
           for (int step = 16; step > 0; step >>= 1)
-            if (ws->pre[o + step] <= e) o += step;
-          uint32_t m = ws->mrow[o];
-          for (int q = e - ws->pre[o]; q > 0; --q) m &= m - 1;
+            if (ws->pre[g][o + step] <= e) o += step;
+          const uint64_t cw = ws->cm[g][o];
+          uint32_t m = (uint32_t)((cw | (cw >> 16) | (cw >> 32) | (cw >> 48)) & 0xffffull);
+          for (int q = e - ws->pre[g][o]; q > 0; --q) m &= m - 1;
           const int t = __ffs(m) - 1;
           const int pl = ws->perm[o];  // its neighbour lane
           const PairInfo &pi = ws->pi[pl];
           // reference roles: the lower half of a diagonal block, block (J, I) for J > I
           const bool diag_blk = (pi.kind == K_DIAG);
           const bool flip = diag_blk ? (t > r) : (pi.swap != 0);
-          const uint64_t co = ws->cm[o] >> t;
+          const uint64_t co = cw >> t;
           unsigned conn = (unsigned)((co & 1ull) | ((co >> 15) & 2ull) | ((co >> 30) & 4ull) | ((co >> 45) & 8ull));
           // a diagonal block is symmetric: the transposed element swaps the determinant roles
           if (flip) conn = (conn & 9u) | ((conn & 2u) << 1) | ((conn & 4u) >> 1);
@@ -1512,7 +1530,7 @@ __global__ void __launch_bounds__(WARPS_PER_CTA * 32) k_hbuild_fast(Params P) {
                 if (q < P.kvec) acc[q] = fma(v, xr[q], acc[q]);
             }
           } else if (keep) {
-            atomicOr(&ws->keep[pl], 1u << t);
+            atomicOr(&ws->keep[g][pl], 1u << t);
           }
         }
         if (!DIRECT) {
@@ -1521,34 +1539,40 @@ __global__ void __launch_bounds__(WARPS_PER_CTA * 32) k_hbuild_fast(Params P) {
           kc += __popc(kb);
         }
       }
-      if (DIRECT) {
+      if (DIRECT) {  // one row per group
         if (DIRECT == 2) {
 #pragma unroll
           for (int q = 0; q < 8; ++q) acc[q] = (double)accs[q] - (double)accc[q];
         }
         const double tot = reduce_scatter8_f64(acc, lane);
         const int q = lane >> 2;
-        if ((lane & 3) == 0 && q < P.kvec && tot != 0.0) atomicAdd(P.dy + (P.sefoff[I] + r) * P.ldy + q, tot);
+        if ((lane & 3) == 0 && q < P.kvec && tot != 0.0) atomicAdd(P.dy + (P.sefoff[I] + r0) * P.ldy + q, tot);
         __syncwarp();
         continue;
       }
       __syncwarp();
-      const uint32_t keepm = (lane < n) ? ws->keep[lane] : 0u;
-      // offsets in the row run follow the evaluation order
-      const int cs = __popc(__shfl_sync(0xffffffffu, keepm, src));
-      int incl = cs;
+      // per row of the group: its kept count, its run's place in the slab, and each pair's
+      // offset in the run (kept columns before it, in the evaluation order)
+      unsigned long long run = base;
+      for (int g = 0; g < nr; ++g) {
+        const uint32_t keepm = (lane < n) ? ws->keep[g][lane] : 0u;
+        const int cs = __popc(__shfl_sync(0xffffffffu, keepm, src));
+        int incl = cs;
 #pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        const int v = __shfl_up_sync(0xffffffffu, incl, o);
-        if (lane >= o) incl += v;
+        for (int o = 1; o < 32; o <<= 1) {
+          const int v = __shfl_up_sync(0xffffffffu, incl, o);
+          if (lane >= o) incl += v;
+        }
+        const int kg = __shfl_sync(0xffffffffu, incl, 31);
+        ws->pre[g][src] = (int16_t)(incl - cs);  // the element loop is done with pre
+        __syncwarp();
+        if (lane == 0) {
+          P.seg_cnt[P.seg_rowoff[s] + r0 + g] = kg;
+          P.seg_slot[P.seg_rowoff[s] + r0 + g] = (int64_t)run;
+        }
+        if (lane < n) P.prm[prbase + (int64_t)lane * nsefI + r0 + g] = keepm | ((uint32_t)ws->pre[g][lane] << 16);
+        run += (unsigned long long)kg;
       }
-      ws->pre[src] = incl - cs;  // the element loop is done with pre
-      __syncwarp();
-      if (lane == 0) {
-        P.seg_cnt[P.seg_rowoff[s] + r] = kc;
-        P.seg_slot[P.seg_rowoff[s] + r] = (int64_t)base;
-      }
-      if (lane < n) P.prm[prbase + (int64_t)lane * nsefI + r] = keepm | ((uint32_t)ws->pre[lane] << 16);
       cursor += (unsigned long long)kc;
       __syncwarp();
     }
