@@ -97,8 +97,8 @@ struct Params {
   const int64_t *segoff;   // first segment of each configuration
   const int64_t *nlow;     // neighbours J <= I
   const int64_t *pr_off;   // first (pair, row) mask of each configuration
-  uint32_t *prm;           // bits 0-15: kept column SEFs t; bits 16-31: offset in the slot
-  int64_t *seg_slot;       // slab position of each (segment, row)
+  uint64_t *prm;           // bits 0-15: kept column SEFs t; bits 16-63: slab position of the first
+                           // of them (the pair's values in the row run follow one another)
   unsigned long long *slab_counter;
   int64_t slab_cap;
   double *slab_val;
@@ -1566,11 +1566,10 @@ __global__ void __launch_bounds__(WARPS_PER_CTA * 32) k_hbuild_fast(Params P) {
         const int kg = __shfl_sync(0xffffffffu, incl, 31);
         ws->pre[g][src] = (int16_t)(incl - cs);  // the element loop is done with pre
         __syncwarp();
-        if (lane == 0) {
-          P.seg_cnt[P.seg_rowoff[s] + r0 + g] = kg;
-          P.seg_slot[P.seg_rowoff[s] + r0 + g] = (int64_t)run;
-        }
-        if (lane < n) P.prm[prbase + (int64_t)lane * nsefI + r0 + g] = keepm | ((uint32_t)ws->pre[g][lane] << 16);
+        if (lane == 0) P.seg_cnt[P.seg_rowoff[s] + r0 + g] = kg;
+        if (lane < n)
+          P.prm[prbase + (int64_t)lane * nsefI + r0 + g] =
+              (uint64_t)keepm | ((uint64_t)(run + (unsigned long long)ws->pre[g][lane]) << 16);
         run += (unsigned long long)kg;
       }
       cursor += (unsigned long long)kc;
@@ -1794,9 +1793,9 @@ __global__ void k_mirror_count(Params P, int64_t *row_nnz, int32_t *mk, int *err
       }
       mk[b0 + k] = (int32_t)(lo - jb);
       const int nsefJ = (int)(P.sefoff[J + 1] - P.sefoff[J]);
-      const uint32_t *pm = P.prm + P.pr_off[J] + (lo - jb) * nsefJ;
+      const uint64_t *pm = P.prm + P.pr_off[J] + (lo - jb) * nsefJ;
       for (int t = 0; t < nsefJ; ++t) {
-        const uint32_t m = pm[t];
+        const uint32_t m = (uint32_t)pm[t];
 #pragma unroll
         for (int r = 0; r < FAST_MAXSEF; ++r) up[r] += (int)((m >> r) & 1u);
       }
@@ -1820,11 +1819,13 @@ __global__ void k_mirror_count(Params P, int64_t *row_nnz, int32_t *mk, int *err
 constexpr int ASM_THREADS = 256;
 __global__ void __launch_bounds__(ASM_THREADS) k_assemble(Params P, const int32_t *mk) {
   __shared__ int s_off[ASM_THREADS / 32][33];     // per lane: first entry of the lane in the row
-  __shared__ int s_soff[ASM_THREADS / 32][32];    // per lane: its first value in the slab run
+  __shared__ int s_soff[ASM_THREADS / 32][32];    // lower part: per row, its first entry in the segment
   __shared__ uint32_t s_msk[ASM_THREADS / 32][32];  // per lane: columns t of the run, as bits
   __shared__ int32_t s_J[ASM_THREADS / 32][32];
-  __shared__ int64_t s_col[ASM_THREADS / 32][32], s_rs[ASM_THREADS / 32][32];
-  __shared__ uint32_t s_mm[ASM_THREADS / 32][32][FAST_MAXSEF];
+  __shared__ int64_t s_col[ASM_THREADS / 32][32];
+  __shared__ uint64_t s_mm[ASM_THREADS / 32][32][FAST_MAXSEF];  // mask words (prm)
+  __shared__ int16_t s_ro[ASM_THREADS / 32][FAST_MAXSEF][32];  // lower part: per row, first entry of each slot
+  __shared__ int64_t s_dst[ASM_THREADS / 32][FAST_MAXSEF];      // lower part: per row, its write position
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
@@ -1834,7 +1835,9 @@ __global__ void __launch_bounds__(ASM_THREADS) k_assemble(Params P, const int32_
     const int64_t b0 = P.nbroff[I], nl = P.nlow[I], nn = P.nbroff[I + 1] - b0;
     int64_t mypos = (lane < nsefI) ? P.rowptr[row0 + lane] : 0;
     // lower pairs, segment by segment: the run of (segment, row r) is contiguous in the slab
-    // and in row r, in the same order
+    // and in row r, in the same order.  The segment's runs and mask words are loaded first;
+    // then its entries, all rows together, are numbered in (row, neighbour, column) order
+    // and spread evenly over the lanes.
     for (int64_t sg = P.segoff[I]; sg < P.segoff[I + 1]; ++sg) {
       const int64_t k0 = P.seg_k0[sg];
       const int ns = P.seg_n[sg];
@@ -1843,68 +1846,86 @@ __global__ void __launch_bounds__(ASM_THREADS) k_assemble(Params P, const int32_
         s_J[wib][lane] = J;
         s_col[wib][lane] = P.sefoff[J];
       }
-      const uint32_t *pm = P.prm + P.pr_off[I] + (k0 - b0 + lane) * nsefI;
+      // mask words of (neighbour o, row r): contiguous in prm, pair-major
+      const uint64_t *pm = P.prm + P.pr_off[I] + (k0 - b0) * nsefI;
+      for (int q = lane; q < ns * nsefI; q += 32) s_mm[wib][q / nsefI][q % nsefI] = pm[q];
+      // row r (lane r): its entry count and its first entry in the segment
+      int cnt = 0;
+      if (lane < nsefI) {
+        cnt = (int)P.seg_cnt[P.seg_rowoff[sg] + lane];
+        s_dst[wib][lane] = mypos;
+      }
+      int rincl = cnt;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int v = __shfl_up_sync(0xffffffffu, rincl, o);
+        if (lane >= o) rincl += v;
+      }
+      const int T = __shfl_sync(0xffffffffu, rincl, 31);
+      s_soff[wib][lane] = rincl - cnt;
+      __syncwarp();
+      // per row, the first entry of each neighbour: the row takes the pairs in neighbour
+      // order; the slab run holds them in the evaluation order, each where its prm word says
       for (int r = 0; r < nsefI; ++r) {
-        const int64_t slot = P.seg_rowoff[sg] + r;
-        const int cnt = (int)P.seg_cnt[slot];
-        const int64_t src0 = P.seg_slot[slot];
-        const int64_t dst = __shfl_sync(0xffffffffu, mypos, r);
-        // the row takes the pairs in neighbour order; the slab run holds them in the
-        // evaluation order, each pair at its prm offset
-        const uint32_t w = (lane < ns) ? pm[r] : 0u;
-        const int cl = __popc(w & 0xffffu);
+        const int cl = (lane < ns) ? __popc(s_mm[wib][lane][r] & 0xffffu) : 0;
         int incl = cl;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
           const int v = __shfl_up_sync(0xffffffffu, incl, o);
           if (lane >= o) incl += v;
         }
-        s_off[wib][lane] = incl - cl;
-        s_soff[wib][lane] = (int)(w >> 16);
-        s_msk[wib][lane] = w & 0xffffu;
-        __syncwarp();
-        for (int e = lane; e < cnt; e += 32) {
-          int o = 0;
-#pragma unroll
-          for (int st = 16; st > 0; st >>= 1)
-            if (o + st < 32 && s_off[wib][o + st] <= e) o += st;
-          uint32_t m = s_msk[wib][o];
-          for (int q = e - s_off[wib][o]; q > 0; --q) m &= m - 1;
-          const int t = __ffs(m) - 1;
-          const double v = P.slab_val[src0 + s_soff[wib][o] + (e - s_off[wib][o])];
-          P.col[dst + e] = (int32_t)(s_col[wib][o] + t);
-          P.val[dst + e] = v;
-          if (P.val32) P.val32[dst + e] = (float)v;
-          if (s_J[wib][o] == (int)I && t == r) P.diag[row0 + r] = v;
-        }
-        __syncwarp();
-        if (lane == r) mypos += cnt;
+        s_ro[wib][r][lane] = (int16_t)(incl - cl);
       }
+      __syncwarp();
+      for (int e = lane; e < T; e += 32) {
+        int r = 0;  // the row of entry e: last row whose first entry is <= e
+#pragma unroll
+        for (int st = 8; st > 0; st >>= 1)
+          if (r + st < nsefI && s_soff[wib][r + st] <= e) r += st;
+        const int el = e - s_soff[wib][r];
+        int o = 0;  // its neighbour: last slot whose first entry in the row is <= el
+#pragma unroll
+        for (int st = 16; st > 0; st >>= 1)
+          if (o + st < 32 && s_ro[wib][r][o + st] <= el) o += st;
+        const uint64_t w = s_mm[wib][o][r];
+        const int k = el - s_ro[wib][r][o];
+        uint32_t m = (uint32_t)w & 0xffffu;
+        for (int q = k; q > 0; --q) m &= m - 1;
+        const int t = __ffs(m) - 1;
+        const double v = P.slab_val[(int64_t)(w >> 16) + k];
+        const int64_t dst = s_dst[wib][r] + el;
+        P.col[dst] = (int32_t)(s_col[wib][o] + t);
+        P.val[dst] = v;
+        if (P.val32) P.val32[dst] = (float)v;
+        if (s_J[wib][o] == (int)I && t == r) P.diag[row0 + r] = v;
+      }
+      __syncwarp();
+      mypos += cnt;
     }
     // upper neighbours, 32 at a time: column r of their lower block (J, I)
     for (int64_t kc = nl; kc < nn; kc += 32) {
       const int64_t k = kc + lane;
-      uint32_t mm[FAST_MAXSEF];
+      uint32_t mm[FAST_MAXSEF];  // kept-column masks of the block's rows t
 #pragma unroll
       for (int t = 0; t < FAST_MAXSEF; ++t) mm[t] = 0u;
-      int64_t colJ = 0, rowslotJ = 0;
+      int64_t colJ = 0;
       if (k < nn) {
         const int J = P.nbr[b0 + k];
         const int kk = mk[b0 + k];
         if (kk >= 0) {
           const int nsefJ = (int)(P.sefoff[J + 1] - P.sefoff[J]);
           colJ = P.sefoff[J];
-          rowslotJ = P.seg_rowoff[P.segoff[J] + kk / PSOCI_SEG];
-          const uint32_t *pm = P.prm + P.pr_off[J] + (int64_t)kk * nsefJ;
+          const uint64_t *pm = P.prm + P.pr_off[J] + (int64_t)kk * nsefJ;
 #pragma unroll
           for (int t = 0; t < FAST_MAXSEF; ++t)
-            if (t < nsefJ) mm[t] = pm[t];
+            if (t < nsefJ) {
+              const uint64_t w = pm[t];
+              s_mm[wib][lane][t] = w;
+              mm[t] = (uint32_t)w & 0xffffu;
+            }
         }
       }
-#pragma unroll
-      for (int t = 0; t < FAST_MAXSEF; ++t) s_mm[wib][lane][t] = mm[t];
       s_col[wib][lane] = colJ;
-      s_rs[wib][lane] = rowslotJ;
       for (int r = 0; r < nsefI; ++r) {
         uint32_t cm = 0u;  // columns t of this lane's block whose row t keeps column r
 #pragma unroll
@@ -1930,8 +1951,8 @@ __global__ void __launch_bounds__(ASM_THREADS) k_assemble(Params P, const int32_
           uint32_t m = s_msk[wib][o];
           for (int q = e - s_off[wib][o]; q > 0; --q) m &= m - 1;
           const int t = __ffs(m) - 1;
-          const uint32_t wt = s_mm[wib][o][t];
-          const double v = P.slab_val[P.seg_slot[s_rs[wib][o] + t] + (wt >> 16) + __popc(wt & below)];
+          const uint64_t wt = s_mm[wib][o][t];
+          const double v = P.slab_val[(int64_t)(wt >> 16) + __popc((uint32_t)wt & below)];
           P.col[dst + e] = (int32_t)(s_col[wib][o] + t);
           P.val[dst + e] = v;
           if (P.val32) P.val32[dst + e] = (float)v;
@@ -2208,12 +2229,12 @@ psoci_status run_build(psoci_ctx *c, psoci_hmode mode, int64_t *nnz_out) {
   int64_t *d_cnt = nullptr, *d_nbroff = nullptr, *d_nseg = nullptr, *d_nrow = nullptr, *d_segoff = nullptr,
           *d_rowslot = nullptr, *d_segk0 = nullptr, *d_segrow = nullptr, *d_segcnt = nullptr, *d_rownnz = nullptr;
   int32_t *d_nbr = nullptr, *d_segcfg = nullptr, *d_segn = nullptr;
-  int64_t *d_soff = nullptr, *d_tot = nullptr, *d_segslot = nullptr, *d_candoff = nullptr;
+  int64_t *d_soff = nullptr, *d_tot = nullptr, *d_candoff = nullptr;
   int64_t *d_nlow = nullptr, *d_prrows = nullptr, *d_proff = nullptr;
   int32_t *d_cand = nullptr, *d_mk = nullptr;
   int64_t *d_gcnt = nullptr, *d_goff = nullptr;
   uint32_t *d_glist = nullptr;
-  uint32_t *d_prm = nullptr;
+  uint64_t *d_prm = nullptr;
   uint64_t *d_cg = nullptr;
   int *d_err = nullptr;
   unsigned long long *d_counter = nullptr;
@@ -2226,7 +2247,7 @@ psoci_status run_build(psoci_ctx *c, psoci_hmode mode, int64_t *nnz_out) {
   auto cleanup = [&]() {
     for (auto &e : ev)
       if (e) cudaEventDestroy(e);
-    psoci_free(d_soff); psoci_free(d_tot); psoci_free(d_segslot); psoci_free(d_counter);
+    psoci_free(d_soff); psoci_free(d_tot); psoci_free(d_counter);
     psoci_free(d_candoff); psoci_free(d_cand);
     psoci_free(d_nlow); psoci_free(d_prrows); psoci_free(d_proff); psoci_free(d_mk); psoci_free(d_prm); psoci_free(d_cg);
     psoci_free(d_err); psoci_free(d_slabval); psoci_free(d_jslab); psoci_free(d_jstart);
@@ -2355,7 +2376,6 @@ psoci_status run_build(psoci_ctx *c, psoci_hmode mode, int64_t *nnz_out) {
       TRY(psoci_alloc(c, &d_cg, nprm));
       P.cg = d_cg;
     }
-    TRY(psoci_alloc(c, &d_segslot, nslots));
     TRY(psoci_alloc(c, &d_counter, 1));
     TRYC(cudaMemGetInfo(&freeb, &totb));
     // slots hold the kept elements of the lower pairs plus the unused tails of the warps'
@@ -2374,7 +2394,7 @@ psoci_status run_build(psoci_ctx *c, psoci_hmode mode, int64_t *nnz_out) {
         fprintf(stderr, "psoci: H build slab allocation %.4f s (%lld slots)\n",
                 std::chrono::duration<double>(std::chrono::steady_clock::now() - t_al).count(), (long long)cap);
       TRYC(cudaMemsetAsync(d_counter, 0, sizeof(unsigned long long), st));
-      P.seg_slot = d_segslot; P.slab_counter = d_counter; P.slab_cap = cap; P.slab_val = d_slabval;
+      P.slab_counter = d_counter; P.slab_cap = cap; P.slab_val = d_slabval;
       TRYC(cudaEventRecord(ev[2], st));
       if (split && attempt == 0) {
         const int mblocks = (int)std::max<int64_t>(1, std::min<int64_t>((nseg + MASK_WARPS - 1) / MASK_WARPS, 152 * 8));
