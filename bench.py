@@ -379,7 +379,7 @@ def run_ours(args):
             "h_build_ms": {k: round(bs[k], 3) for k in ("screen_ms", "evaluate_ms", "rows_ms", "assemble_ms",
                                                          "total_ms")},
             "h_build_counts": {k: int(bs[k]) for k in ("candidates", "pairs", "segments", "nnz", "nnz_lower",
-                                                        "slab_slots", "evaluations")},
+                                                        "slab_slots", "evaluations", "eval_launches")},
             "energy_gradient": grad,
             "projection_methods": tsprod,
             "density1": {"s": round(den_s, 6), "first_call_s": round(den_first, 6), "roots": NROOTS,

@@ -131,10 +131,17 @@ typedef struct {
   int evaluations;       /* 1, or 2 after a slab overflow                                    */
   int fast;              /* 1: lower blocks evaluated once and mirrored; 0: generic path      */
   int lookup_screen;     /* 1: neighbours found by table lookup; 0: all-pairs test            */
-  int reserved;
+  int eval_launches;     /* fast path: 2 masks and elements launched apart, 1 one launch;    */
+                         /* 0 otherwise                                                     */
   double screen_ms, evaluate_ms, rows_ms, assemble_ms, total_ms;
 } psoci_build_info;
 PSOCI_API psoci_status psoci_build_stats(const psoci_ctx *ctx, psoci_build_info *info);
+/* The fast build evaluates its elements in two launches (the determinant-connectivity masks,
+ * 8 bytes per (pair, row SEF), then the elements) when those masks fit in a quarter of the
+ * free device memory, else in one launch.  launches = 1 asks for the one-launch form (less
+ * memory, slower), 0 for the automatic choice (the default).  The stored matrix is the same
+ * bit for bit either way.  No counterpart in the reference (a GPU scheduling choice). */
+PSOCI_API psoci_status psoci_set_eval_launches(psoci_ctx *ctx, int launches);
 
 /* Replaces PsociHamiltonian::generateSOCIblocks (PsociHamiltonian.C:401-558) for a batch of
  * configuration pairs: block q is the reference's nsef_A x nsef_B sefsef matrix for

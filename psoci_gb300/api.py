@@ -44,7 +44,7 @@ class BuildInfo(ctypes.Structure):
     _fields_ = [("candidates", ctypes.c_int64), ("pairs", ctypes.c_int64), ("segments", ctypes.c_int64),
                 ("nnz", ctypes.c_int64), ("nnz_lower", ctypes.c_int64), ("slab_slots", ctypes.c_int64),
                 ("evaluations", ctypes.c_int), ("fast", ctypes.c_int), ("lookup_screen", ctypes.c_int),
-                ("reserved", ctypes.c_int),
+                ("eval_launches", ctypes.c_int),
                 ("screen_ms", ctypes.c_double), ("evaluate_ms", ctypes.c_double), ("rows_ms", ctypes.c_double),
                 ("assemble_ms", ctypes.c_double), ("total_ms", ctypes.c_double)]
 
@@ -97,6 +97,7 @@ SIGNATURES = {
     "psoci_tsprod": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int64, ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
                                     ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p]),
     "psoci_autotune_sigma": (ctypes.c_int, [_P, ctypes.c_int, _IP, ctypes.POINTER(ctypes.c_float)]),
+    "psoci_set_eval_launches": (ctypes.c_int, [_P, ctypes.c_int]),
     "psoci_davidson_batch": (ctypes.c_int, [ctypes.POINTER(_P), ctypes.c_int, ctypes.POINTER(DavOpts),
                                             ctypes.POINTER(_DP), ctypes.POINTER(_DP), ctypes.POINTER(_DP),
                                             ctypes.POINTER(DavStats), _IP]),
@@ -350,6 +351,10 @@ class Context:
         t = (ctypes.c_float * 6)()
         self._check(self.lib.psoci_autotune_sigma(self.ctx, k, ctypes.byref(ch), t), "autotune_sigma")
         return ch.value, [float(x) for x in t]
+
+    def set_eval_launches(self, launches: int):
+        """1: evaluate the H build's elements in one launch; 0: automatic (two when they fit)."""
+        self._check(self.lib.psoci_set_eval_launches(self.ctx, launches), "set_eval_launches")
 
     def set_sigma_variant(self, v: int):
         """Install mixed-sigma variant v (0..5) without timing."""

@@ -439,6 +439,14 @@ psoci_status psoci_davidson(psoci_ctx *c, const psoci_dav_opts *opts, double *ev
   return psoci_davidson_impl(c, opts, evals, evecs, rnorms, stats);
 }
 
+psoci_status psoci_set_eval_launches(psoci_ctx *c, int launches) {
+  if (!c) return PSOCI_ERR_INVALID_ARG;
+  if (launches != 0 && launches != 1)
+    return psoci_fail(c, PSOCI_ERR_INVALID_ARG, "psoci_set_eval_launches: launches must be 0 or 1");
+  c->eval_launches = launches;
+  return PSOCI_OK;
+}
+
 psoci_status psoci_autotune_sigma(psoci_ctx *c, int k, int *choice, float *times_ms) {
   if (!c) return PSOCI_ERR_INVALID_ARG;
   psoci_status s;

@@ -2370,7 +2370,7 @@ psoci_status run_build(psoci_ctx *c, psoci_hmode mode, int64_t *nnz_out) {
     // otherwise both phases in one launch
     size_t freeb = 0, totb = 0;
     TRYC(cudaMemGetInfo(&freeb, &totb));
-    split = (double)nprm * 8.0 <= 0.25 * (double)freeb;
+    split = c->eval_launches != 1 && (double)nprm * 8.0 <= 0.25 * (double)freeb;
     if (split) {
       TRYC(cudaFuncSetAttribute(k_hbuild_fast<W, 0, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
       TRY(psoci_alloc(c, &d_cg, nprm));
@@ -2500,6 +2500,7 @@ psoci_status run_build(psoci_ctx *c, psoci_hmode mode, int64_t *nnz_out) {
     b.candidates = ncand; b.pairs = npairs; b.segments = nseg; b.nnz = nnz; b.nnz_lower = direct ? 0 : (nnz + N) / 2;
     b.slab_slots = slab_used; b.evaluations = evaluations; b.fast = fast ? 1 : 0;
     b.lookup_screen = c->join_ok ? 1 : 0;
+    b.eval_launches = fast ? (split ? 2 : 1) : 0;
     float ms = 0.f;
     if (cudaEventElapsedTime(&ms, ev[0], ev[1]) == cudaSuccess) b.screen_ms = ms;
     if (cudaEventElapsedTime(&ms, ev[2], ev[3]) == cudaSuccess) b.evaluate_ms = ms;

@@ -31,6 +31,7 @@ struct DevBuf {
 struct psoci_ctx {
   int device = 0;
   int verbose = 0;
+  int eval_launches = 0;  // 0: automatic; 1: the element evaluation in one launch
   cudaStream_t stream = nullptr;
   std::string err;
   // released device blocks kept for reuse (size -> pointer), see psoci_alloc

@@ -94,6 +94,31 @@ def test_mrci_lookup_screen(oracle_mod, kind, kw, ksym):
     assert c.build_stats()["lookup_screen"] == 1
 
 
+@pytest.mark.parametrize("name", ["fci_6e8o", "mrcis_6e8o_v40"])
+def test_one_launch_evaluation_matches_two(name):
+    """The element evaluation in two launches (connectivity masks, then elements; the default
+    when they fit) and in one launch (the fallback for short memory) store the same matrix,
+    bit for bit, with the mixed FP32 copy."""
+    from psoci_gb300.inputs import named_workload
+
+    p = small_problem(name, 1) if name == "fci_6e8o" else named_workload(name, seed=0, ksym=1)
+    c = _ctx(p)
+    c.build_hamiltonian(mixed=True)
+    assert c.build_stats()["eval_launches"] == 2
+    two = c.get_hamiltonian()
+    c.set_eval_launches(1)
+    c.build_hamiltonian(mixed=True)
+    assert c.build_stats()["eval_launches"] == 1
+    one = c.get_hamiltonian()
+    for a, b in zip(two, one):
+        assert a.shape == b.shape and np.array_equal(a, b)
+    c.set_eval_launches(0)
+    c.build_hamiltonian(mixed=True)
+    assert c.build_stats()["eval_launches"] == 2
+    with pytest.raises(Exception):
+        c.set_eval_launches(3)
+
+
 def test_fci_takes_all_pairs_screen(oracle_mod):
     p = small_problem("fci_6e8o", 1)
     c = _ctx(p)
