@@ -508,17 +508,22 @@ template <int W, int MODE>
 __global__ void __launch_bounds__(256) k_join(Params P, JoinTabs J, int64_t *cnt, int64_t *ncand, const int64_t *off,
                                               JoinSlab S) {
   __shared__ int s_pre[8][33], s_q0[8][32], s_lp[8][32], s_h[8][32];
+  __shared__ uint32_t s_hx[8][32];  // per hi pattern: its part of the excitation from i (see below)
+  __shared__ int s_hn[8][32];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
   const uint32_t lomask = (1u << J.s) - 1u;
   unsigned long long cursor = 0, chunk_end = 0;  // MODE 2: this warp's slab chunk
   for (int64_t i = warp; i < P.nconf; i += nwarps) {
-    uint64_t a1[W], a2[W];
-#pragma unroll
-    for (int w = 0; w < W; ++w) { a1[w] = P.e1[i * W + w]; a2[w] = P.e2[i * W + w]; }
     const int li = J.lid[i], js_i = P.jsym[i], gi = J.gid[i];
     const int ne_i = hi_electrons(J.hdec[gi]);
+    // the excitation i -> j splits into its lo part (orbitals < s, from the two lo keys) and
+    // its hi part (from the two hi patterns, once per hi pattern); orbitals ascend, so the lo
+    // orbitals come first in each list
+    uint64_t g1[W], g2[W];
+    hi_bits<W>(J.hdec[gi], J.s, g1, g2);
+    const uint32_t keyi = J.lokey[li], e1i = keyi & lomask, e2i = keyi >> J.s;
     int64_t nk = 0, nc = 0;
     int64_t base = (MODE == 1) ? off[i] : 0;
     unsigned long long lstart = cursor;  // MODE 2: where this configuration's list begins
@@ -535,12 +540,21 @@ __global__ void __launch_bounds__(256) k_join(Params P, JoinTabs J, int64_t *cnt
         h = (int)(ent & 0x0fffffffu);
         const int d = (int)(ent >> 28);
         const int tau = 4 - d;
-        const int k = ne_i - hi_electrons(J.hdec[h]) + 2;  // lo electrons of l' minus l_i's, + 2
+        const int code = J.hdec[h];
+        const int k = ne_i - hi_electrons(code) + 2;  // lo electrons of l' minus l_i's, + 2
         if (tau <= 0) { len = (k == 2); q0 = -1; }
         else {
           const int64_t at = (int64_t)(tau - 1) * (5 * (int64_t)J.L + 1) + 5 * (int64_t)li + k;
           q0 = J.lnoff[at];
           len = J.lnoff[at + 1] - q0;
+          // hi part: the electrons leaving g_i (the first two, ascending, with multiplicity)
+          // and their count, the first two arriving in h; 8 bits per orbital
+          uint64_t b1[W], b2[W];
+          hi_bits<W>(code, J.s, b1, b2);
+          int x0, x1, y0, y1;
+          s_hn[wib][lane] = excitation_r<W>(g1, g2, b1, b2, x0, x1, y0, y1);
+          s_hx[wib][lane] = (uint32_t)(x0 & 0xff) | ((uint32_t)(x1 & 0xff) << 8) | ((uint32_t)(y0 & 0xff) << 16) |
+                            ((uint32_t)(y1 & 0xff) << 24);
         }
       }
       int incl = len;
@@ -572,14 +586,23 @@ __global__ void __launch_bounds__(256) k_join(Params P, JoinTabs J, int64_t *cnt
             found = true;
             keep = true;
             if (j != (int)i && qo >= 0) {
-              uint64_t b1[W], b2[W];
-              hi_bits<W>(J.hdec[ho], J.s, b1, b2);
-              const uint32_t key = J.lokey[lp];
-              b1[0] |= key & lomask;
-              b2[0] |= key >> J.s;
+              // lo part from the keys (bit q: orbital q occupied; bit s + q: doubly)
+              const uint32_t key = J.lokey[lp], e1j = key & lomask, e2j = key >> J.s;
+              const uint32_t i1 = e1i & ~e1j, i2 = e2i & ~e2j, j1 = e1j & ~e1i, j2 = e2j & ~e2i;
+              const int lni = __popc(i1) + __popc(i2), lnj = __popc(j1) + __popc(j2);
+              const int ni = lni + s_hn[wib][o];
+              const uint32_t hx = s_hx[wib][o];
+              const int hx0 = (int)(hx & 0xffu), hx1 = (int)((hx >> 8) & 0xffu);
+              const int hy0 = (int)((hx >> 16) & 0xffu), hy1 = (int)(hx >> 24);
+              // first two orbitals of each list: lo ones (a doubly emptied / filled orbital
+              // twice), then hi ones
+              const int la0 = __ffs(i1 | i2) - 1, lb0 = __ffs(j1 | j2) - 1;
+              const int la1 = (lni < 2) ? -1 : ((i1 & i2) >> la0) & 1u ? la0 : __ffs((i1 | i2) & ~(1u << la0)) - 1;
+              const int lb1 = (lnj < 2) ? -1 : ((j1 & j2) >> lb0) & 1u ? lb0 : __ffs((j1 | j2) & ~(1u << lb0)) - 1;
+              const int ex0 = (lni >= 1) ? la0 : hx0, jy0 = (lnj >= 1) ? lb0 : hy0;
+              const int ex1 = (lni >= 2) ? la1 : (lni == 1) ? hx0 : hx1;
+              const int jy1 = (lnj >= 2) ? lb1 : (lnj == 1) ? hy0 : hy1;
               // the tests below are symmetric in the two configurations' roles
-              int ex0, ex1, jy0, jy1;
-              const int ni = excitation_r<W>(a1, a2, b1, b2, ex0, ex1, jy0, jy1);
               if (ni == 2) {
                 const int64_t e = ((int64_t)ex1 * (ex1 + 1) / 2 + ex0) * J.nt + (int64_t)jy1 * (jy1 + 1) / 2 + jy0;
                 keep = (__ldg(J.dkept + (e >> 5)) >> (e & 31)) & 1u;
