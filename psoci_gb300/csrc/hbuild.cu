@@ -85,6 +85,7 @@ struct Params {
   // screen
   const int64_t *nbroff;
   int32_t *nbr;
+  int64_t nbr_len;         // entries of nbr
   // segments
   int64_t nseg;
   const int32_t *seg_cfg;
@@ -1788,7 +1789,15 @@ __global__ void __launch_bounds__(MASK_WARPS * 32) k_hbuild_masks(Params P) {
 // mask bit r is set in the (J, I) pair's rows t.  mk[k] is the position of I in J's list.
 //
 // One warp per configuration: row lengths, and I's position in each upper neighbour's list.
-__global__ void k_mirror_count(Params P, int64_t *row_nnz, int32_t *mk, int *err) {
+constexpr int NBR_SKIP = 16;  // one skip-table entry per 16 neighbour-list entries
+
+// skip[q] = nbr[16 q]: the first entry of every 64-byte block of the neighbour lists
+__global__ void k_nbr_skip(int64_t nq, const int32_t *__restrict__ nbr, int32_t *__restrict__ skip) {
+  for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < nq; q += (int64_t)gridDim.x * blockDim.x)
+    skip[q] = nbr[q * NBR_SKIP];
+}
+
+__global__ void k_mirror_count(Params P, const int32_t *__restrict__ skip, int64_t *row_nnz, int32_t *mk, int *err) {
   const int lane = threadIdx.x & 31;
   const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
@@ -1804,12 +1813,34 @@ __global__ void k_mirror_count(Params P, int64_t *row_nnz, int32_t *mk, int *err
     for (int64_t k = nl + lane; k < nn; k += 32) {
       const int J = P.nbr[b0 + k];
       const int64_t jb = P.nbroff[J], je = jb + P.nlow[J];
-      int64_t lo = jb, hi = je;
-      while (lo < hi) {  // first entry >= I
-        const int64_t mid = (lo + hi) >> 1;
-        if (P.nbr[mid] < (int32_t)I) lo = mid + 1; else hi = mid;
+      // I in J's lower list [jb, je) (ascending): the last 16-entry block starting inside
+      // the list whose first entry is <= I, by binary search over the skip table (small
+      // enough to stay in L2), then a scan of that block (64 bytes)
+      int64_t qa = jb / NBR_SKIP, qb = (je - 1) / NBR_SKIP;  // blocks qa + 1 .. qb start inside
+      while (qa < qb) {
+        const int64_t mid = (qa + qb + 1) >> 1;
+        if (__ldg(skip + mid) <= (int32_t)I) qa = mid; else qb = mid - 1;
       }
-      if (lo >= je || P.nbr[lo] != (int32_t)I) {
+      int64_t lo = -1;
+      const int64_t b16 = qa * NBR_SKIP;
+      if (b16 + NBR_SKIP <= P.nbr_len) {  // the block as four 16-byte loads, compared in registers
+        const int4 *blk = reinterpret_cast<const int4 *>(P.nbr + b16);
+        int4 v[NBR_SKIP / 4];
+#pragma unroll
+        for (int u = 0; u < NBR_SKIP / 4; ++u) v[u] = __ldg(blk + u);
+#pragma unroll
+        for (int u = 0; u < NBR_SKIP / 4; ++u) {
+          const int64_t p = b16 + 4 * u;
+          if (v[u].x == (int32_t)I && p >= jb && p < je) lo = p;
+          if (v[u].y == (int32_t)I && p + 1 >= jb && p + 1 < je) lo = p + 1;
+          if (v[u].z == (int32_t)I && p + 2 >= jb && p + 2 < je) lo = p + 2;
+          if (v[u].w == (int32_t)I && p + 3 >= jb && p + 3 < je) lo = p + 3;
+        }
+      } else {  // the last, partial block of the lists
+        for (int64_t p = max(jb, b16); p < je && p < b16 + NBR_SKIP; ++p)
+          if (P.nbr[p] == (int32_t)I) lo = p;
+      }
+      if (lo < 0) {
         atomicExch(err, 1);
         mk[b0 + k] = -1;
         continue;
@@ -2254,7 +2285,7 @@ psoci_status run_build(psoci_ctx *c, psoci_hmode mode, int64_t *nnz_out) {
   int32_t *d_nbr = nullptr, *d_segcfg = nullptr, *d_segn = nullptr;
   int64_t *d_soff = nullptr, *d_tot = nullptr, *d_candoff = nullptr;
   int64_t *d_nlow = nullptr, *d_prrows = nullptr, *d_proff = nullptr;
-  int32_t *d_cand = nullptr, *d_mk = nullptr;
+  int32_t *d_cand = nullptr, *d_mk = nullptr, *d_skip = nullptr;
   int64_t *d_gcnt = nullptr, *d_goff = nullptr;
   uint32_t *d_glist = nullptr;
   uint64_t *d_prm = nullptr;
@@ -2271,7 +2302,7 @@ psoci_status run_build(psoci_ctx *c, psoci_hmode mode, int64_t *nnz_out) {
     for (auto &e : ev)
       if (e) cudaEventDestroy(e);
     psoci_free(d_soff); psoci_free(d_tot); psoci_free(d_counter);
-    psoci_free(d_candoff); psoci_free(d_cand);
+    psoci_free(d_candoff); psoci_free(d_cand); psoci_free(d_skip);
     psoci_free(d_nlow); psoci_free(d_prrows); psoci_free(d_proff); psoci_free(d_mk); psoci_free(d_prm); psoci_free(d_cg);
     psoci_free(d_err); psoci_free(d_slabval); psoci_free(d_jslab); psoci_free(d_jstart);
     psoci_free(d_tpairs); psoci_free(d_dkept);
@@ -2450,8 +2481,14 @@ psoci_status run_build(psoci_ctx *c, psoci_hmode mode, int64_t *nnz_out) {
     TRY(psoci_alloc(c, &d_err, 1));
     TRYC(cudaMemsetAsync(d_err, 0, sizeof(int), st));
     const int cfg_blocks = (int)std::max<int64_t>(1, std::min<int64_t>(((int64_t)n * 32 + 255) / 256, 152 * 32));
+    const int64_t nq = (npairs + NBR_SKIP - 1) / NBR_SKIP;
+    P.nbr_len = npairs;
+    TRY(psoci_alloc(c, &d_skip, nq));
     psoci_note_launch();
-    k_mirror_count<<<cfg_blocks, 256, 0, st>>>(P, d_rownnz, d_mk, d_err);
+    k_nbr_skip<<<(int)std::min<int64_t>((nq + 255) / 256, 152 * 16), 256, 0, st>>>(nq, d_nbr, d_skip);
+    TRYC(cudaGetLastError());
+    psoci_note_launch();
+    k_mirror_count<<<cfg_blocks, 256, 0, st>>>(P, d_skip, d_rownnz, d_mk, d_err);
     TRYC(cudaGetLastError());
     int herr = 0;
     TRYC(cudaMemcpyAsync(&herr, d_err, sizeof(int), cudaMemcpyDeviceToHost, st));
