@@ -1282,17 +1282,6 @@ struct FastSmem {
   int8_t perm[PSOCI_SEG];  // evaluation order: slot -> neighbour lane, grouped by pair kind
 };
 
-// may det (aA, bA) of A and det (aB, bB) of B have a non-zero element?
-template <int W>
-__device__ __forceinline__ bool det_connected(bool so, const uint64_t *aA, const uint64_t *bA, int naA,
-                                              const uint64_t *aB, const uint64_t *bB, int naB) {
-  int ua = 0, ub = 0;
-#pragma unroll
-  for (int w = 0; w < W; ++w) { ua += __popcll(aB[w] & ~aA[w]); ub += __popcll(bB[w] & ~bA[w]); }
-  if (so) return ua <= 1 && ua + ub <= 1;
-  return naA == naB && ua + ub <= 2;
-}
-
 // DIRECT (direct mode): segments over the full neighbour lists; instead of storing the kept
 // elements, Y[row, 0:kvec] += element * X[column, 0:kvec], added atomically per row.
 // PH: 0 both phases in one launch; 2 phase 2 alone, from the connectivity masks that
@@ -1331,7 +1320,7 @@ __global__ void __launch_bounds__(WARPS_PER_CTA * 32) k_hbuild_fast(Params P) {
     //   c(a) = F + #{p in x : p not in m_a} + #{p in y : p in m_a}
     // spin-orbitals of b, where x, y are b's alpha / beta patterns on I's open shells and F
     // counts b's electrons in orbitals empty in I.  Non-spin-orbit pairs need c(a) <= 2 and
-    // equal alpha counts, spin-orbit pairs c(a) <= 1 (det_connected's test).  The sets
+    // equal alpha counts, spin-orbit pairs c(a) <= 1 (the tests det_elem starts with).  The sets
     // {a : p in m_a} and {a : |m_a| = k} are warp ballots; c(a) is kept as a saturating
     // bit-sliced counter over all row dets at once.
     uint32_t Ap[FAST_MAXOPEN], Nk[FAST_MAXOPEN + 1];
