@@ -36,6 +36,8 @@ def main(argv=None):
     ap.add_argument("--density", action="store_true", help="1-particle densities of the roots")
     ap.add_argument("--gradient", action="store_true", help="energy gradients of the roots")
     ap.add_argument("--direct", action="store_true", help="direct mode: no stored elements")
+    ap.add_argument("--eval-launches", type=int, default=0, choices=(0, 1),
+                    help="1: the H build's element evaluation in one launch (default 0: two when they fit)")
     ap.add_argument("--max-subspace", type=int, default=48)
     ap.add_argument("--device", type=int, default=0)
     ap.add_argument("--verbose", type=int, default=0)
@@ -44,6 +46,7 @@ def main(argv=None):
     mixed = not a.fp64
     with api.Context(a.device, verbose=a.verbose) as c:
         c.load_problem(p)
+        c.set_eval_launches(a.eval_launches)
         t0 = time.perf_counter()
         c.build_determinants()
         nnz = c.build_hamiltonian(mixed=mixed, direct=a.direct)
