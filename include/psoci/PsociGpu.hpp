@@ -208,6 +208,11 @@ class PsociGAhamiltonian {
     check(dev_.get(), psoci_build_hamiltonian(dev_.get(), PSOCI_HMODE_DIRECT, &nnz_), "psoci_build_hamiltonian");
   }
   int64_t numberNonzeroElements() const { return nnz_; }
+  // the build's element evaluation in one launch (launches = 1: less memory, slower; the
+  // same matrix) or the automatic choice (0); no reference counterpart
+  void setEvalLaunches(int launches) {
+    check(dev_.get(), psoci_set_eval_launches(dev_.get(), launches), "psoci_set_eval_launches");
+  }
   // constructCIdensityAltOrbMapChunkJmap (PsociGAhamiltonian.C:11570-11760): density[root] is
   // the packed nbf(nbf+1)/2 spin-free 1-particle density of root-major vectors vecs (k x N)
   int64_t constructCIdensityAltOrbMapChunkJmap(int numRoots, const std::vector<double> &vecs, int nbf,
